@@ -1,0 +1,110 @@
+// extern "C" entry points of libpbte_gb300: argument checks, then the
+// launchers.  Every call is asynchronous on the caller's stream.
+#include <cuda_runtime.h>
+
+#include "pbte_internal.cuh"
+
+namespace {
+inline cudaStream_t S(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+}  // namespace
+
+extern "C" {
+
+const char *pbte_version(void) { return "pbte_gb300 1.0 (sm_103a)"; }
+
+int pbte_sweep(pbte_ctx *c, const double *ts, const double *qxs, const double *qys, double *vdf,
+               const double *flux_wall, const double *pbuf, int use_pbuf, void *stream) {
+    if (!c || !ts || !qxs || !qys || !vdf) return PBTE_ERR_ARG;
+    if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
+    if (use_pbuf && !pbuf) return PBTE_ERR_ARG;
+    // Source iteration over periodic faces reads the partner "as of its place
+    // in the reference element order"; only the explicit-state form (pbuf) is
+    // implemented here.
+    if (c->has_periodic && !use_pbuf) return PBTE_ERR_UNSUPPORTED;
+    int rc = pbte::launch_sources(c, ts, qxs, qys, false, S(stream));
+    if (rc) return rc;
+    return pbte::launch_sweep64(c, vdf, flux_wall, pbuf, use_pbuf, S(stream));
+}
+
+int pbte_sweep_f32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys, float *vdf32,
+                   const double *flux_wall, double wall_scale, void *stream) {
+    if (!c || !ts || !qxs || !qys || !vdf32) return PBTE_ERR_ARG;
+    if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
+    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
+    int rc = pbte::launch_sources(c, ts, qxs, qys, true, S(stream));
+    if (rc) return rc;
+    return pbte::launch_sweep32(c, vdf32, flux_wall, wall_scale, S(stream));
+}
+
+int pbte_moments(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys, double *temp,
+                 double *qx, double *qy, void *stream) {
+    if (!c || !vdf || !ts || !qxs || !qys || !temp || !qx || !qy) return PBTE_ERR_ARG;
+    return pbte::launch_moments64(c, vdf, ts, qxs, qys, temp, qx, qy, S(stream));
+}
+
+int pbte_moments_f32(pbte_ctx *c, const float *vdf32, double *ts, double *qxs, double *qys, double *temp,
+                     double *qx, double *qy, void *stream) {
+    if (!c || !vdf32 || !ts || !qxs || !qys || !temp || !qx || !qy) return PBTE_ERR_ARG;
+    return pbte::launch_moments32(c, vdf32, ts, qxs, qys, temp, qx, qy, S(stream));
+}
+
+int pbte_wall_flux(pbte_ctx *c, const double *vdf, double *flux_wall, void *stream) {
+    if (!c || !vdf || (c->n_wall_ad && !flux_wall)) return PBTE_ERR_ARG;
+    return pbte::launch_wall_flux64(c, vdf, flux_wall, S(stream));
+}
+
+int pbte_wall_flux_f32(pbte_ctx *c, const float *vdf32, double *flux_wall, void *stream) {
+    if (!c || !vdf32 || (c->n_wall_ad && !flux_wall)) return PBTE_ERR_ARG;
+    return pbte::launch_wall_flux32(c, vdf32, flux_wall, S(stream));
+}
+
+int pbte_residual_iterate(pbte_ctx *c, const double *temp, double *t_old, double *out, void *stream) {
+    if (!c || !temp || !t_old || !out) return PBTE_ERR_ARG;
+    return pbte::launch_residual(c, temp, t_old, out, S(stream));
+}
+
+int pbte_set_done_flag(pbte_ctx *c, const int32_t *done) {
+    if (!c) return PBTE_ERR_ARG;
+    c->done = done;
+    return PBTE_OK;
+}
+
+int pbte_residual_check(pbte_ctx *c, const double *res, double tol, int64_t tmax, int32_t *done,
+                        int64_t *count, double *hist, int64_t hist_cap, void *stream) {
+    if (!c || !res || !done || !count || hist_cap < 0) return PBTE_ERR_ARG;
+    return pbte::launch_residual_check(c, res, tol, tmax, done, count, hist, hist_cap, S(stream));
+}
+
+int pbte_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                            const double *vdf, const double *flux_wall, const double *pbuf, double *num,
+                            double *den, void *stream) {
+    if (!c || !ts || !qxs || !qys || !vdf || !num || !den) return PBTE_ERR_ARG;
+    if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
+    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
+    return pbte::launch_transport_residual(c, ts, qxs, qys, vdf, flux_wall, pbuf, num, den, S(stream));
+}
+
+int pbte_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, void *stream) {
+    if (!c || !vdf || !work) return PBTE_ERR_ARG;
+    return pbte::launch_hot_source(c, vdf, tc5, work, S(stream));
+}
+
+int pbte_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int32_t nk, const int32_t *tri_list,
+                    const int32_t *lfc_list, double *out, void *stream) {
+    if (!c || !vdf || nk < 0 || (nk && (!tri_fc_fc || !tri_list || !lfc_list || !out))) return PBTE_ERR_ARG;
+    return pbte::launch_wall_trace(c, vdf, tri_fc_fc, nk, tri_list, lfc_list, out, S(stream));
+}
+
+int pbte_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_hmin, double tau_thr,
+                 int use_hmin, double *ts, double *qxs, double *qys, double *temp, double *qx, double *qy,
+                 void *stream) {
+    if (!c || !vdf || !uq || !tri_hmin || !ts || !qxs || !qys || !temp || !qx || !qy) return PBTE_ERR_ARG;
+    return pbte::launch_correct(c, vdf, uq, tri_hmin, tau_thr, use_hmin, ts, qxs, qys, temp, qx, qy, S(stream));
+}
+
+int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int32_t *singular, void *stream) {
+    if (!a || !inv || !singular || n < 0 || m <= 0) return PBTE_ERR_ARG;
+    return pbte::launch_batched_inverse(a, inv, n, m, singular, S(stream));
+}
+
+}  // extern "C"

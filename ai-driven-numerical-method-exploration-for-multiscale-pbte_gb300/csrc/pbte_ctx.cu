@@ -1,0 +1,290 @@
+// Context creation: sweep scheduling on the host, operator upload, optional
+// precomputed FP64 factors.  Stands in for SweepContext.build / factorise
+// (pybte/sweep.py:74-129) and build_sweep_order (pybte/ordering.py:143-175).
+//
+// Scheduling.  pybte walks each direction's elements in a topological order
+// (TRI_ORDER) one at a time.  Without periodic faces or broken cycles, an
+// element's solve reads only its upwind neighbours' final values, so every
+// topological order gives the same bits; the GPU walks wavefront *levels*
+// instead (level = 1 + max level of the upwind neighbours) and solves all
+// elements of a level at once.  Directions whose upwind relation agrees on
+// every interior face (same sign of c.n) share one level list: they form a
+// "class".  On the structured benchmark meshes the face normals take four
+// orientations, so all ordinates fall into a handful of classes.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <unordered_map>
+#include <vector>
+
+#include "pbte_internal.cuh"
+
+namespace {
+
+template <typename T>
+int upload(const T *h, size_t n, T **d, size_t *bytes) {
+    if (n == 0) { *d = nullptr; return PBTE_OK; }
+    if (cudaMalloc((void **)d, n * sizeof(T)) != cudaSuccess) return PBTE_ERR_NOMEM;
+    *bytes += n * sizeof(T);
+    if (cudaMemcpy(*d, h, n * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return PBTE_ERR_CUDA;
+    return PBTE_OK;
+}
+
+template <typename T>
+int alloc(size_t n, T **d, size_t *bytes) {
+    if (n == 0) { *d = nullptr; return PBTE_OK; }
+    if (cudaMalloc((void **)d, n * sizeof(T)) != cudaSuccess) return PBTE_ERR_NOMEM;
+    *bytes += n * sizeof(T);
+    return PBTE_OK;
+}
+
+int8_t sgn(double v) { return v > 0.0 ? 1 : (v < 0.0 ? -1 : 0); }
+
+// Kahn levels of one direction's dependency graph.  Returns false on a cycle.
+bool levels_for(const pbte_case_desc *d, double cx, double cy, std::vector<int32_t> &level,
+                std::vector<int32_t> &indeg, std::vector<int32_t> &queue) {
+    const int nt = d->n_tris;
+    level.assign(nt, 0);
+    indeg.assign(nt, 0);
+    for (int i = 0; i < nt; ++i)
+        for (int il = 0; il < 3; ++il) {
+            int nb = d->upwind_tri[i * 3 + il];
+            int fc = d->tri_faces[i * 3 + il];
+            if (nb < 0 || d->face_bc[fc] >= 0) continue;  // walls and periodic faces: no in-sweep dependency
+            double s = cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il];
+            if (s < 0.0) indeg[i]++;
+        }
+    queue.clear();
+    for (int i = 0; i < nt; ++i)
+        if (indeg[i] == 0) queue.push_back(i);
+    size_t head = 0;
+    while (head < queue.size()) {
+        int i = queue[head++];
+        for (int il = 0; il < 3; ++il) {
+            int nb = d->upwind_tri[i * 3 + il];
+            int fc = d->tri_faces[i * 3 + il];
+            if (nb < 0 || d->face_bc[fc] >= 0) continue;
+            double s = cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il];
+            if (s > 0.0) {  // i is upwind of nb across this face
+                level[nb] = std::max(level[nb], level[i] + 1);
+                if (--indeg[nb] == 0) queue.push_back(nb);
+            }
+        }
+    }
+    return (int)queue.size() == nt;
+}
+
+}  // namespace
+
+extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
+    if (!c) return PBTE_OK;
+    void *ptrs[] = {c->d_cx, c->d_cy, c->d_w, c->d_cells64, c->d_cells32, c->d_ref64, c->d_ref32,
+                    c->d_edofs, c->d_dir_class, c->d_class_lvl_off, c->d_class_nlev, c->d_lvl_ptr,
+                    c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
+                    c->d_piv, c->d_red, c->d_singular};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    delete c;
+    return PBTE_OK;
+}
+
+extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx **out) {
+    if (!d || !out) return PBTE_ERR_ARG;
+    *out = nullptr;
+    const int nt = d->n_tris, nd = d->ndof, nf = d->ndof_fc, ndir = d->ndir;
+    int deg = nf - 1;
+    if (nt <= 0 || ndir <= 0 || d->n_faces <= 0 || deg < 1 || deg > 4 ||
+        nd != (deg + 1) * (deg + 2) / 2)
+        return PBTE_ERR_ARG;
+    pbte_ctx *c = new pbte_ctx();
+    c->n_tris = nt; c->n_faces = d->n_faces; c->nd = nd; c->nf = nf; c->ndir = ndir;
+    c->nbc = d->nbc; c->deg = deg;
+    c->cv = d->cv; c->vg = d->vg; c->tau_r = d->tau_r; c->tau_n = d->tau_n; c->tau_c = d->tau_c;
+    c->h_cx.assign(d->cxv, d->cxv + ndir);
+    c->h_cy.assign(d->cyv, d->cyv + ndir);
+    c->h_w.assign(d->domega, d->domega + ndir);
+    int rc = PBTE_OK;
+#define TRY(x) do { rc = (x); if (rc != PBTE_OK) { pbte_ctx_destroy(c); return rc; } } while (0)
+
+    // ---- element records -------------------------------------------------
+    std::vector<pbte::CellRec<double>> r64(nt);
+    std::vector<pbte::CellRec<float>> r32(nt);
+    const double four_pi = 4.0 * pbte::kPi;
+    for (int i = 0; i < nt; ++i) {
+        auto &r = r64[i];
+        std::memset(&r, 0, sizeof(r));
+        r.area2 = d->area2[i];
+        r.gxa = d->dxi[i * 2 + 0]; r.gxb = d->dxi[i * 2 + 1];
+        r.gya = d->deta[i * 2 + 0]; r.gyb = d->deta[i * 2 + 1];
+        for (int il = 0; il < 3; ++il) {
+            r.es[il] = d->edge_scale[i * 3 + il];
+            r.nx[il] = d->nx[i * 3 + il];
+            r.ny[il] = d->ny[i * 3 + il];
+            int fc = d->tri_faces[i * 3 + il];
+            if (fc < 0 || fc >= d->n_faces) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+            r.face[il] = fc;
+            r.upw[il] = d->upwind_tri[i * 3 + il];
+            int bc = d->face_bc[fc];
+            if (bc < 0) {
+                r.kind[il] = 0;
+                if (r.upw[il] < 0 || r.upw[il] >= nt) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+            } else {
+                if (bc >= d->nbc) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+                int t = d->bc_type[bc];
+                if (t == 1) { r.kind[il] = 1; r.bval[il] = d->cv / four_pi * d->bc_temp[bc]; }
+                else if (t == 2) r.kind[il] = 2;
+                else if (t == 3) { r.kind[il] = 3; c->has_periodic = true; }
+                else { pbte_ctx_destroy(c); return PBTE_ERR_UNSUPPORTED; }
+            }
+            for (int b = 0; b < nf; ++b) {
+                int v = r.upw[il] >= 0 ? d->edge_map[(i * 3 + il) * nf + b] : 0;
+                if (v < 0 || v >= nd) v = 0;
+                r.emap[il][b] = (int8_t)v;
+            }
+        }
+        auto &q = r32[i];
+        std::memset(&q, 0, sizeof(q));
+        q.area2 = (float)r.area2; q.gxa = (float)r.gxa; q.gxb = (float)r.gxb;
+        q.gya = (float)r.gya; q.gyb = (float)r.gyb;
+        for (int il = 0; il < 3; ++il) {
+            q.es[il] = (float)r.es[il]; q.nx[il] = (float)r.nx[il]; q.ny[il] = (float)r.ny[il];
+            q.bval[il] = (float)r.bval[il]; q.face[il] = r.face[il]; q.upw[il] = r.upw[il];
+            q.kind[il] = r.kind[il];
+            for (int b = 0; b < pbte::kMaxNf; ++b) q.emap[il][b] = r.emap[il][b];
+        }
+    }
+    TRY(upload(r64.data(), (size_t)nt, &c->d_cells64, &c->device_bytes));
+    TRY(upload(r32.data(), (size_t)nt, &c->d_cells32, &c->device_bytes));
+
+    // ---- reference matrices, edge DOFs, ordinates -----------------------
+    std::vector<double> ref(6 * nd * nd);
+    std::memcpy(ref.data(), d->ref_mass, sizeof(double) * nd * nd);
+    std::memcpy(ref.data() + nd * nd, d->ref_dx, sizeof(double) * nd * nd);
+    std::memcpy(ref.data() + 2 * nd * nd, d->ref_dy, sizeof(double) * nd * nd);
+    std::memcpy(ref.data() + 3 * nd * nd, d->ref_edge, sizeof(double) * 3 * nd * nd);
+    std::vector<float> ref32(ref.begin(), ref.end());
+    TRY(upload(ref.data(), ref.size(), &c->d_ref64, &c->device_bytes));
+    TRY(upload(ref32.data(), ref32.size(), &c->d_ref32, &c->device_bytes));
+    TRY(upload(d->edge_dofs, (size_t)3 * nf, &c->d_edofs, &c->device_bytes));
+    TRY(upload(d->cxv, (size_t)ndir, &c->d_cx, &c->device_bytes));
+    TRY(upload(d->cyv, (size_t)ndir, &c->d_cy, &c->device_bytes));
+    TRY(upload(d->domega, (size_t)ndir, &c->d_w, &c->device_bytes));
+    TRY(upload(d->int_tri, (size_t)nd * nt, &c->d_int_tri, &c->device_bytes));
+
+    // ---- adiabatic wall faces -------------------------------------------
+    std::vector<pbte::WallFace> walls;
+    for (int f = 0; f < d->n_faces; ++f) {
+        int bc = d->face_bc[f];
+        if (bc < 0 || d->bc_type[bc] != 2) continue;
+        pbte::WallFace w{};
+        w.face = f;
+        if (d->face_tri[f * 2 + 0] < 0) { w.tri = d->face_tri[f * 2 + 1]; w.lfc = d->face_lfc[f * 2 + 1]; }
+        else { w.tri = d->face_tri[f * 2 + 0]; w.lfc = d->face_lfc[f * 2 + 0]; }
+        w.nx = -d->nx[w.tri * 3 + w.lfc];
+        w.ny = -d->ny[w.tri * 3 + w.lfc];
+        walls.push_back(w);
+    }
+    c->n_wall_ad = (int)walls.size();
+    TRY(upload(walls.data(), walls.size(), &c->d_wall_ad, &c->device_bytes));
+
+    // ---- direction classes and wavefront levels -------------------------
+    // sign pattern of c.n over the interior faces, hashed (FNV-1a) and then
+    // compared in full against the class representative
+    std::vector<int32_t> iface_tri, iface_lfc;
+    for (int f = 0; f < d->n_faces; ++f)
+        if (d->face_bc[f] < 0) {
+            int t = d->face_tri[f * 2 + 0] >= 0 ? d->face_tri[f * 2 + 0] : d->face_tri[f * 2 + 1];
+            int l = d->face_tri[f * 2 + 0] >= 0 ? d->face_lfc[f * 2 + 0] : d->face_lfc[f * 2 + 1];
+            iface_tri.push_back(t);
+            iface_lfc.push_back(l);
+        }
+    auto pattern = [&](int dir, std::vector<int8_t> &p) {
+        p.resize(iface_tri.size());
+        for (size_t k = 0; k < iface_tri.size(); ++k) {
+            int t = iface_tri[k], l = iface_lfc[k];
+            p[k] = sgn(d->cxv[dir] * d->nx[t * 3 + l] + d->cyv[dir] * d->ny[t * 3 + l]);
+        }
+    };
+    std::unordered_multimap<uint64_t, int> by_hash;  // hash -> class id
+    std::vector<int> class_rep;
+    std::vector<int32_t> dir_class(ndir);
+    std::vector<int8_t> pat, pat2;
+    for (int dir = 0; dir < ndir; ++dir) {
+        pattern(dir, pat);
+        uint64_t h = 1469598103934665603ull;
+        for (int8_t v : pat) { h ^= (uint8_t)v; h *= 1099511628211ull; }
+        int found = -1;
+        auto range = by_hash.equal_range(h);
+        for (auto it = range.first; it != range.second && found < 0; ++it) {
+            pattern(class_rep[it->second], pat2);
+            if (pat2 == pat) found = it->second;
+        }
+        if (found < 0) {
+            found = (int)class_rep.size();
+            class_rep.push_back(dir);
+            by_hash.emplace(h, found);
+        }
+        dir_class[dir] = found;
+    }
+    c->nclass = (int)class_rep.size();
+    std::vector<int32_t> lvl_cells((size_t)c->nclass * nt), lvl_ptr, class_off(c->nclass),
+        class_nlev(c->nclass);
+    std::vector<int32_t> level, indeg, queue, count;
+    for (int k = 0; k < c->nclass; ++k) {
+        int dir = class_rep[k];
+        if (!levels_for(d, d->cxv[dir], d->cyv[dir], level, indeg, queue)) {
+            pbte_ctx_destroy(c);
+            return PBTE_ERR_CYCLE;
+        }
+        int nlev = 0;
+        for (int i = 0; i < nt; ++i) nlev = std::max(nlev, level[i] + 1);
+        count.assign(nlev + 1, 0);
+        for (int i = 0; i < nt; ++i) count[level[i] + 1]++;
+        for (int L = 0; L < nlev; ++L) count[L + 1] += count[L];
+        class_off[k] = (int32_t)lvl_ptr.size();
+        class_nlev[k] = nlev;
+        for (int L = 0; L <= nlev; ++L) lvl_ptr.push_back(count[L] + k * nt);
+        std::vector<int32_t> fill(count.begin(), count.end() - 1);
+        for (int i = 0; i < nt; ++i) lvl_cells[(size_t)k * nt + fill[level[i]]++] = i;
+        c->nlev_max = std::max(c->nlev_max, nlev);
+    }
+    TRY(upload(dir_class.data(), dir_class.size(), &c->d_dir_class, &c->device_bytes));
+    TRY(upload(class_off.data(), class_off.size(), &c->d_class_lvl_off, &c->device_bytes));
+    TRY(upload(class_nlev.data(), class_nlev.size(), &c->d_class_nlev, &c->device_bytes));
+    TRY(upload(lvl_ptr.data(), lvl_ptr.size(), &c->d_lvl_ptr, &c->device_bytes));
+    TRY(upload(lvl_cells.data(), lvl_cells.size(), &c->d_lvl_cells, &c->device_bytes));
+
+    // ---- scratch ----------------------------------------------------------
+    TRY(alloc((size_t)3 * nd * nt, &c->d_S64, &c->device_bytes));
+    TRY(alloc((size_t)3 * nd * nt, &c->d_S32, &c->device_bytes));
+    TRY(alloc((size_t)4096, &c->d_red, &c->device_bytes));
+    TRY(alloc((size_t)1, &c->d_singular, &c->device_bytes));
+    if (cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
+
+    if (precompute) {
+        TRY(alloc((size_t)ndir * nt * nd * nd, &c->d_lu, &c->device_bytes));
+        TRY(alloc((size_t)ndir * nt * nd, &c->d_piv, &c->device_bytes));
+        TRY(pbte::launch_factorise(c, 0));
+        int32_t bad = 0;
+        if (cudaMemcpy(&bad, c->d_singular, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) {
+            pbte_ctx_destroy(c);
+            return PBTE_ERR_CUDA;
+        }
+        if (bad) { pbte_ctx_destroy(c); return PBTE_ERR_SINGULAR; }
+    }
+    if (cudaDeviceSynchronize() != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
+#undef TRY
+    *out = c;
+    return PBTE_OK;
+}
+
+extern "C" int pbte_ctx_info(const pbte_ctx *c, int64_t *nlev, int64_t *ncls, int64_t *bytes) {
+    if (!c) return PBTE_ERR_ARG;
+    if (nlev) *nlev = c->nlev_max;
+    if (ncls) *ncls = c->nclass;
+    if (bytes) *bytes = (int64_t)c->device_bytes;
+    return PBTE_OK;
+}

@@ -1,0 +1,108 @@
+// Internal definitions shared by the translation units of libpbte_gb300.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "pbte_gb300.h"
+
+namespace pbte {
+
+constexpr double kPi = 3.141592653589793238462643383279502884;
+constexpr int kMaxNf = 5;   // deg <= 4
+
+// Per-element record read by the sweep: the compact operator description of
+// one triangle plus its three faces.  One 16-byte-aligned struct per element
+// so a thread fetches it in a few wide loads.
+template <typename T>
+struct alignas(16) CellRec {
+    T area2;        // 2 * area
+    T gxa, gxb;     // d(xi)/dx, d(eta)/dx  (gx = area2 (gxa ref_dx + gxb ref_dy))
+    T gya, gyb;     // d(xi)/dy, d(eta)/dy
+    T es[3];        // edge scale: len12, len23/sqrt2, len31
+    T nx[3], ny[3]; // outward unit normals
+    T bval[3];      // cv/(4 pi) T_wall on thermalising edges, else 0
+    int32_t face[3];
+    int32_t upw[3];         // upwind element across the edge (neighbour or periodic partner), -1 on walls
+    int8_t kind[3];         // 0 interior, 1 thermalising, 2 adiabatic, 3 periodic
+    int8_t emap[3][kMaxNf]; // neighbour DOF facing each of this element's edge DOFs
+};
+
+struct WallFace {
+    int32_t face, tri, lfc, pad;
+    double nx, ny;  // inward normal (-n_out of the adjacent element)
+};
+
+}  // namespace pbte
+
+struct pbte_ctx {
+    int n_tris = 0, n_faces = 0, nd = 0, nf = 0, ndir = 0, nbc = 0, deg = 0;
+    double cv = 1, vg = 1, tau_r = 1, tau_n = 1, tau_c = 1;
+    std::vector<double> h_cx, h_cy, h_w;
+    bool has_periodic = false;
+
+    // device data
+    double *d_cx = nullptr, *d_cy = nullptr, *d_w = nullptr;
+    pbte::CellRec<double> *d_cells64 = nullptr;
+    pbte::CellRec<float> *d_cells32 = nullptr;
+    double *d_ref64 = nullptr;   // [6][nd*nd]: mass, dx, dy, edge0, edge1, edge2
+    float *d_ref32 = nullptr;
+    int32_t *d_edofs = nullptr;  // [3][nf]
+    int32_t *d_dir_class = nullptr;
+    int32_t *d_class_lvl_off = nullptr;  // [nclass]: offset of the class's level pointer block
+    int32_t *d_class_nlev = nullptr;     // [nclass]
+    int32_t *d_lvl_ptr = nullptr;        // concatenated level pointers (into d_lvl_cells)
+    int32_t *d_lvl_cells = nullptr;      // [nclass][n_tris]
+    int nclass = 0, nlev_max = 0;
+    double *d_int_tri = nullptr;
+    int n_wall_ad = 0;
+    pbte::WallFace *d_wall_ad = nullptr;
+    double *d_S64 = nullptr;  // [3][nd][n_tris] moment sources of the current sweep
+    float *d_S32 = nullptr;
+    double *d_lu = nullptr;   // [ndir][n_tris][nd][nd] precomputed factors (optional)
+    int8_t *d_piv = nullptr;
+    double *d_red = nullptr;  // reduction scratch
+    int32_t *d_singular = nullptr;
+    const int32_t *done = nullptr;  // optional device stop flag
+    size_t device_bytes = 0;
+};
+
+// launchers (pbte_kernels.cu)
+namespace pbte {
+int launch_sources(pbte_ctx *c, const double *ts, const double *qxs, const double *qys, bool f32,
+                   cudaStream_t s);
+int launch_sweep64(pbte_ctx *c, double *vdf, const double *flux_wall, const double *pbuf,
+                   int use_pbuf, cudaStream_t s);
+int launch_sweep32(pbte_ctx *c, float *vdf32, const double *flux_wall, double wall_scale,
+                   cudaStream_t s);
+int launch_factorise(pbte_ctx *c, cudaStream_t s);
+int launch_moments64(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys,
+                     double *temp, double *qx, double *qy, cudaStream_t s);
+int launch_moments32(pbte_ctx *c, const float *vdf, double *ts, double *qxs, double *qys,
+                     double *temp, double *qx, double *qy, cudaStream_t s);
+int launch_wall_flux64(pbte_ctx *c, const double *vdf, double *fw, cudaStream_t s);
+int launch_wall_flux32(pbte_ctx *c, const float *vdf, double *fw, cudaStream_t s);
+int launch_residual(pbte_ctx *c, const double *temp, double *t_old, double *out, cudaStream_t s);
+int launch_residual_check(pbte_ctx *c, const double *res, double tol, int64_t tmax, int32_t *done,
+                          int64_t *count, double *hist, int64_t hist_cap, cudaStream_t s);
+int launch_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                              const double *vdf, const double *fw, const double *pbuf,
+                              double *num, double *den, cudaStream_t s);
+int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s);
+int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk,
+                      const int32_t *tri_list, const int32_t *lfc_list, double *out,
+                      cudaStream_t s);
+int launch_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_hmin,
+                   double tau_thr, int use_hmin, double *ts, double *qxs, double *qys,
+                   double *temp, double *qx, double *qy, cudaStream_t s);
+int launch_batched_inverse(const double *a, double *inv, int n, int m, int32_t *singular,
+                           cudaStream_t s);
+}  // namespace pbte
+
+#define PBTE_CUDA_TRY(expr)                                  \
+    do {                                                     \
+        cudaError_t _e = (expr);                             \
+        if (_e != cudaSuccess) return PBTE_ERR_CUDA;         \
+    } while (0)

@@ -1,0 +1,819 @@
+// Device kernels of libpbte_gb300 (sm_103a).
+//
+// Transport sweep (pybte/_kernels.py:107-269).  One thread block walks one
+// ordinate's wavefront levels; the threads of the block split the elements
+// of a level, and each thread forms its element's N_p x N_p operator
+//     A = area2 [ M/tau_c - (c.grad-xi) Dx - (c.grad-eta) Dy ] + sum_out (c.n) L_e R_e
+// from the six reference matrices in shared memory, adds the upwind inflow
+// through the edge gather map, and solves A x = b with partial pivoting in
+// registers (or with stored FP64 factors in the "precomputed" mode).
+// Other kernels: moment sources, moments, adiabatic-wall emission, residuals,
+// transport residual, GSIS hot source / wall trace / correction, batched
+// inverse.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+
+#include "pbte_internal.cuh"
+
+namespace pbte {
+
+constexpr int kSweepThreads = 128;
+
+template <int DEG>
+struct Shape {
+    static constexpr int NP = (DEG + 1) * (DEG + 2) / 2;
+    static constexpr int NF = DEG + 1;
+    __host__ __device__ static constexpr int idx(int i, int j) { return j * (DEG + 1) - j * (j - 1) / 2 + i; }
+    // element DOF of the b-th node along local edge il (edges walk node1->2, 2->3, 3->1)
+    __host__ __device__ static constexpr int edof(int il, int b) {
+        return il == 0 ? idx(b, 0) : (il == 1 ? idx(DEG - b, b) : idx(0, DEG - b));
+    }
+};
+
+__device__ __forceinline__ bool stopped(const int32_t *done) { return done != nullptr && *(volatile const int32_t *)done != 0; }
+
+template <typename T>
+struct SweepParams {
+    const CellRec<T> *cells;
+    const T *ref;  // [6][NP*NP]
+    const T *S;    // [n_tris][3][NP]
+    T *vdf;        // [ndir][n_tris][NP]
+    const double *flux_wall;
+    const double *pbuf;
+    int use_pbuf;
+    const double *cx, *cy;
+    const int32_t *dir_class, *class_off, *class_nlev, *lvl_ptr, *lvl_cells;
+    const double *lu;
+    const int8_t *piv;
+    int32_t *singular;
+    const int32_t *done;
+    int nt, n_faces;
+    T inv_tau_c, ca, cb, wall_scale;
+};
+
+// Assemble the element operator (without the volume part when PRECOMP).
+template <typename T, int DEG>
+__device__ __forceinline__ void assemble(const T *sref, const CellRec<T> &r, T cx, T cy, T inv_tau_c,
+                                         const T (&s)[3], T (&A)[Shape<DEG>::NP][Shape<DEG>::NP]) {
+    constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
+    const T p = r.area2 * inv_tau_c;
+    const T q = -r.area2 * (cx * r.gxa + cy * r.gya);
+    const T w = -r.area2 * (cx * r.gxb + cy * r.gyb);
+#pragma unroll
+    for (int m = 0; m < NP; ++m)
+#pragma unroll
+        for (int l = 0; l < NP; ++l)
+            A[m][l] = p * sref[m * NP + l] + q * sref[NP * NP + m * NP + l] + w * sref[2 * NP * NP + m * NP + l];
+#pragma unroll
+    for (int il = 0; il < 3; ++il) {
+        const T sc = s[il] > T(0) ? s[il] * r.es[il] : T(0);
+        const T *R = sref + (3 + il) * NP * NP;
+#pragma unroll
+        for (int a = 0; a < NF; ++a)
+#pragma unroll
+            for (int b = 0; b < NF; ++b) {
+                const int ma = Shape<DEG>::edof(il, a), lb = Shape<DEG>::edof(il, b);
+                A[ma][lb] += sc * R[ma * NP + lb];
+            }
+    }
+}
+
+// Right-hand side: Callaway source from the moment sources plus the upwind inflow.
+template <typename T, int DEG>
+__device__ __forceinline__ void rhs(const SweepParams<T> &P, const T *sref, const CellRec<T> &r, int i,
+                                    int d, T cx, T cy, const T (&s)[3], const T *f,
+                                    T (&b)[Shape<DEG>::NP]) {
+    constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
+    const T *S = P.S + (size_t)i * 3 * NP;
+#pragma unroll
+    for (int m = 0; m < NP; ++m) b[m] = P.ca * S[m] + P.cb * (cx * S[NP + m] + cy * S[2 * NP + m]);
+#pragma unroll
+    for (int il = 0; il < 3; ++il) {
+        if (!(s[il] < T(0))) continue;
+        const T w = s[il];
+        const T *R = sref + (3 + il) * NP * NP;
+        const int kind = r.kind[il];
+        if (kind == 0 || kind == 3) {
+            T g[NF];
+            if (kind == 3 && P.use_pbuf) {
+                const double *pb = P.pbuf + ((size_t)d * P.n_faces + r.face[il]) * NP;
+#pragma unroll
+                for (int bb = 0; bb < NF; ++bb) g[bb] = (T)pb[r.emap[il][bb]];
+            } else {
+                const T *fn = f + (size_t)r.upw[il] * NP;
+#pragma unroll
+                for (int bb = 0; bb < NF; ++bb) g[bb] = fn[r.emap[il][bb]];
+            }
+            const T sc = w * r.es[il];
+#pragma unroll
+            for (int a = 0; a < NF; ++a) {
+                const int ma = Shape<DEG>::edof(il, a);
+                T acc = T(0);
+#pragma unroll
+                for (int bb = 0; bb < NF; ++bb) acc += R[ma * NP + Shape<DEG>::edof(il, bb)] * g[bb];
+                b[ma] -= sc * acc;
+            }
+        } else if (kind == 1) {
+            const T sc = w * r.bval[il] * P.wall_scale * r.es[il];
+#pragma unroll
+            for (int a = 0; a < NF; ++a) {
+                const int ma = Shape<DEG>::edof(il, a);
+                T rs = T(0);
+#pragma unroll
+                for (int bb = 0; bb < NF; ++bb) rs += R[ma * NP + Shape<DEG>::edof(il, bb)];
+                b[ma] -= sc * rs;
+            }
+        } else {
+            const double *fw = P.flux_wall + (size_t)r.face[il] * NP;
+#pragma unroll
+            for (int m = 0; m < NP; ++m) b[m] -= w * (-(T)fw[m]);
+        }
+    }
+}
+
+// LU with partial pivoting (first maximum, as DGETF2) applied to b on the fly,
+// then back substitution; returns the number of zero pivots.
+template <typename T, int N>
+__device__ __forceinline__ int lu_solve(T (&A)[N][N], T (&b)[N]) {
+    int sing = 0;
+    T rinv[N];
+#pragma unroll
+    for (int k = 0; k < N; ++k) {
+        T big = fabs(A[k][k]);
+        int p = k;
+#pragma unroll
+        for (int i = k + 1; i < N; ++i) {
+            const T v = fabs(A[i][k]);
+            if (v > big) { big = v; p = i; }
+        }
+#pragma unroll
+        for (int i = k + 1; i < N; ++i) {
+            if (p == i) {
+#pragma unroll
+                for (int j = 0; j < N; ++j) { const T t = A[k][j]; A[k][j] = A[i][j]; A[i][j] = t; }
+                const T t = b[k]; b[k] = b[i]; b[i] = t;
+            }
+        }
+        sing += (A[k][k] == T(0));
+        rinv[k] = T(1) / A[k][k];
+#pragma unroll
+        for (int i = k + 1; i < N; ++i) {
+            const T l = A[i][k] * rinv[k];
+#pragma unroll
+            for (int j = k + 1; j < N; ++j) A[i][j] -= l * A[k][j];
+            b[i] -= l * b[k];
+        }
+    }
+#pragma unroll
+    for (int k = N - 1; k >= 0; --k) {
+        b[k] *= rinv[k];
+#pragma unroll
+        for (int i = 0; i < k; ++i) b[i] -= b[k] * A[i][k];
+    }
+    return sing;
+}
+
+template <typename T, int DEG, bool PRECOMP>
+__global__ void __launch_bounds__(kSweepThreads) sweep_kernel(SweepParams<T> P) {
+    constexpr int NP = Shape<DEG>::NP;
+    __shared__ T sref[6 * NP * NP];
+    if (stopped(P.done)) return;
+    const int d = blockIdx.x;
+    for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
+    __syncthreads();
+    const T cx = (T)P.cx[d], cy = (T)P.cy[d];
+    const int cls = P.dir_class[d];
+    const int off = P.class_off[cls], nlev = P.class_nlev[cls];
+    T *f = P.vdf + (size_t)d * P.nt * NP;
+    int sing = 0;
+    for (int L = 0; L < nlev; ++L) {
+        const int beg = P.lvl_ptr[off + L], end = P.lvl_ptr[off + L + 1];
+        for (int k = beg + threadIdx.x; k < end; k += blockDim.x) {
+            const int i = P.lvl_cells[k];
+            const CellRec<T> r = P.cells[i];
+            T s[3];
+#pragma unroll
+            for (int il = 0; il < 3; ++il) s[il] = cx * r.nx[il] + cy * r.ny[il];
+            T b[NP];
+            rhs<T, DEG>(P, sref, r, i, d, cx, cy, s, f, b);
+            if constexpr (PRECOMP) {
+                const double *lu = P.lu + ((size_t)d * P.nt + i) * NP * NP;
+                const int8_t *pv = P.piv + ((size_t)d * P.nt + i) * NP;
+#pragma unroll
+                for (int k2 = 0; k2 < NP; ++k2) {
+                    const int p = pv[k2];
+#pragma unroll
+                    for (int j = k2 + 1; j < NP; ++j)
+                        if (p == j) { const T t = b[k2]; b[k2] = b[j]; b[j] = t; }
+                }
+#pragma unroll
+                for (int k2 = 0; k2 < NP; ++k2)
+#pragma unroll
+                    for (int j = k2 + 1; j < NP; ++j) b[j] -= b[k2] * (T)lu[j * NP + k2];
+#pragma unroll
+                for (int k2 = NP - 1; k2 >= 0; --k2) {
+                    b[k2] *= (T)lu[k2 * NP + k2];  // stored as 1/U_kk
+#pragma unroll
+                    for (int j = 0; j < k2; ++j) b[j] -= b[k2] * (T)lu[j * NP + k2];
+                }
+            } else {
+                T A[NP][NP];
+                assemble<T, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A);
+                sing += lu_solve<T, NP>(A, b);
+            }
+            T *out = f + (size_t)i * NP;
+#pragma unroll
+            for (int m = 0; m < NP; ++m) out[m] = b[m];
+        }
+        __syncthreads();
+    }
+    if (sing) atomicAdd(P.singular, sing);
+}
+
+// Stored factors for the precomputed FP64 mode: LU with the row interchanges
+// of partial pivoting, unit-lower multipliers below the diagonal, U above it
+// and 1/U_kk on it; ipiv as in DGETF2.
+template <int DEG>
+__global__ void factorise_kernel(SweepParams<double> P, double *lu_out, int8_t *piv_out, int ndir) {
+    constexpr int NP = Shape<DEG>::NP;
+    __shared__ double sref[6 * NP * NP];
+    for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
+    __syncthreads();
+    const size_t total = (size_t)ndir * P.nt;
+    int sing = 0;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int d = (int)(t / P.nt), i = (int)(t % P.nt);
+        const double cx = P.cx[d], cy = P.cy[d];
+        const CellRec<double> r = P.cells[i];
+        double s[3];
+        for (int il = 0; il < 3; ++il) s[il] = cx * r.nx[il] + cy * r.ny[il];
+        double A[NP][NP];
+        assemble<double, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A);
+        int8_t pv[NP];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) {
+            double big = fabs(A[k][k]);
+            int p = k;
+#pragma unroll
+            for (int i2 = k + 1; i2 < NP; ++i2) {
+                const double v = fabs(A[i2][k]);
+                if (v > big) { big = v; p = i2; }
+            }
+            pv[k] = (int8_t)p;
+#pragma unroll
+            for (int i2 = k + 1; i2 < NP; ++i2)
+                if (p == i2)
+#pragma unroll
+                    for (int j = 0; j < NP; ++j) { const double tt = A[k][j]; A[k][j] = A[i2][j]; A[i2][j] = tt; }
+            sing += (A[k][k] == 0.0);
+            const double rr = 1.0 / A[k][k];
+#pragma unroll
+            for (int i2 = k + 1; i2 < NP; ++i2) {
+                A[i2][k] *= rr;
+#pragma unroll
+                for (int j = k + 1; j < NP; ++j) A[i2][j] -= A[i2][k] * A[k][j];
+            }
+            A[k][k] = rr;
+        }
+        double *o = lu_out + t * NP * NP;
+#pragma unroll
+        for (int m = 0; m < NP; ++m)
+#pragma unroll
+            for (int l = 0; l < NP; ++l) o[m * NP + l] = A[m][l];
+#pragma unroll
+        for (int m = 0; m < NP; ++m) piv_out[t * NP + m] = pv[m];
+    }
+    if (sing) atomicAdd(P.singular, sing);
+}
+
+// Moment sources: S[i][q][m] = area2_i sum_l M[l][m] mom_q[l][i], q = ts, qxs, qys.
+template <typename T>
+__global__ void sources_kernel(const CellRec<double> *cells, const double *ref_mass, const double *ts,
+                               const double *qxs, const double *qys, T *S, int nt, int NP,
+                               const int32_t *done) {
+    if (stopped(done)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    const double a2 = cells[i].area2;
+    const double *mom[3] = {ts, qxs, qys};
+    for (int q = 0; q < 3; ++q)
+        for (int m = 0; m < NP; ++m) {
+            double acc = 0.0;
+            for (int l = 0; l < NP; ++l) acc += ref_mass[l * NP + m] * mom[q][(size_t)l * nt + i];
+            S[((size_t)i * 3 + q) * NP + m] = (T)(a2 * acc);
+        }
+}
+
+// Moments: one thread per (element, DOF); sum over ordinates in order.
+template <typename T>
+__global__ void moments_kernel(const T *vdf, const double *cx, const double *cy, const double *w, int ndir,
+                               int nt, int NP, double cv, double *ts, double *qxs, double *qys,
+                               const int32_t *done) {
+    if (stopped(done)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int total = nt * NP;
+    if (t >= total) return;
+    const int i = t / NP, l = t % NP;
+    double ss = 0.0, ssx = 0.0, ssy = 0.0;
+    if constexpr (sizeof(T) == 8) {
+        for (int d = 0; d < ndir; ++d) {
+            const double f = (double)vdf[(size_t)d * total + t];
+            const double fw = f * w[d];
+            ss += fw;
+            ssx += cx[d] * fw;
+            ssy += cy[d] * fw;
+        }
+    } else {
+        // FP32 accumulation within blocks of 32 ordinates, FP64 across blocks
+        for (int d0 = 0; d0 < ndir; d0 += 32) {
+            float s0 = 0.f, sx = 0.f, sy = 0.f;
+            const int d1 = min(ndir, d0 + 32);
+            for (int d = d0; d < d1; ++d) {
+                const float fw = (float)vdf[(size_t)d * total + t] * (float)w[d];
+                s0 += fw;
+                sx += (float)cx[d] * fw;
+                sy += (float)cy[d] * fw;
+            }
+            ss += s0; ssx += sx; ssy += sy;
+        }
+    }
+    ts[(size_t)l * nt + i] = ss / cv;
+    qxs[(size_t)l * nt + i] = ssx;
+    qys[(size_t)l * nt + i] = ssy;
+}
+
+__global__ void element_integrals_kernel(const double *ts, const double *qxs, const double *qys,
+                                         const double *int_tri, int nt, int NP, double cv, double *temp,
+                                         double *qx, double *qy, const int32_t *done) {
+    if (stopped(done)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    double a = 0.0, bx = 0.0, by = 0.0;
+    for (int l = 0; l < NP; ++l) {
+        const double it = int_tri[(size_t)l * nt + i];
+        a += ts[(size_t)l * nt + i] * cv * it / cv;
+        bx += qxs[(size_t)l * nt + i] * it;
+        by += qys[(size_t)l * nt + i] * it;
+    }
+    temp[i] = a;
+    qx[i] = bx;
+    qy[i] = by;
+}
+
+// Adiabatic-wall emission: one block per wall face, ordinates over threads.
+template <typename T>
+__global__ void wall_flux_kernel(const T *vdf, const WallFace *walls, const CellRec<double> *cells,
+                                 const double *ref_edge, const double *cx, const double *cy,
+                                 const double *w, int ndir, int nt, int NP, double *fw_out,
+                                 const int32_t *done) {
+    if (stopped(done)) return;
+    extern __shared__ double red[];  // [blockDim][NP+1]
+    const WallFace wf = walls[blockIdx.x];
+    const double es = cells[wf.tri].es[wf.lfc];
+    const double *R = ref_edge + (size_t)wf.lfc * NP * NP;
+    double acc[16];
+    for (int m = 0; m < NP; ++m) acc[m] = 0.0;
+    double s2 = 0.0;
+    for (int d = threadIdx.x; d < ndir; d += blockDim.x) {
+        const double u = cx[d] * wf.nx + cy[d] * wf.ny;
+        if (u < 0.0) {
+            const T *f = vdf + ((size_t)d * nt + wf.tri) * NP;
+            for (int m = 0; m < NP; ++m) {
+                double a = 0.0;
+                for (int l = 0; l < NP; ++l) a += (double)f[l] * (es * R[m * NP + l]);
+                acc[m] += u * w[d] * a;
+            }
+        } else {
+            s2 -= u * w[d];
+        }
+    }
+    for (int m = 0; m < NP; ++m) red[threadIdx.x * (NP + 1) + m] = acc[m];
+    red[threadIdx.x * (NP + 1) + NP] = s2;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int m = 0; m <= NP; ++m) red[threadIdx.x * (NP + 1) + m] += red[(threadIdx.x + h) * (NP + 1) + m];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double ss2 = red[NP];
+        for (int m = 0; m < NP; ++m) fw_out[(size_t)wf.face * NP + m] = -red[m] / ss2;
+    }
+}
+
+// Step residual and mass; out[0] = residual, out[1] = sum(temp); t_old <- temp.
+__global__ void residual_kernel(const double *temp, double *t_old, int n, double *out, const int32_t *done) {
+    if (stopped(done)) return;
+    __shared__ double s1[1024], s2[1024], s3[1024];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const double d = temp[i] - t_old[i];
+        a += d * d;
+        b += temp[i] * temp[i];
+        c += temp[i];
+    }
+    s1[threadIdx.x] = a; s2[threadIdx.x] = b; s3[threadIdx.x] = c;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            s1[threadIdx.x] += s1[threadIdx.x + h];
+            s2[threadIdx.x] += s2[threadIdx.x + h];
+            s3[threadIdx.x] += s3[threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) { out[0] = sqrt(s1[0] / s2[0]); out[1] = s3[0]; }
+    for (int i = threadIdx.x; i < n; i += blockDim.x) t_old[i] = temp[i];
+}
+
+// Convergence bookkeeping for graph-captured loops.  res[0] residual, res[1] mass;
+// hist[2k], hist[2k+1] record them when hist is given.
+__global__ void residual_check_kernel(const double *res, double tol, int64_t tmax, int32_t *done,
+                                      int64_t *count, double *hist, int64_t hist_cap) {
+    if (*done) return;
+    const int64_t k = *count;
+    if (hist && k < hist_cap) { hist[2 * k] = res[0]; hist[2 * k + 1] = res[1]; }
+    *count = k + 1;
+    if (res[0] < tol) *done = 1;
+    else if (k + 1 >= tmax) *done = 2;
+}
+
+// ||A f - b||^2 per ordinate (no sweep): one block per ordinate.
+template <int DEG>
+__global__ void transport_residual_kernel(SweepParams<double> P, double *num, double *den) {
+    constexpr int NP = Shape<DEG>::NP;
+    __shared__ double sref[6 * NP * NP];
+    __shared__ double r1[kSweepThreads], r2[kSweepThreads];
+    const int d = blockIdx.x;
+    for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
+    __syncthreads();
+    const double cx = P.cx[d], cy = P.cy[d];
+    const double *f = P.vdf + (size_t)d * P.nt * NP;
+    double a = 0.0, b2 = 0.0;
+    for (int i = threadIdx.x; i < P.nt; i += blockDim.x) {
+        const CellRec<double> r = P.cells[i];
+        double s[3];
+        for (int il = 0; il < 3; ++il) s[il] = cx * r.nx[il] + cy * r.ny[il];
+        double b[NP];
+        rhs<double, DEG>(P, sref, r, i, d, cx, cy, s, f, b);
+        double A[NP][NP];
+        assemble<double, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A);
+        const double *fi = f + (size_t)i * NP;
+#pragma unroll
+        for (int m = 0; m < NP; ++m) {
+            double rr = -b[m];
+#pragma unroll
+            for (int l = 0; l < NP; ++l) rr += A[m][l] * fi[l];
+            a += rr * rr;
+            b2 += b[m] * b[m];
+        }
+    }
+    r1[threadIdx.x] = a;
+    r2[threadIdx.x] = b2;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) { r1[threadIdx.x] += r1[threadIdx.x + h]; r2[threadIdx.x] += r2[threadIdx.x + h]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        num[d] = r1[0];
+        den[d] = r2[0];
+    }
+}
+
+__global__ void scale_by_weight_kernel(double *num, double *den, const double *w, int ndir) {
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d < ndir) { num[d] *= w[d]; den[d] *= w[d]; }
+}
+
+// GSIS third-order moment source (hot_source.py:29-58), regrouped: the four
+// angular moments a_k(c) w f are taken first, then contracted with gx, gy.
+__global__ void hot_source_kernel(const double *vdf, const CellRec<double> *cells, const double *ref,
+                                  const double *cx, const double *cy, const double *w, int ndir, int nt,
+                                  int NP, double tc5, double *work) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nt) return;
+    double mk[4][16];
+    for (int k = 0; k < 4; ++k)
+        for (int l = 0; l < NP; ++l) mk[k][l] = 0.0;
+    for (int d = 0; d < ndir; ++d) {
+        const double c1 = cx[d], c2 = cy[d], dw = w[d];
+        const double a1 = c1 * (5.0 * c1 * c1 - 3.0) * dw, a2 = c2 * (5.0 * c1 * c1 - 1.0) * dw;
+        const double a3 = c1 * (5.0 * c2 * c2 - 1.0) * dw, a4 = c2 * (5.0 * c2 * c2 - 3.0) * dw;
+        const double *f = vdf + ((size_t)d * nt + i) * NP;
+        for (int l = 0; l < NP; ++l) {
+            const double fl = f[l];
+            mk[0][l] += a1 * fl; mk[1][l] += a2 * fl; mk[2][l] += a3 * fl; mk[3][l] += a4 * fl;
+        }
+    }
+    const CellRec<double> r = cells[i];
+    const double *Dx = ref + NP * NP, *Dy = ref + 2 * NP * NP;
+    double *o = work + (size_t)i * 7 * NP;
+    for (int m = 0; m < NP; ++m) {
+        double pxx = 0.0, pxy = 0.0, pyy = 0.0;
+        for (int l = 0; l < NP; ++l) {
+            const double gx = r.area2 * (r.gxa * Dx[l * NP + m] + r.gxb * Dy[l * NP + m]);
+            const double gy = r.area2 * (r.gya * Dx[l * NP + m] + r.gyb * Dy[l * NP + m]);
+            pxx += gx * mk[0][l] + gy * mk[1][l];
+            pxy += gx * mk[1][l] + gy * mk[2][l];
+            pyy += gx * mk[2][l] + gy * mk[3][l];
+        }
+        o[3 * NP + m] = (pxx + 0.5 * pyy) * tc5;
+        o[4 * NP + m] = 0.5 * pxy * tc5;
+        o[5 * NP + m] = 0.5 * pxy * tc5;
+        o[6 * NP + m] = (0.5 * pxx + pyy) * tc5;
+    }
+}
+
+// Kinetic wall-trace moments (global_solve.py:31-53), one thread per (wall face, face DOF).
+__global__ void wall_trace_kernel(const double *vdf, const double *tri_fc_fc, const double *cx,
+                                  const double *cy, const double *w, int ndir, int nt, int NP, int NF,
+                                  int nk, const int32_t *tri_list, const int32_t *lfc_list, double *out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nk * NF) return;
+    const int k = t / NF, m = t % NF;
+    const int tri = tri_list[k], lfc = lfc_list[k];
+    double c[16];
+    for (int l = 0; l < NP; ++l) c[l] = tri_fc_fc[(((size_t)l * NF + m) * nt + tri) * 3 + lfc];
+    double tb = 0.0, qxb = 0.0, qyb = 0.0;
+    for (int d = 0; d < ndir; ++d) {
+        const double *f = vdf + ((size_t)d * nt + tri) * NP;
+        double tt = 0.0;
+        for (int l = 0; l < NP; ++l) tt += f[l] * c[l];
+        tb += tt * w[d];
+        qxb += cx[d] * tt * w[d];
+        qyb += cy[d] * tt * w[d];
+    }
+    out[(size_t)k * 3 * NF + m] = tb;
+    out[(size_t)k * 3 * NF + NF + m] = qxb;
+    out[(size_t)k * 3 * NF + 2 * NF + m] = qyb;
+}
+
+// Damped correction (correction.py:29-75): one thread per (element, DOF).
+__global__ void correct_kernel(double *vdf, const double *uq, const double *cx, const double *cy,
+                               const double *w, const double *tri_hmin, int ndir, int nt, int NP,
+                               double cv, double vg, double tau_r, double tau_n, double tau_c,
+                               double tau_thr, int use_hmin, double *ts, double *qxs, double *qys) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nt * NP) return;
+    const int i = t / NP, m = t % NP;
+    const double drift = tau_c / tau_n * 3.0 / 4.0 / kPi / vg / vg;
+    const double tau_loc = use_hmin ? tau_r / tri_hmin[i] : tau_r;
+    const double beta = fmin(tau_loc, tau_thr) / tau_loc;
+    double tv = 0.0, qxv = 0.0, qyv = 0.0;
+    for (int d = 0; d < ndir; ++d) {
+        const double f = vdf[(size_t)d * nt * NP + t];
+        tv += f * w[d];
+        qxv += cx[d] * f * w[d];
+        qyv += cy[d] * f * w[d];
+    }
+    tv = tv / cv;
+    const double lt = (uq[(size_t)m * nt + i] - tv) * beta;
+    const double lqx = (uq[(size_t)(NP + m) * nt + i] - qxv) * beta;
+    const double lqy = (uq[(size_t)(2 * NP + m) * nt + i] - qyv) * beta;
+    const double eq = lt * cv / 4.0 / kPi;
+    for (int d = 0; d < ndir; ++d) {
+        double *f = vdf + (size_t)d * nt * NP + t;
+        *f = *f + eq + (cx[d] * lqx + cy[d] * lqy) * drift;
+    }
+    ts[(size_t)m * nt + i] = lt + tv;
+    qxs[(size_t)m * nt + i] = lqx + qxv;
+    qys[(size_t)m * nt + i] = lqy + qyv;
+}
+
+// Batched Gauss-Jordan inverse with partial pivoting, one warp per matrix,
+// the augmented [A | I] rows held in shared memory.
+__global__ void batched_inverse_kernel(const double *a, double *inv, int n, int m, int32_t *singular) {
+    extern __shared__ double sm[];
+    const int warps = blockDim.x / 32;
+    const int wid = threadIdx.x / 32, lane = threadIdx.x % 32;
+    const int id = blockIdx.x * warps + wid;
+    double *M = sm + (size_t)wid * m * 2 * m;
+    if (id >= n) return;
+    const int w2 = 2 * m;
+    for (int k = lane; k < m * w2; k += 32) {
+        const int r = k / w2, c = k % w2;
+        M[k] = c < m ? a[(size_t)id * m * m + r * m + c] : (c - m == r ? 1.0 : 0.0);
+    }
+    __syncwarp();
+    int sing = 0;
+    for (int k = 0; k < m; ++k) {
+        // pivot: first maximum |M[r][k]|, r >= k
+        double best = -1.0;
+        int p = k;
+        for (int r = k + lane; r < m; r += 32) {
+            const double v = fabs(M[r * w2 + k]);
+            if (v > best) { best = v; p = r; }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ob = __shfl_down_sync(0xffffffffu, best, o);
+            const int op = __shfl_down_sync(0xffffffffu, p, o);
+            if (ob > best || (ob == best && op < p)) { best = ob; p = op; }
+        }
+        p = __shfl_sync(0xffffffffu, p, 0);
+        if (p != k)
+            for (int c = lane; c < w2; c += 32) {
+                const double t = M[k * w2 + c]; M[k * w2 + c] = M[p * w2 + c]; M[p * w2 + c] = t;
+            }
+        __syncwarp();
+        const double piv = M[k * w2 + k];
+        if (piv == 0.0) { sing = 1; continue; }
+        const double rp = 1.0 / piv;
+        for (int c = lane; c < w2; c += 32) M[k * w2 + c] *= rp;
+        __syncwarp();
+        for (int r = 0; r < m; ++r) {
+            if (r == k) continue;
+            const double fct = M[r * w2 + k];
+            __syncwarp();
+            for (int c = lane; c < w2; c += 32) M[r * w2 + c] -= fct * M[k * w2 + c];
+            __syncwarp();
+        }
+    }
+    for (int k = lane; k < m * m; k += 32) inv[(size_t)id * m * m + k] = M[(k / m) * w2 + m + k % m];
+    if (sing && lane == 0) atomicAdd(singular, 1);
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+template <typename T>
+static SweepParams<T> make_params(pbte_ctx *c) {
+    SweepParams<T> P{};
+    P.cx = c->d_cx; P.cy = c->d_cy;
+    P.dir_class = c->d_dir_class; P.class_off = c->d_class_lvl_off; P.class_nlev = c->d_class_nlev;
+    P.lvl_ptr = c->d_lvl_ptr; P.lvl_cells = c->d_lvl_cells;
+    P.singular = c->d_singular; P.done = c->done;
+    P.nt = c->n_tris; P.n_faces = c->n_faces;
+    P.inv_tau_c = (T)(1.0 / c->tau_c);
+    P.ca = (T)(c->cv / (4.0 * kPi) * (1.0 / c->tau_r + 1.0 / c->tau_n));
+    P.cb = (T)(3.0 / (4.0 * kPi) / (c->vg * c->vg) / c->tau_n);
+    P.wall_scale = (T)1;
+    return P;
+}
+
+int launch_sources(pbte_ctx *c, const double *ts, const double *qxs, const double *qys, bool f32,
+                   cudaStream_t s) {
+    const int th = 128, bl = (c->n_tris + th - 1) / th;
+    if (f32)
+        sources_kernel<float><<<bl, th, 0, s>>>(c->d_cells64, c->d_ref64, ts, qxs, qys, c->d_S32, c->n_tris, c->nd, c->done);
+    else
+        sources_kernel<double><<<bl, th, 0, s>>>(c->d_cells64, c->d_ref64, ts, qxs, qys, c->d_S64, c->n_tris, c->nd, c->done);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+template <typename T, bool PRE>
+static int sweep_dispatch(pbte_ctx *c, SweepParams<T> P, cudaStream_t s) {
+    switch (c->deg) {
+        case 1: sweep_kernel<T, 1, PRE><<<c->ndir, kSweepThreads, 0, s>>>(P); break;
+        case 2: sweep_kernel<T, 2, PRE><<<c->ndir, kSweepThreads, 0, s>>>(P); break;
+        case 3: sweep_kernel<T, 3, PRE><<<c->ndir, kSweepThreads, 0, s>>>(P); break;
+        case 4: sweep_kernel<T, 4, PRE><<<c->ndir, kSweepThreads, 0, s>>>(P); break;
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_sweep64(pbte_ctx *c, double *vdf, const double *fw, const double *pbuf, int use_pbuf,
+                   cudaStream_t s) {
+    SweepParams<double> P = make_params<double>(c);
+    P.cells = c->d_cells64; P.ref = c->d_ref64; P.S = c->d_S64; P.vdf = vdf;
+    P.flux_wall = fw; P.pbuf = pbuf; P.use_pbuf = use_pbuf;
+    P.lu = c->d_lu; P.piv = c->d_piv;
+    if (c->d_lu) return sweep_dispatch<double, true>(c, P, s);
+    return sweep_dispatch<double, false>(c, P, s);
+}
+
+int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale, cudaStream_t s) {
+    SweepParams<float> P = make_params<float>(c);
+    P.cells = c->d_cells32; P.ref = c->d_ref32; P.S = c->d_S32; P.vdf = vdf32;
+    P.flux_wall = fw; P.wall_scale = (float)wall_scale;
+    return sweep_dispatch<float, false>(c, P, s);
+}
+
+int launch_factorise(pbte_ctx *c, cudaStream_t s) {
+    SweepParams<double> P = make_params<double>(c);
+    P.cells = c->d_cells64; P.ref = c->d_ref64;
+    const int th = 128;
+    const size_t total = (size_t)c->ndir * c->n_tris;
+    const int bl = (int)std::min<size_t>((total + th - 1) / th, 152 * 16);
+    switch (c->deg) {
+        case 1: factorise_kernel<1><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
+        case 2: factorise_kernel<2><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
+        case 3: factorise_kernel<3><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
+        case 4: factorise_kernel<4><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+template <typename T>
+static int moments_impl(pbte_ctx *c, const T *vdf, double *ts, double *qxs, double *qys, double *temp,
+                        double *qx, double *qy, cudaStream_t s) {
+    const int total = c->n_tris * c->nd, th = 256;
+    moments_kernel<T><<<(total + th - 1) / th, th, 0, s>>>(vdf, c->d_cx, c->d_cy, c->d_w, c->ndir, c->n_tris,
+                                                          c->nd, c->cv, ts, qxs, qys, c->done);
+    element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts, qxs, qys, c->d_int_tri, c->n_tris,
+                                                                     c->nd, c->cv, temp, qx, qy, c->done);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_moments64(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys, double *temp,
+                     double *qx, double *qy, cudaStream_t s) {
+    return moments_impl<double>(c, vdf, ts, qxs, qys, temp, qx, qy, s);
+}
+
+int launch_moments32(pbte_ctx *c, const float *vdf, double *ts, double *qxs, double *qys, double *temp,
+                     double *qx, double *qy, cudaStream_t s) {
+    return moments_impl<float>(c, vdf, ts, qxs, qys, temp, qx, qy, s);
+}
+
+template <typename T>
+static int wall_flux_impl(pbte_ctx *c, const T *vdf, double *fw, cudaStream_t s) {
+    if (c->n_wall_ad == 0) return PBTE_OK;
+    const int th = 64;
+    const size_t shm = (size_t)th * (c->nd + 1) * sizeof(double);
+    wall_flux_kernel<T><<<c->n_wall_ad, th, shm, s>>>(vdf, c->d_wall_ad, c->d_cells64, c->d_ref64 + 3 * c->nd * c->nd,
+                                                      c->d_cx, c->d_cy, c->d_w, c->ndir, c->n_tris, c->nd, fw,
+                                                      c->done);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_wall_flux64(pbte_ctx *c, const double *vdf, double *fw, cudaStream_t s) { return wall_flux_impl<double>(c, vdf, fw, s); }
+int launch_wall_flux32(pbte_ctx *c, const float *vdf, double *fw, cudaStream_t s) { return wall_flux_impl<float>(c, vdf, fw, s); }
+
+int launch_residual(pbte_ctx *c, const double *temp, double *t_old, double *out, cudaStream_t s) {
+    residual_kernel<<<1, 1024, 0, s>>>(temp, t_old, c->n_tris, out, c->done);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_residual_check(pbte_ctx *c, const double *res, double tol, int64_t tmax, int32_t *done,
+                          int64_t *count, double *hist, int64_t hist_cap, cudaStream_t s) {
+    (void)c;
+    residual_check_kernel<<<1, 1, 0, s>>>(res, tol, tmax, done, count, hist, hist_cap);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                              const double *vdf, const double *fw, const double *pbuf, double *num,
+                              double *den, cudaStream_t s) {
+    int rc = launch_sources(c, ts, qxs, qys, false, s);
+    if (rc) return rc;
+    SweepParams<double> P = make_params<double>(c);
+    P.done = nullptr;
+    P.cells = c->d_cells64; P.ref = c->d_ref64; P.S = c->d_S64; P.vdf = const_cast<double *>(vdf);
+    P.flux_wall = fw; P.pbuf = pbuf; P.use_pbuf = 0;
+    switch (c->deg) {
+        case 1: transport_residual_kernel<1><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        case 2: transport_residual_kernel<2><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        case 3: transport_residual_kernel<3><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        case 4: transport_residual_kernel<4><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+    scale_by_weight_kernel<<<(c->ndir + 127) / 128, 128, 0, s>>>(num, den, c->d_w, c->ndir);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s) {
+    const int th = 128;
+    hot_source_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(vdf, c->d_cells64, c->d_ref64, c->d_cx, c->d_cy,
+                                                              c->d_w, c->ndir, c->n_tris, c->nd, tc5, work);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk, const int32_t *tri_list,
+                      const int32_t *lfc_list, double *out, cudaStream_t s) {
+    if (nk <= 0) return PBTE_OK;
+    const int th = 128, total = nk * c->nf;
+    wall_trace_kernel<<<(total + th - 1) / th, th, 0, s>>>(vdf, tri_fc_fc, c->d_cx, c->d_cy, c->d_w, c->ndir,
+                                                          c->n_tris, c->nd, c->nf, nk, tri_list, lfc_list, out);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_hmin, double tau_thr,
+                   int use_hmin, double *ts, double *qxs, double *qys, double *temp, double *qx, double *qy,
+                   cudaStream_t s) {
+    const int th = 256, total = c->n_tris * c->nd;
+    correct_kernel<<<(total + th - 1) / th, th, 0, s>>>(vdf, uq, c->d_cx, c->d_cy, c->d_w, tri_hmin, c->ndir,
+                                                       c->n_tris, c->nd, c->cv, c->vg, c->tau_r, c->tau_n,
+                                                       c->tau_c, tau_thr, use_hmin, ts, qxs, qys);
+    element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts, qxs, qys, c->d_int_tri, c->n_tris, c->nd,
+                                                                     c->cv, temp, qx, qy, nullptr);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_batched_inverse(const double *a, double *inv, int n, int m, int32_t *singular, cudaStream_t s) {
+    if (n <= 0) return PBTE_OK;
+    if (m <= 0 || m > 64) return PBTE_ERR_ARG;
+    const int warps = 4;
+    const size_t shm = (size_t)warps * m * 2 * m * sizeof(double);
+    if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
+    if (shm > 48 * 1024 &&
+        cudaFuncSetAttribute(batched_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
+        return PBTE_ERR_CUDA;
+    batched_inverse_kernel<<<(n + warps - 1) / warps, warps * 32, shm, s>>>(a, inv, n, m, singular);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+}  // namespace pbte

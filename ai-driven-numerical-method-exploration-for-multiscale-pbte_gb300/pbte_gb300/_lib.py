@@ -1,0 +1,143 @@
+"""ctypes binding of ``libpbte_gb300.so`` (the C ABI declared in
+``include/pbte_gb300.h``) and its in-tree build.
+
+The library is the only compute path: if it is missing or fails to load,
+every GPU entry point raises -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from pathlib import Path
+
+PKG_ROOT = Path(__file__).resolve().parent.parent          # holds csrc/ and _build/
+REPO_ROOT = PKG_ROOT.parent
+CSRC = PKG_ROOT / "csrc"
+INCLUDE = REPO_ROOT / "include"
+LIB_PATH = PKG_ROOT / "_build" / "libpbte_gb300.so"
+SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_capi.cu"]
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+PBTE_OK = 0
+ERRORS = {-1: "bad argument", -2: "CUDA runtime error", -3: "sweep graph has a cycle",
+          -4: "configuration not supported", -5: "device wait timed out",
+          -6: "singular element operator", -7: "device allocation failed"}
+
+
+class PbteError(RuntimeError):
+    def __init__(self, code: int, what: str):
+        self.code = code
+        super().__init__(f"{what}: {ERRORS.get(code, 'error')} (status {code})")
+
+
+def _sources() -> list[Path]:
+    return [CSRC / s for s in SOURCES if (CSRC / s).exists()]
+
+
+def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile the library for sm_103a with nvcc (one shared object)."""
+    srcs = _sources()
+    deps = srcs + list(CSRC.glob("*.cuh")) + [INCLUDE / "pbte_gb300.h"]
+    if LIB_PATH.exists() and not force:
+        t = LIB_PATH.stat().st_mtime
+        if all(p.stat().st_mtime <= t for p in deps):
+            return LIB_PATH
+    LIB_PATH.parent.mkdir(exist_ok=True)
+    nvcc = os.environ.get("NVCC", "nvcc")
+    objs = []
+    procs = []
+    for s in srcs:
+        o = LIB_PATH.parent / (s.stem + ".o")
+        objs.append(o)
+        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+               f"-I{INCLUDE}", f"-I{CSRC}", str(s), "-o", str(o)]
+        procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
+    for cmd, p in procs:
+        out, _ = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"nvcc failed: {' '.join(cmd)}\n{out.decode()}")
+        if verbose:
+            print(out.decode())
+    tmp = LIB_PATH.with_suffix(f".{os.getpid()}.tmp")
+    subprocess.run([nvcc, ARCH, "-shared", "-o", str(tmp)] + [str(o) for o in objs]
+                   + ["-lcudart"], check=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+_d = ctypes.POINTER(ctypes.c_double)
+_i32 = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+
+class CaseDesc(ctypes.Structure):
+    """Mirror of ``pbte_case_desc``."""
+    _fields_ = [("n_tris", ctypes.c_int32), ("n_faces", ctypes.c_int32), ("ndof", ctypes.c_int32),
+                ("ndof_fc", ctypes.c_int32), ("ndir", ctypes.c_int32), ("nbc", ctypes.c_int32),
+                ("cv", ctypes.c_double), ("vg", ctypes.c_double), ("tau_r", ctypes.c_double),
+                ("tau_n", ctypes.c_double), ("tau_c", ctypes.c_double),
+                ("cxv", _d), ("cyv", _d), ("domega", _d),
+                ("ref_mass", _d), ("ref_dx", _d), ("ref_dy", _d), ("ref_edge", _d),
+                ("edge_dofs", _i32), ("area2", _d), ("dxi", _d), ("deta", _d),
+                ("edge_scale", _d), ("nx", _d), ("ny", _d), ("tri_faces", _i32),
+                ("upwind_tri", _i32), ("edge_map", _i32), ("face_bc", _i32),
+                ("face_tri", _i32), ("face_lfc", _i32), ("bc_type", _i32), ("bc_temp", _d),
+                ("int_tri", _d)]
+
+
+_SIGS = {
+    "pbte_ctx_create": ([ctypes.POINTER(CaseDesc), ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
+    "pbte_ctx_destroy": ([_vp], ctypes.c_int),
+    "pbte_ctx_info": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                       ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "pbte_sweep": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp], ctypes.c_int),
+    "pbte_sweep_f32": ([_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, _vp], ctypes.c_int),
+    "pbte_moments": ([_vp] + [_vp] * 7 + [_vp], ctypes.c_int),
+    "pbte_moments_f32": ([_vp] + [_vp] * 7 + [_vp], ctypes.c_int),
+    "pbte_wall_flux": ([_vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_wall_flux_f32": ([_vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_residual_iterate": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_set_done_flag": ([_vp, _vp], ctypes.c_int),
+    "pbte_residual_check": ([_vp, _vp, ctypes.c_double, ctypes.c_int64, _vp, _vp, _vp,
+                             ctypes.c_int64, _vp], ctypes.c_int),
+    "pbte_transport_residual": ([_vp] + [_vp] * 9 + [_vp], ctypes.c_int),
+    "pbte_hot_source": ([_vp, _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
+    "pbte_wall_trace": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],
+                     ctypes.c_int),
+    "pbte_batched_inverse": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+    "pbte_version": ([], ctypes.c_char_p),
+}
+
+_lib = None
+
+
+def lib():
+    """Load (building first if needed) the library; raises if unavailable."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        build()
+    try:
+        handle = ctypes.CDLL(str(LIB_PATH))
+    except OSError as e:
+        raise RuntimeError(f"cannot load {LIB_PATH}: {e}; the GPU path has no fallback") from e
+    for name, (args, res) in _SIGS.items():
+        fn = getattr(handle, name, None)
+        if fn is None:
+            continue
+        fn.argtypes = args
+        fn.restype = res
+    _lib = handle
+    return _lib
+
+
+def check(status: int, what: str) -> None:
+    if status != PBTE_OK:
+        raise PbteError(status, what)
+
+
+def exported_symbols() -> list[str]:
+    return [n for n in _SIGS]

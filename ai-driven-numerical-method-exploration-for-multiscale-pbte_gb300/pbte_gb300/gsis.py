@@ -1,0 +1,293 @@
+"""GSIS / HDG macroscopic acceleration on the device (``pybte/acceleration/``).
+
+Per outer iteration, after the sweep (``acceleration/__init__.py:95-115``):
+
+1. hot source: third-order angular moments of the kinetic solution contracted
+   with the gradient tensors (device kernel), premultiplied by the element
+   inverses ``inv_aa_sol`` (batched product);
+2. trace right-hand side: ``BA_SOL @ AA_SRC`` from the one or two elements of
+   each face, wall rows imposed from the kinetic wall traces (device);
+3. trace solve with the once-factorised global matrix;
+4. local recovery ``UQ = AA_SRC + sum AA_TRACE @ U_TRACE`` (batched product);
+5. damped correction of the distribution and the moments (device kernel).
+
+Setup (``assembly.py:44-269``) builds the 7x7-block element matrices on the
+host, inverts them with the library's batched Gauss-Jordan kernel, forms
+``AA_TRACE``, ``BA_SOL`` and the sparse trace matrix, and factorises it once.
+The defect-repair experiment of the reference (off by default there) is not
+carried.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib
+from .constants import BC_NONTHERMALISING, BC_PERIODIC, BC_THERMALISING
+from .trace_solver import TraceSolver
+
+__all__ = ["GSIS", "local_blocks"]
+
+
+def _mirror_perm(nf):
+    base = np.arange(nf)[::-1]
+    return np.concatenate([base + b * nf for b in range(3)])
+
+
+def local_blocks(disc, st, variant):
+    """Element matrices ``AA_SOL`` (n, 7nd, 7nd) and trace couplings ``T``
+    (n, 3, 7nd, 3nf) of ``build_local_operators`` (``assembly.py:44-125``)."""
+    c, m, it = disc.case, disc.mesh, disc.integrals
+    nd, nf = disc.ndof, c.ndof_fc
+    n = m.n_tris
+    tau_r, tau_c, cv = c.flow.tau_r, c.tau_c, c.flow.cv
+    scale = tau_r if variant == "B" else 1.0
+    aa, bb = it.int_tri_tri_x, it.int_tri_tri_y
+    cc, dd = np.transpose(aa, (0, 2, 1)), np.transpose(bb, (0, 2, 1))
+    pp = it.int_tri_fc.sum(axis=1)
+    oo = np.transpose(it.int_tri_tri, (2, 0, 1))
+    A = np.zeros((n, 7 * nd, 7 * nd))
+
+    def put(r, col, v):
+        A[:, r * nd:(r + 1) * nd, col * nd:(col + 1) * nd] = v
+    put(0, 0, st[0] * pp); put(0, 1, cc); put(0, 2, dd)
+    put(1, 0, -aa * cv / 3.0 * scale)
+    put(1, 1, (oo + st[1] * pp) if variant == "B" else (st[1] * pp + oo / tau_r))
+    put(1, 3, -4.0 / 3.0 * cc); put(1, 4, -dd); put(1, 5, -dd); put(1, 6, 2.0 / 3.0 * cc)
+    put(2, 0, -bb * cv / 3.0 * scale)
+    put(2, 2, (oo + st[2] * pp) if variant == "B" else (st[2] * pp + oo / tau_r))
+    put(2, 3, 2.0 / 3.0 * dd); put(2, 4, -cc); put(2, 5, -cc); put(2, 6, -4.0 / 3.0 * dd)
+    tc5 = tau_c * scale / 5.0
+    put(3, 1, aa * tc5); put(3, 3, oo); put(4, 1, bb * tc5); put(4, 4, oo)
+    put(5, 2, aa * tc5); put(5, 5, oo); put(6, 2, bb * tc5); put(6, 6, oo)
+
+    ww = np.transpose(it.int_tri_fc_fc, (2, 3, 0, 1))           # (n, 3, nd, nf)
+    nxe = m.tri_normal[:, :, 0][:, :, None, None]
+    nye = m.tri_normal[:, :, 1][:, :, None, None]
+    T = np.zeros((n, 3, 7 * nd, 3 * nf))
+
+    def tput(r, col, v):
+        T[:, :, r * nd:(r + 1) * nd, col * nf:(col + 1) * nf] = v
+    tput(0, 0, st[0] * ww)
+    tput(1, 0, -nxe * ww * cv / 3.0 * scale); tput(1, 1, st[1] * ww)
+    tput(2, 0, -nye * ww * cv / 3.0 * scale); tput(2, 2, st[2] * ww)
+    tput(3, 1, nxe * ww * tc5); tput(4, 1, nye * ww * tc5)
+    tput(5, 2, nxe * ww * tc5); tput(6, 2, nye * ww * tc5)
+    return A, T, tc5
+
+
+def ba_sol_blocks(disc, st, variant):
+    """``BA_SOL`` (n, 3, 3nf, 7nd) of ``build_ba_sol`` (``assembly.py:128-184``)."""
+    c, m, it = disc.case, disc.mesh, disc.integrals
+    nd, nf = disc.ndof, c.ndof_fc
+    bc_type = disc.bcdata.bc_type
+    B = np.zeros((m.n_tris, 3, 3 * nf, 7 * nd))
+    bb2 = np.transpose(it.int_tri_fc_fc, (2, 3, 1, 0))
+    nx = m.tri_normal[:, :, 0][:, :, None, None]
+    ny = m.tri_normal[:, :, 1][:, :, None, None]
+    fb = m.face_bc[m.tri_faces]
+    code = np.where(fb >= 0, bc_type[np.clip(fb, 0, None)], 0)
+    interior = fb < 0
+    std = (interior | ((~interior) & (code == BC_PERIODIC)))[:, :, None, None]
+    wall_th = ((~interior) & (code == BC_THERMALISING))[:, :, None, None]
+
+    def put(r, col, v, mask):
+        sl = (slice(None), slice(None), slice(r * nf, (r + 1) * nf), slice(col * nd, (col + 1) * nd))
+        B[sl] = np.where(mask, v, B[sl])
+    put(0, 0, 0.5 * bb2, std); put(0, 1, nx / 2.0 / st[0] * bb2, std); put(0, 2, ny / 2.0 / st[0] * bb2, std)
+    put(1, 1, 0.5 * bb2, std); put(1, 3, -2.0 * nx / 3.0 / st[1] * bb2, std)
+    put(1, 4, -ny / 2.0 / st[1] * bb2, std); put(1, 5, -ny / 2.0 / st[1] * bb2, std)
+    put(1, 6, nx / 3.0 / st[1] * bb2, std)
+    put(2, 2, 0.5 * bb2, std); put(2, 3, ny / 3.0 / st[2] * bb2, std)
+    put(2, 4, -nx / 2.0 / st[2] * bb2, std); put(2, 5, -nx / 2.0 / st[2] * bb2, std)
+    put(2, 6, -2.0 * ny / 3.0 / st[2] * bb2, std)
+    if variant == "A":
+        put(1, 1, bb2, wall_th); put(1, 3, -4.0 * nx / 3.0 / st[1] * bb2, wall_th)
+        put(1, 4, -ny / st[1] * bb2, wall_th); put(1, 5, -ny / st[1] * bb2, wall_th)
+        put(1, 6, 2.0 * nx / 3.0 / st[1] * bb2, wall_th)
+        put(2, 2, bb2, wall_th); put(2, 3, 2.0 * ny / 3.0 / st[2] * bb2, wall_th)
+        put(2, 4, -nx / st[2] * bb2, wall_th); put(2, 5, -nx / st[2] * bb2, wall_th)
+        put(2, 6, -4.0 * ny / 3.0 / st[2] * bb2, wall_th)
+    return B
+
+
+class GSIS:
+    def __init__(self, solver):
+        from scipy.sparse import coo_matrix
+
+        s = solver
+        disc = s.disc
+        c, m, it = disc.case, disc.mesh, disc.integrals
+        self.s = s
+        dev = s.device
+        nd, nf = disc.ndof, c.ndof_fc
+        self.nd, self.nf = nd, nf
+        self.variant = c.scheme.acc_variant
+        st = np.asarray(c.scheme.stabilisation, dtype=float).copy()
+        if c.scheme.scale_by_hmin:
+            st[1] /= m.hmin
+            st[2] /= m.hmin
+        self.st = st
+        n = m.n_tris
+        A, T, self.tc5 = local_blocks(disc, st, self.variant)
+        f64 = dict(dtype=torch.float64, device=dev)
+        A_d = torch.from_numpy(A).to(dev)
+        inv = torch.empty_like(A_d)
+        bad = torch.zeros(1, dtype=torch.int32, device=dev)
+        _lib.check(_lib.lib().pbte_batched_inverse(A_d.data_ptr(), inv.data_ptr(), n, 7 * nd, bad.data_ptr(),
+                                                   torch.cuda.current_stream().cuda_stream), "batched_inverse")
+        if int(bad.item()):
+            raise np.linalg.LinAlgError(f"{int(bad.item())} singular HDG element matrices")
+        del A_d
+        self.inv_aa_sol = inv                                           # (n, 7nd, 7nd)
+        T_d = torch.from_numpy(T).to(dev)
+        self.aa_trace = torch.einsum("ipq,ilqr->ilpr", inv, T_d).contiguous()   # (n, 3, 7nd, 3nf)
+        del T_d
+        B = ba_sol_blocks(disc, st, self.variant)
+        self.ba_sol = torch.from_numpy(B).to(dev)                        # (n, 3, 3nf, 7nd)
+
+        bc_type = disc.bcdata.bc_type
+        flip = disc.bcdata.periodic_flip
+        perm = _mirror_perm(nf)
+        nf3 = 3 * nf
+        adj_t, adj_l = m.adjacent_all()
+        fbc = m.face_bc
+        code = np.where(fbc >= 0, bc_type[np.clip(fbc, 0, None)], 0)
+        interior = fbc < 0
+        periodic = (~interior) & (code == BC_PERIODIC)
+        p1_tri = np.where(interior, m.face_tri[:, 0], adj_t).astype(np.int64)
+        p1_lfc = np.where(interior, m.face_lfc[:, 0], adj_l).astype(np.int64)
+        p2_tri = np.full(m.n_faces, -1, dtype=np.int64)
+        p2_lfc = np.full(m.n_faces, -1, dtype=np.int64)
+        p2_tri[interior] = m.face_tri[interior, 1]
+        p2_lfc[interior] = m.face_lfc[interior, 1]
+        if periodic.any():
+            pf = np.flatnonzero(periodic)
+            p2_tri[pf] = adj_t[m.face_pair[pf]]
+            p2_lfc[pf] = adj_l[m.face_pair[pf]]
+        has_p2 = p2_tri >= 0
+        mirror2 = periodic & flip
+
+        # global trace matrix K (assembly.py:200-269), blocks formed on the device
+        rows, cols, vals = [], [], []
+        diag = np.zeros((m.n_faces, nf3, nf3))
+        for k in range(3):
+            diag[:, k * nf:(k + 1) * nf, k * nf:(k + 1) * nf] = np.transpose(it.int_fc_fc, (2, 0, 1))
+        rr, cc = np.meshgrid(np.arange(nf3), np.arange(nf3), indexing="ij")
+        fid = np.arange(m.n_faces)
+        rows.append((fid[:, None, None] * nf3 + rr).ravel())
+        cols.append((fid[:, None, None] * nf3 + cc).ravel())
+        vals.append(diag.ravel())
+        permt = torch.from_numpy(perm).to(dev)
+        for side in (0, 1):
+            sel = np.ones(m.n_faces, bool) if side == 0 else has_p2
+            fsel = np.flatnonzero(sel)
+            tri = (p1_tri if side == 0 else p2_tri)[fsel]
+            lfc = (p1_lfc if side == 0 else p2_lfc)[fsel]
+            ba = self.ba_sol[torch.from_numpy(tri).to(dev), torch.from_numpy(lfc).to(dev)]       # (k, nf3, 7nd)
+            for il in range(3):
+                at = self.aa_trace[torch.from_numpy(tri).to(dev), il]                                  # (k, 7nd, nf3)
+                D = torch.bmm(ba, at)
+                if side == 1 and mirror2[fsel].any():
+                    mm = torch.from_numpy(mirror2[fsel]).to(dev)
+                    D[mm] = D[mm][:, permt]
+                g = m.tri_faces[tri, il]
+                rows.append((fsel[:, None, None] * nf3 + rr).ravel())
+                cols.append((g[:, None, None] * nf3 + cc).ravel())
+                vals.append((-D).cpu().numpy().ravel())
+        nn = m.n_faces * nf3
+        K = coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                       shape=(nn, nn)).tocsr()
+        K.sum_duplicates()
+        drop = 1e-30 if self.variant == "A" else 0.0
+        K.data[np.abs(K.data) <= drop] = 0.0
+        K.eliminate_zeros()
+        K.sort_indices()
+        self.K = K
+        self.solver = TraceSolver(K, dev)
+
+        # per-iteration bookkeeping (global_solve.py:88-117)
+        self.p1 = (torch.from_numpy(p1_tri).to(dev), torch.from_numpy(p1_lfc).to(dev))
+        sel2 = np.flatnonzero(has_p2)
+        self.sel2 = torch.from_numpy(sel2).to(dev)
+        self.p2 = (torch.from_numpy(p2_tri[sel2]).to(dev), torch.from_numpy(p2_lfc[sel2]).to(dev))
+        self.ba1 = self.ba_sol[self.p1].contiguous()
+        self.ba2 = self.ba_sol[self.p2].contiguous()
+        self.flip2 = torch.from_numpy(mirror2[sel2]).to(dev)
+        self.perm = permt
+        wall_th = np.flatnonzero((fbc >= 0) & (code == BC_THERMALISING))
+        wall_ad = np.flatnonzero((fbc >= 0) & (code == BC_NONTHERMALISING))
+        self.wall_all = np.concatenate([wall_th, wall_ad])
+        self.n_th = wall_th.size
+        self.wall_idx = torch.from_numpy(self.wall_all).to(dev)
+        self.wall_tri = torch.from_numpy(p1_tri[self.wall_all].astype(np.int32)).to(dev)
+        self.wall_lfc = torch.from_numpy(p1_lfc[self.wall_all].astype(np.int32)).to(dev)
+        wnx = m.tri_normal[p1_tri[wall_ad], p1_lfc[wall_ad], 0]
+        wny = m.tri_normal[p1_tri[wall_ad], p1_lfc[wall_ad], 1]
+        self.ad_nx = torch.from_numpy(wnx).to(dev)
+        self.ad_ny = torch.from_numpy(wny).to(dev)
+        self.tri_fc_fc = torch.from_numpy(np.ascontiguousarray(it.int_tri_fc_fc)).to(dev)
+        self.tri_faces = torch.from_numpy(m.tri_faces.astype(np.int64)).to(dev)
+        self.tri_hmin = torch.from_numpy(np.ascontiguousarray(m.tri_hmin)).to(dev)
+        self.use_hmin = self.variant == "A"
+        self.work = torch.zeros((n, 7 * nd), **f64)
+        self.wall_mom = torch.zeros((max(1, self.wall_all.size), nf3), **f64)
+        self.ffa = torch.zeros((nf3, m.n_faces), **f64)
+        self.uq = torch.zeros((7 * nd, n), **f64)
+        self.solve_count = 0
+
+    def rhs(self, aa_src: torch.Tensor, vdf: torch.Tensor, stream=None) -> torch.Tensor:
+        """``GlobalSolver.rhs`` (``global_solve.py:131-187``)."""
+        nf = self.nf
+        src_t = aa_src.T                                   # (n, 7nd)
+        ffa = torch.bmm(self.ba1, src_t[self.p1[0]].unsqueeze(-1)).squeeze(-1)   # (n_faces, nf3)
+        if self.sel2.numel():
+            c2 = torch.bmm(self.ba2, src_t[self.p2[0]].unsqueeze(-1)).squeeze(-1)
+            if bool(self.flip2.any()):
+                c2[self.flip2] = c2[self.flip2][:, self.perm]
+            ffa.index_add_(0, self.sel2, c2)
+        if self.wall_all.size:
+            s = (stream or torch.cuda.current_stream()).cuda_stream
+            _lib.check(_lib.lib().pbte_wall_trace(self.s.ctx.handle, vdf.data_ptr(), self.tri_fc_fc.data_ptr(),
+                                                  int(self.wall_all.size), self.wall_tri.data_ptr(),
+                                                  self.wall_lfc.data_ptr(), self.wall_mom.data_ptr(), s),
+                       "wall_trace")
+            mom = self.wall_mom
+            cv = self.s.case.flow.cv
+            th = self.wall_idx[:self.n_th]
+            ad = self.wall_idx[self.n_th:]
+            if self.n_th:
+                ffa[th, 0:nf] = mom[:self.n_th, 0:nf] / cv
+                if self.variant == "B":
+                    ffa[th, nf:3 * nf] = mom[:self.n_th, nf:3 * nf]
+            if ad.numel():
+                ffa[ad, 0:nf] = mom[self.n_th:, 0:nf] / cv
+                qxb = mom[self.n_th:, nf:2 * nf]
+                qyb = mom[self.n_th:, 2 * nf:3 * nf]
+                nx = self.ad_nx[:, None]
+                ny = self.ad_ny[:, None]
+                ffa[ad, nf:2 * nf] = qxb * (ny * ny) - qyb * (nx * ny)
+                ffa[ad, 2 * nf:3 * nf] = -qxb * (nx * ny) + qyb * (nx * nx)
+        return ffa                                          # (n_faces, nf3): Fortran-flattened order
+
+    def apply(self, stream=None) -> None:
+        s = self.s
+        L = _lib.lib()
+        st = (stream or torch.cuda.current_stream()).cuda_stream
+        _lib.check(L.pbte_hot_source(s.ctx.handle, s.vdf.data_ptr(), float(self.tc5), self.work.data_ptr(), st),
+                   "hot_source")
+        aa_src = torch.bmm(self.inv_aa_sol, self.work.unsqueeze(-1)).squeeze(-1).T.contiguous()   # (7nd, n)
+        ffa = self.rhs(aa_src, s.vdf, stream)
+        u_trace = self.solver.solve(ffa.reshape(-1)).reshape(-1, 3 * self.nf)                  # (n_faces, nf3)
+        self.solve_count += 1
+        traces = u_trace[self.tri_faces]                                                       # (n, 3, nf3)
+        uq = aa_src.T + torch.einsum("ilpr,ilr->ip", self.aa_trace, traces)
+        self.uq = uq.T.contiguous()
+        m = s.mom
+        _lib.check(L.pbte_correct(s.ctx.handle, s.vdf.data_ptr(), self.uq.data_ptr(), self.tri_hmin.data_ptr(),
+                                  float(s.case.flow.tau_thr), int(self.use_hmin), m.ts.data_ptr(),
+                                  m.qxs.data_ptr(), m.qys.data_ptr(), m.temp.data_ptr(), m.qx.data_ptr(),
+                                  m.qy.data_ptr(), st), "correct")
+        _ = ctypes

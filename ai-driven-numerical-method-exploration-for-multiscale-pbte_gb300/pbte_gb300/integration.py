@@ -1,0 +1,211 @@
+"""Element and face integral tensors (``pybte/integration.py:159-404``).
+
+Index order and meaning are pybte's (Fortran order, 0-based):
+
+* ``int_tri[L, I]``            ``int phi_L``
+* ``int_tri_tri[M, L, I]``     mass ``int phi_M phi_L``
+* ``int_tri_tri_x[I, M, L]``   ``int d_x(phi_M) phi_L`` (``_y`` likewise)
+* ``int_tri_fc[I, IL, M, L]``  ``int_edge phi_M phi_L`` on local edge IL
+* ``int_tri_fc_fc[M, L, I, IL]`` element basis M against face basis L on edge IL
+* ``int_fc_fc[M, L, F]``, ``int_fc[M, F]``  face-basis mass / integral
+* ``int_tri_tri_fc[I, IL, M, L]`` element I's basis against the neighbour's
+  (or the periodic partner's) basis on edge IL; on a wall edge the column
+  index is meaningless and every column holds ``int_edge phi_M``.
+
+The analytic tensors contract the monomial coefficients with the closed-form
+reference moments ``int_T xi^a eta^b = a! b! / (a+b+2)!`` (and the edge
+analogues).  The two cross-space tensors use a 15-point Gauss-Legendre rule
+along each face, walked from the face's node 1 to its node 2.
+
+Besides pybte's tensors, :class:`Integrals` keeps the element-independent
+reference matrices (``ref_mass``, ``ref_dx``, ``ref_dy``, ``ref_edge``) and
+the per-element affine factors, from which every per-element tensor above is
+one scaling away; the GPU sweep is built on that compact form.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+from math import factorial, sqrt
+
+import numpy as np
+
+from .basis import Basis
+from .constants import BC_PERIODIC
+from .mesh import Mesh
+from .quadrature import face_rule
+
+__all__ = ["Integrals", "build_integrals", "edge_nodes"]
+
+
+def edge_nodes(deg: int) -> np.ndarray:
+    """``(3, deg+1)`` element DOFs lying on local edges 0 (eta=0, node1->node2),
+    1 (xi+eta=1, node2->node3) and 2 (xi=0, node3->node1), each listed in the
+    edge's walking direction."""
+    idx = {}
+    c = 0
+    for j in range(deg + 1):
+        for i in range(deg - j + 1):
+            idx[(i, j)] = c
+            c += 1
+    e0 = [idx[(i, 0)] for i in range(deg + 1)]
+    e1 = [idx[(deg - t, t)] for t in range(deg + 1)]
+    e2 = [idx[(0, deg - t)] for t in range(deg + 1)]
+    return np.array([e0, e1, e2], dtype=np.int64)
+
+
+def _mom(a: int, b: int, extra: int = 2) -> float:
+    """``a! b! / (a+b+extra)!``."""
+    return factorial(a) * factorial(b) / factorial(a + b + extra)
+
+
+@dataclass
+class Integrals:
+    int_tri: np.ndarray
+    int_tri_tri: np.ndarray
+    int_tri_tri_x: np.ndarray
+    int_tri_tri_y: np.ndarray
+    int_tri_fc: np.ndarray
+    int_tri_fc_fc: np.ndarray
+    int_fc_fc: np.ndarray
+    int_fc: np.ndarray
+    int_tri_tri_fc: np.ndarray
+    # compact form -------------------------------------------------------
+    ref_mass: np.ndarray      # (nd, nd)
+    ref_dx: np.ndarray        # (nd, nd)  int d_xi(phi_M) phi_L
+    ref_dy: np.ndarray
+    ref_edge: np.ndarray      # (3, nd, nd) edge masses on the reference triangle
+    area2: np.ndarray         # (n_tris,)  2 * area
+    dxi: np.ndarray           # (n_tris, 2)  d(xi)/dx, d(eta)/dx
+    deta: np.ndarray          # (n_tris, 2)  d(xi)/dy, d(eta)/dy
+    edge_scale: np.ndarray    # (n_tris, 3)  len12, len23/sqrt2, len31
+
+
+def _eval_points(basis: Basis, nodes, tri_nodes_rows, xp, yp):
+    """Shape functions of the given triangles at physical points (..., q)."""
+    x = nodes[tri_nodes_rows, 0]
+    y = nodes[tri_nodes_rows, 1]
+    x1, x2, x3 = x[..., 0:1], x[..., 1:2], x[..., 2:3]
+    y1, y2, y3 = y[..., 0:1], y[..., 1:2], y[..., 2:3]
+    A = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)
+    E = (x3 - x1) * (y2 - y1) - (x2 - x1) * (y3 - y1)
+    xi = (y3 - y1) / A * xp + (x1 - x3) / A * yp + ((x3 - x1) * y1 - (y3 - y1) * x1) / A
+    eta = (y2 - y1) / E * xp + (x1 - x2) / E * yp + ((x2 - x1) * y1 - (y2 - y1) * x1) / E
+    return basis.eval_tri(xi, eta)
+
+
+def build_integrals(mesh: Mesh, basis: Basis, np_fc: int = 15, bc_codes=None,
+                    bc_xoff=None, bc_yoff=None, chunk: int = 65536) -> Integrals:
+    nd, nf, deg = basis.ndof_tri, basis.ndof_fc, basis.deg
+    mono = basis.mono
+    C = basis.nodfun_tri
+    Cf = basis.nodfun_fc
+    nodes = mesh.nodes
+    n_tris = mesh.n_tris
+    area2 = 2.0 * mesh.tri_area
+    ax, ay = mono[:, 0], mono[:, 1]
+
+    # reference moment tables ------------------------------------------
+    e_vec = np.array([_mom(a, b) for a, b in mono])
+    e_mass = np.array([[_mom(ax[m] + ax[l], ay[m] + ay[l]) for l in range(nd)] for m in range(nd)])
+    e_dx = np.array([[ax[m] * _mom(ax[m] - 1 + ax[l], ay[m] + ay[l]) if ax[m] > 0 else 0.0
+                      for l in range(nd)] for m in range(nd)])
+    e_dy = np.array([[ay[m] * _mom(ax[m] + ax[l], ay[m] - 1 + ay[l]) if ay[m] > 0 else 0.0
+                      for l in range(nd)] for m in range(nd)])
+    e_e = np.zeros((3, nd, nd))
+    for m in range(nd):
+        for l in range(nd):
+            a, b = ax[m] + ax[l], ay[m] + ay[l]
+            e_e[0, m, l] = 1.0 / (a + 1) if b == 0 else 0.0
+            e_e[1, m, l] = sqrt(2.0) * _mom(a, b, 1)
+            e_e[2, m, l] = 1.0 / (b + 1) if a == 0 else 0.0
+
+    ref_tri = C @ e_vec
+    ref_mass = C @ e_mass @ C.T
+    ref_dx = C @ e_dx @ C.T
+    ref_dy = C @ e_dy @ C.T
+    ref_edge = np.einsum("mk,ekl,nl->emn", C, e_e, C)
+
+    int_tri = ref_tri[:, None] * area2[None, :]
+    int_tri_tri = ref_mass[:, :, None] * area2[None, None, :]
+
+    x = nodes[mesh.tri_nodes, 0]
+    y = nodes[mesh.tri_nodes, 1]
+    x1, x2, x3 = x[:, 0], x[:, 1], x[:, 2]
+    y1, y2, y3 = y[:, 0], y[:, 1], y[:, 2]
+    ss = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)
+    dxi = np.stack([(y3 - y1) / ss, (y1 - y2) / ss], 1)
+    deta = np.stack([(x1 - x3) / ss, (x2 - x1) / ss], 1)
+    int_tri_tri_x = (dxi[:, 0, None, None] * ref_dx + dxi[:, 1, None, None] * ref_dy) * area2[:, None, None]
+    int_tri_tri_y = (deta[:, 0, None, None] * ref_dx + deta[:, 1, None, None] * ref_dy) * area2[:, None, None]
+
+    len12 = np.sqrt((x2 - x1) ** 2 + (y2 - y1) ** 2)
+    len23 = np.sqrt((x3 - x2) ** 2 + (y3 - y2) ** 2)
+    len31 = np.sqrt((x3 - x1) ** 2 + (y3 - y1) ** 2)
+    edge_scale = np.stack([len12, len23 / sqrt(2.0), len31], 1)
+    int_tri_fc = edge_scale[:, :, None, None] * ref_edge[None]
+
+    # face basis on [-1, 1]
+    e_line = np.array([[2.0 / (m + l + 1) if (m + l) % 2 == 0 else 0.0
+                        for l in range(nf)] for m in range(nf)])
+    ref_fc_fc = Cf @ e_line @ Cf.T
+    ref_fc = Cf @ e_line[:, 0]
+    half = 0.5 * mesh.face_len
+    int_fc_fc = ref_fc_fc[:, :, None] * half[None, None, :]
+    int_fc = ref_fc[:, None] * half[None, :]
+
+    # numerical face tensors ---------------------------------------------
+    bc_codes = np.asarray(bc_codes if bc_codes is not None else [], dtype=np.int64)
+    bc_xoff = np.asarray(bc_xoff if bc_xoff is not None else np.zeros(bc_codes.size), dtype=float)
+    bc_yoff = np.asarray(bc_yoff if bc_yoff is not None else np.zeros(bc_codes.size), dtype=float)
+
+    int_tri_fc_fc = np.zeros((nd, nf, n_tris, 3))
+    int_tri_tri_fc = np.zeros((n_tris, 3, nd, nd))
+    adj_tri, _ = mesh.adjacent_all()
+    for lo in range(0, n_tris, chunk):
+        hi = min(n_tris, lo + chunk)
+        ids = np.arange(lo, hi)
+        for j2 in range(3):
+            fc = mesh.tri_faces[ids, j2]
+            ln = mesh.face_len[fc][:, None]
+            p1 = nodes[mesh.face_nodes[fc, 0]]
+            p2 = nodes[mesh.face_nodes[fc, 1]]
+            s, w = face_rule(np_fc, ln[:, 0])
+            xp = (p2[:, 0:1] - p1[:, 0:1]) / ln * s + p1[:, 0:1]
+            yp = (p2[:, 1:2] - p1[:, 1:2]) / ln * s + p1[:, 1:2]
+            pm = _eval_points(basis, nodes, mesh.tri_nodes[ids], xp, yp)      # (k, q, nd)
+            pl_fc = basis.eval_fc(2.0 * s / ln - 1.0)                         # (k, q, nf)
+            int_tri_fc_fc[:, :, lo:hi, j2] = np.einsum("kqm,kql,kq->mlk", pm, pl_fc, w)
+
+            bc = mesh.face_bc[fc]
+            code = np.where(bc >= 0, bc_codes[np.clip(bc, 0, None)] if bc_codes.size else 0, 0)
+            interior = bc < 0
+            periodic = (bc >= 0) & (code == BC_PERIODIC)
+            other = np.full(ids.size, -1, dtype=np.int64)
+            ft = mesh.face_tri[fc]
+            other[interior] = np.where(ft[interior, 0] == ids[interior], ft[interior, 1], ft[interior, 0])
+            ox = np.zeros(ids.size)
+            oy = np.zeros(ids.size)
+            if periodic.any():
+                pair = mesh.face_pair[fc[periodic]]
+                other[periodic] = adj_tri[pair]
+                bcp = mesh.face_bc[pair]
+                ox[periodic] = bc_xoff[bcp]
+                oy[periodic] = bc_yoff[bcp]
+            coupled = other >= 0
+            if coupled.any():
+                shifted = nodes[mesh.tri_nodes[other[coupled]]] + np.stack([ox[coupled], oy[coupled]], 1)[:, None, :]
+                tmp_nodes = shifted.reshape(-1, 2)
+                rows = np.arange(tmp_nodes.shape[0]).reshape(-1, 3)
+                po = _eval_points(basis, tmp_nodes, rows, xp[coupled], yp[coupled])
+                int_tri_tri_fc[ids[coupled], j2] = np.einsum("kqm,kql,kq->kml", pm[coupled], po, w[coupled])
+            wall = ~coupled
+            if wall.any():
+                v = np.einsum("kqm,kq->km", pm[wall], w[wall])
+                int_tri_tri_fc[ids[wall], j2] = v[:, :, None]
+
+    return Integrals(int_tri=int_tri, int_tri_tri=int_tri_tri, int_tri_tri_x=int_tri_tri_x,
+                     int_tri_tri_y=int_tri_tri_y, int_tri_fc=int_tri_fc,
+                     int_tri_fc_fc=int_tri_fc_fc, int_fc_fc=int_fc_fc, int_fc=int_fc,
+                     int_tri_tri_fc=int_tri_tri_fc, ref_mass=ref_mass, ref_dx=ref_dx,
+                     ref_dy=ref_dy, ref_edge=ref_edge, area2=area2, dxi=dxi, deta=deta,
+                     edge_scale=edge_scale)

@@ -1,0 +1,272 @@
+"""GMRES on the outer fixed point, on the device (``pybte/krylov.py:55-363``).
+
+One outer step is the affine map ``u -> F(u) = T u + g`` on the state ``u``
+(moments, plus the wall emission when there are adiabatic walls); GMRES
+solves ``(I - T) u = g`` with one sweep per product.  The Krylov basis, the
+state and the products live on the device; the map ``F`` (sweep + moments +
+emission) is captured once as a CUDA graph on fixed input/output buffers.
+The Hessenberg column (``j + 2`` numbers) comes to the host each step for the
+Givens rotations, as in the reference.
+
+Orthogonalisation is classical Gram-Schmidt applied twice (the reference's
+CGS2), in FP64.  Stopping follows the reference: GMRES to
+``tol * krylov_tol_factor`` (floored at 1e-14 of ``||g||``), a bounded
+extension once under ``tol * 1e-2``, a closing sweep, and convergence
+decided on the true transport residual.  ``iterations`` counts sweeps.
+"""
+from __future__ import annotations
+
+import time
+
+import numpy as np
+import torch
+
+from . import _lib
+
+__all__ = ["FixedPointOperator", "gmres", "run_krylov"]
+
+_ENOUGH = 1.0e-2
+_FLOOR = 1.0e-14
+
+
+class FixedPointOperator:
+    """``u -> F(u)``: scatter into the sweep's inputs, sweep, moments, wall
+    emission, gather (``pybte/krylov.py:64-136``).  Periodic faces are not
+    supported by the GPU sweep's source-iteration form and are refused."""
+
+    def __init__(self, solver, precision: str = "fp64", homogeneous: bool = False):
+        s = solver
+        if s.bcdata.has_periodic:
+            raise NotImplementedError("periodic faces: the Krylov state needs the partner DOFs")
+        self.s = s
+        self.nd, self.nt = s.ndof, s.n_tris
+        self.k = self.nd * self.nt
+        self.nmom = 3 * self.k
+        self.wall = bool(s.bcdata.has_nonthermalising)
+        self.nwall = s.mesh.n_faces * self.nd if self.wall else 0
+        self.n = self.nmom + self.nwall
+        dev = s.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.uin = torch.zeros(self.n + (0 if self.wall else s.mesh.n_faces * self.nd), **f64)
+        self.uout = torch.zeros_like(self.uin)
+        self.precision = precision
+        self.homogeneous = homogeneous
+        self.vdf = s.vdf if precision == "fp64" else torch.zeros(s.vdf.shape, dtype=torch.float32, device=dev)
+        self.temp = torch.zeros(self.nt, **f64)
+        self.qx = torch.zeros(self.nt, **f64)
+        self.qy = torch.zeros(self.nt, **f64)
+        self.sweeps = 0
+        self.graph = None
+        self.stream = torch.cuda.Stream(device=dev)
+
+    def _views(self, u):
+        k = self.k
+        return (u[:k].view(self.nd, self.nt), u[k:2 * k].view(self.nd, self.nt),
+                u[2 * k:3 * k].view(self.nd, self.nt), u[3 * k:].view(-1, self.nd))
+
+    def _launch(self, s: int) -> None:
+        L = _lib.lib()
+        ctx = self.s.ctx.handle
+        ts, qxs, qys, fw = self._views(self.uin)
+        ots, oqxs, oqys, ofw = self._views(self.uout)
+        if self.precision == "fp64":
+            _lib.check(L.pbte_sweep(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), self.vdf.data_ptr(),
+                                    fw.data_ptr(), self.s.ctx.pbuf.data_ptr(), 0, s), "sweep")
+            _lib.check(L.pbte_moments(ctx, self.vdf.data_ptr(), ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(),
+                                      self.temp.data_ptr(), self.qx.data_ptr(), self.qy.data_ptr(), s), "moments")
+            if self.wall:
+                _lib.check(L.pbte_wall_flux(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux")
+        else:
+            _lib.check(L.pbte_sweep_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), self.vdf.data_ptr(),
+                                        fw.data_ptr(), 0.0 if self.homogeneous else 1.0, s), "sweep_f32")
+            _lib.check(L.pbte_moments_f32(ctx, self.vdf.data_ptr(), ots.data_ptr(), oqxs.data_ptr(),
+                                          oqys.data_ptr(), self.temp.data_ptr(), self.qx.data_ptr(),
+                                          self.qy.data_ptr(), s), "moments_f32")
+            if self.wall:
+                _lib.check(L.pbte_wall_flux_f32(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux_f32")
+
+    def _capture(self):
+        torch.cuda.synchronize(self.s.device)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=self.stream):
+            self._launch(torch.cuda.current_stream().cuda_stream)
+        self.graph = g
+
+    def apply(self, u: torch.Tensor) -> torch.Tensor:
+        if self.graph is None:
+            self._capture()
+        self.uin[:self.n].copy_(u)
+        torch.cuda.current_stream().synchronize()
+        self.graph.replay()
+        self.stream.synchronize()
+        self.sweeps += 1
+        return self.uout[:self.n].clone()
+
+    def publish(self) -> None:
+        """Copy the last product's moments into the solver's state."""
+        s = self.s
+        ts, qxs, qys, fw = self._views(self.uout)
+        s.mom.ts.copy_(ts)
+        s.mom.qxs.copy_(qxs)
+        s.mom.qys.copy_(qys)
+        s.mom.temp.copy_(self.temp)
+        s.mom.qx.copy_(self.qx)
+        s.mom.qy.copy_(self.qy)
+        if self.wall:
+            s.ctx.flux_wall.copy_(fw)
+
+
+def _back_substitute(r, y):
+    out = np.array(y, dtype=float)
+    for i in range(out.size - 1, -1, -1):
+        s = out[i] - r[i, i + 1:] @ out[i + 1:]
+        out[i] = s / r[i, i] if r[i, i] != 0.0 else 0.0
+    return out
+
+
+def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, max_basis=None,
+          callback=None):
+    """GMRES for ``A x = b`` with device vectors (``pybte/krylov.py:150-246``).
+    Returns ``(x, converged, n_matvec)``."""
+    n = b.numel()
+    x = torch.zeros_like(b) if x0 is None else x0.clone()
+    maxiter = int(n if maxiter is None else maxiter)
+    m_cap = maxiter if max_basis is None else max(1, min(int(max_basis), maxiter))
+    nmv = 0
+    converged = halted = False
+    while nmv < maxiter and not converged and not halted:
+        if bool(torch.any(x != 0).item()):
+            r = b - matvec(x)
+            nmv += 1
+            if callback is not None and callback(float(torch.linalg.vector_norm(r).item())):
+                halted = True
+                break
+        else:
+            r = b.clone()
+        beta = float(torch.linalg.vector_norm(r).item())
+        if beta <= tol_abs:
+            converged = True
+            break
+        m = min(m_cap, maxiter - nmv)
+        if m <= 0:
+            break
+        q = torch.empty((min(m, 64), n), dtype=b.dtype, device=b.device)
+        q[0] = r / beta
+        cols, cs, sn, gam = [], [], [], [beta]
+        for j in range(m):
+            w = matvec(q[j])
+            nmv += 1
+            qj = q[:j + 1]
+            c1 = qj @ w
+            w -= qj.T @ c1
+            c2 = qj @ w
+            w -= qj.T @ c2
+            hcol = torch.cat([c1 + c2, torch.linalg.vector_norm(w).reshape(1)]).cpu().numpy()
+            col = np.array(hcol, dtype=float)
+            hn = float(col[j + 1])
+            for i in range(j):
+                t = cs[i] * col[i] + sn[i] * col[i + 1]
+                col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1]
+                col[i] = t
+            d = float(np.hypot(col[j], col[j + 1]))
+            c_, s_ = (1.0, 0.0) if d == 0.0 else (col[j] / d, col[j + 1] / d)
+            cs.append(c_)
+            sn.append(s_)
+            col[j] = d
+            cols.append(col[:j + 1].copy())
+            gam.append(-s_ * gam[j])
+            gam[j] = c_ * gam[j]
+            res = abs(gam[j + 1])
+            stop = bool(callback(res)) if callback is not None else False
+            if res <= tol_abs:
+                converged = True
+                break
+            if stop:
+                halted = True
+                break
+            if hn == 0.0:
+                break
+            if j + 1 < m:
+                if j + 1 >= q.shape[0]:
+                    grown = torch.empty((min(m, max(2 * q.shape[0], j + 2)), n), dtype=b.dtype, device=b.device)
+                    grown[:j + 1] = q[:j + 1]
+                    q = grown
+                q[j + 1] = w / hn
+        k = len(cols)
+        if k:
+            rmat = np.zeros((k, k))
+            for j, col in enumerate(cols):
+                rmat[:j + 1, j] = col
+            y = torch.from_numpy(_back_substitute(rmat, np.asarray(gam[:k]))).to(b.device)
+            x += q[:k].T @ y
+    return x, converged, nmv
+
+
+def basis_cap(case, n: int) -> int:
+    if case.scheme.krylov_restart is not None:
+        return int(case.scheme.krylov_restart)
+    per = max(1.0, 8.0 * float(n))
+    return int(max(32, min(int(case.iteration.tmax), int(case.scheme.krylov_max_bytes / per))))
+
+
+def run_krylov(solver):
+    """``pybte/krylov.py:257-363`` on the device."""
+    c = solver.case
+    tol, tmax = c.iteration.tol, c.iteration.tmax
+    op = FixedPointOperator(solver)
+    residuals, masses = [], []
+
+    def sweep(u):
+        out = op.apply(u)
+        masses.append(np.nan)
+        residuals.append(np.nan)
+        return out
+
+    torch.cuda.synchronize(solver.device)
+    t0 = time.perf_counter()
+    zero = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
+    g = sweep(zero)
+    gnorm = float(torch.linalg.vector_norm(g).item())
+    scale = gnorm or 1.0
+    residuals[-1] = 1.0
+
+    def matvec(v):
+        return v - (sweep(v) - g)
+
+    enough = max(tol * _ENOUGH, _FLOOR) * scale
+    target = max(tol * c.scheme.krylov_tol_factor, _FLOOR) * scale
+    cap = basis_cap(c, op.n)
+    reached = -1
+
+    def on_residual(res):
+        nonlocal reached
+        residuals[-1] = res / scale
+        n = len(residuals)
+        if reached < 0 and res <= enough:
+            reached = n
+        return reached >= 0 and n - reached > max(64, reached // 4)
+
+    x = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
+    converged = False
+    final = float("nan")
+    for _ in range(c.scheme.krylov_max_rounds):
+        budget = tmax - len(residuals) - 1
+        if budget <= 0:
+            break
+        reached = -1
+        x, _, _ = gmres(matvec, g, x0=x, tol_abs=target, maxiter=budget, max_basis=cap, callback=on_residual)
+        sweep(x)
+        op.publish()
+        final = solver.ctx.true_residual(solver.mom, solver.vdf)
+        residuals[-1] = final
+        converged = bool(final < tol) if np.isfinite(final) else gnorm == 0.0
+        if converged or len(residuals) >= tmax:
+            break
+        target = max(target * 1.0e-3, _FLOOR * scale)
+    torch.cuda.synchronize(solver.device)
+    wall = time.perf_counter() - t0
+    solver.ctx.sweep_count += op.sweeps
+    masses = [solver.mom.mass] * len(residuals)
+    return solver._record(len(residuals), converged, residuals, masses, wall, "KRYLOV",
+                          extra={"krylov_size": op.n, "krylov_basis_cap": cap,
+                                 "transport_residual": final})

@@ -1,0 +1,166 @@
+/*
+ * pbte_gb300.h -- C ABI of the GB300 (sm_103a) transport-sweep library.
+ *
+ * The library replaces the hot path of pybte's steady gray linearised-
+ * Callaway DG discrete-ordinates solve (solver-python/pybte): the per-
+ * direction upwind sweep, the angular moments, the adiabatic-wall emission,
+ * the step and transport residuals, and the GSIS per-iteration kernels.
+ * Each entry point names the reference function it stands in for.
+ *
+ * Conventions
+ *  - Every function returns an int status: PBTE_OK (0), or a negative
+ *    PBTE_ERR_* code.  No C++ exception crosses this boundary.
+ *  - pbte_ctx_create takes HOST arrays (copied once); every other call takes
+ *    DEVICE pointers (e.g. torch tensor data_ptr()) and a cudaStream_t passed
+ *    as void*.  Calls are asynchronous on that stream.
+ *  - Array layouts are the reference's (C order, 0-based):
+ *      vdf[ndir][n_tris][ndof]      ts, qxs, qys[ndof][n_tris]
+ *      temp, qx, qy[n_tris]         flux_wall[n_faces][ndof]
+ *      pbuf[ndir][n_faces][ndof]
+ *    Directions are flattened d = j1 + npole*j2 as in pybte/velocity.py:52-56.
+ */
+#ifndef PBTE_GB300_H
+#define PBTE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PBTE_OK 0
+#define PBTE_ERR_ARG (-1)          /* bad argument / size                    */
+#define PBTE_ERR_CUDA (-2)         /* a CUDA runtime call failed             */
+#define PBTE_ERR_CYCLE (-3)        /* a direction's sweep graph has a cycle  */
+#define PBTE_ERR_UNSUPPORTED (-4)  /* configuration not implemented          */
+#define PBTE_ERR_TIMEOUT (-5)      /* a device-side wait ran out of its cap  */
+#define PBTE_ERR_SINGULAR (-6)     /* singular element operator(s)           */
+#define PBTE_ERR_NOMEM (-7)        /* device allocation failed               */
+
+/* precision of the sweep arithmetic */
+#define PBTE_FP64 0
+#define PBTE_FP32 1
+
+typedef struct pbte_ctx pbte_ctx;
+
+/* One case, host pointers, reference layouts.  The operator description is
+ * the compact form of pybte's integral tensors (pybte/integration.py:159-404):
+ *   mass[:,:,i] = area2[i] * ref_mass
+ *   gx[i]       = area2[i] * (dxi[i][0] * ref_dx + dxi[i][1] * ref_dy)
+ *   gy[i]       = area2[i] * (deta[i][0] * ref_dx + deta[i][1] * ref_dy)
+ *   fcm[i][il]  = edge_scale[i][il] * ref_edge[il]
+ *   ttfc[i][il] = fcm[i][il] gathered through edge_map[i][il][:]
+ * with edge_dofs[il][:] the element DOFs on local edge il.             */
+typedef struct {
+    int32_t n_tris, n_faces, ndof, ndof_fc, ndir, nbc;
+    double cv, vg, tau_r, tau_n, tau_c;
+    const double *cxv, *cyv, *domega;          /* [ndir]                     */
+    const double *ref_mass, *ref_dx, *ref_dy;  /* [ndof*ndof]                */
+    const double *ref_edge;                    /* [3*ndof*ndof]              */
+    const int32_t *edge_dofs;                  /* [3*ndof_fc]                */
+    const double *area2;                       /* [n_tris]                   */
+    const double *dxi, *deta;                  /* [n_tris*2]                 */
+    const double *edge_scale;                  /* [n_tris*3]                 */
+    const double *nx, *ny;                     /* [n_tris*3] outward normals */
+    const int32_t *tri_faces;                  /* [n_tris*3]                 */
+    const int32_t *upwind_tri;                 /* [n_tris*3] neighbour / periodic partner / -1 */
+    const int32_t *edge_map;                   /* [n_tris*3*ndof_fc]         */
+    const int32_t *face_bc;                    /* [n_faces]  -1 interior     */
+    const int32_t *face_tri, *face_lfc;        /* [n_faces*2]                */
+    const int32_t *bc_type;                    /* [nbc] 1 therm. 2 adiab. 3 periodic */
+    const double *bc_temp;                     /* [nbc]                      */
+    const double *int_tri;                     /* [ndof*n_tris]              */
+} pbte_case_desc;
+
+/* Build a sweep context: level schedules per direction class (host C++),
+ * device copies of the compact operators, and -- when `precompute` is set --
+ * the FP64 LU factors of every (direction, element) operator.
+ * Replaces SweepContext.build + factorise (pybte/sweep.py:74-129).
+ * Returns PBTE_ERR_CYCLE if a direction's sweep graph has a cycle, and
+ * PBTE_ERR_SINGULAR if a precomputed factorisation meets a zero pivot. */
+int pbte_ctx_create(const pbte_case_desc *desc, int precompute, pbte_ctx **out);
+int pbte_ctx_destroy(pbte_ctx *ctx);
+
+/* Sizes the context was built with, and the device bytes it holds. */
+int pbte_ctx_info(const pbte_ctx *ctx, int64_t *n_levels_max, int64_t *n_classes,
+                  int64_t *device_bytes);
+
+/* One FP64 transport sweep, in place on vdf.  Replaces SweepContext.sweep
+ * (pybte/sweep.py:132-158 -> _kernels.sweep_precomputed/_onthefly,
+ * pybte/_kernels.py:218-269).  `pbuf`/`use_pbuf` as in the reference
+ * (the Krylov path's periodic state); pbuf may be NULL when use_pbuf == 0. */
+int pbte_sweep(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
+               double *vdf, const double *flux_wall, const double *pbuf, int use_pbuf,
+               void *stream);
+
+/* FP32 sweep (mixed precision): moments and wall emission read in FP64,
+ * element solves and vdf32 in FP32.  With `wall_scale` = 0 the thermalising
+ * walls emit nothing (the homogeneous sweep of a defect correction).  No
+ * reference counterpart: the reference is FP64 only. */
+int pbte_sweep_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
+                   float *vdf32, const double *flux_wall, double wall_scale, void *stream);
+
+/* Angular moments and element integrals.  Replaces compute_moments
+ * (pybte/moments.py:51-55 -> _kernels.moments_kernel, _kernels.py:312-338). */
+int pbte_moments(pbte_ctx *ctx, const double *vdf, double *ts, double *qxs, double *qys,
+                 double *temp, double *qx, double *qy, void *stream);
+/* The same from an FP32 distribution, accumulated in FP32 per direction
+ * block and summed in FP64. */
+int pbte_moments_f32(pbte_ctx *ctx, const float *vdf32, double *ts, double *qxs, double *qys,
+                     double *temp, double *qx, double *qy, void *stream);
+
+/* Adiabatic-wall emission from vdf.  Replaces BoundaryData.update_wall_flux
+ * (pybte/bc.py:47-58 -> _kernels.wall_flux_kernel, _kernels.py:364-397). */
+int pbte_wall_flux(pbte_ctx *ctx, const double *vdf, double *flux_wall, void *stream);
+int pbte_wall_flux_f32(pbte_ctx *ctx, const float *vdf32, double *flux_wall, void *stream);
+
+/* Step residual sqrt(sum (T-T_old)^2 / sum T^2) into *out (device), then
+ * t_old <- temp.  Replaces residual_iterate (pybte/moments.py:58-72). */
+int pbte_residual_iterate(pbte_ctx *ctx, const double *temp, double *t_old, double *out,
+                          void *stream);
+
+/* Per-direction ||A f - b||^2_w numerator and denominator (device arrays of
+ * ndir).  Replaces _kernels.transport_residual (pybte/_kernels.py:275-306),
+ * the body of SweepContext.true_residual (pybte/sweep.py:161-197). */
+int pbte_transport_residual(pbte_ctx *ctx, const double *ts, const double *qxs,
+                            const double *qys, const double *vdf, const double *flux_wall,
+                            const double *pbuf, double *num, double *den, void *stream);
+
+/* Device-side stop flag for graph-captured iteration: when *done != 0 every
+ * sweep/moment/residual kernel launched with the context returns at once.
+ * pbte_set_done_flag(ctx, ptr) installs it (NULL removes it).
+ * pbte_residual_check implements the source-iteration stopping rule of
+ * pybte/driver.py:185-211 on the device: unless *done is already set it
+ * records (res[0], res[1]) at hist[2*count] (when count < hist_cap),
+ * increments *count, and sets *done = 1 if res[0] < tol, or *done = 2 if
+ * *count reached tmax. */
+int pbte_set_done_flag(pbte_ctx *ctx, const int32_t *done);
+int pbte_residual_check(pbte_ctx *ctx, const double *res, double tol, int64_t tmax,
+                        int32_t *done, int64_t *count, double *hist, int64_t hist_cap,
+                        void *stream);
+
+/* GSIS per-iteration kernels (pybte/acceleration/):
+ * third-order moment source, hot_source.py:29-58 -> work[n_tris][7*ndof];
+ * kinetic wall-trace moments, global_solve.py:31-53 -> out[nk][3*ndof_fc];
+ * damped correction, correction.py:29-75 (in place on vdf and moments). */
+int pbte_hot_source(pbte_ctx *ctx, const double *vdf, double tc5, double *work, void *stream);
+int pbte_wall_trace(pbte_ctx *ctx, const double *vdf, const double *tri_fc_fc, int32_t nk,
+                    const int32_t *tri_list, const int32_t *lfc_list, double *out, void *stream);
+int pbte_correct(pbte_ctx *ctx, double *vdf, const double *uq, const double *tri_hmin,
+                 double tau_thr, int use_hmin, double *ts, double *qxs, double *qys,
+                 double *temp, double *qx, double *qy, void *stream);
+
+/* Batched dense inverse of n matrices of order m (FP64, Gauss-Jordan with
+ * partial pivoting), a[n][m][m] -> inv[n][m][m].  Replaces the
+ * np.linalg.inv of build_local_operators (acceleration/assembly.py:100).
+ * *singular (device int) counts zero pivots. */
+int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int32_t *singular,
+                         void *stream);
+
+/* Version string of the built library. */
+const char *pbte_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PBTE_GB300_H */

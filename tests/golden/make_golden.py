@@ -1,0 +1,132 @@
+"""Generate the golden fixtures under tests/golden/ from the reference itself.
+
+Runs the reference solver (dingtao-shen/...-PBTE, ``solver-python/pybte``) in
+its pure-Python/LAPACK mode (numba absent) and records its outputs on small
+cases, plus the certified solutions shipped with the reference's benchmark
+task (``tasks/t01-square/reference/*.npz``).  Needs the reference checkout,
+so it runs only where that is mounted:
+
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+
+The fixtures are plain arrays; nothing at test time reads the reference.
+"""
+from __future__ import annotations
+
+import json
+import sys
+import tempfile
+from pathlib import Path
+
+import numpy as np
+
+OUT = Path(__file__).resolve().parent
+
+
+def main(ref_root: str) -> None:
+    ref = Path(ref_root)
+    sys.path[:0] = [str(ref / "solver-python"), str(ref / "solver-python" / "tools")]
+    from make_meshes import build
+    from pybte import Case, Solver
+    from pybte import krylov as rkrylov
+    from pybte.acceleration import Acceleration  # noqa: F401  (import check)
+
+    tmp = Path(tempfile.mkdtemp())
+    mesh5 = tmp / "A1_Nx6_Ny6.msh"
+    mesh5.write_text(build(5, "cavity", "smootherstep"))
+
+    def case(deg, npole, nazim, tau_r, tau_n, south="nonthermalising", accflag=0,
+             method="source", tol=1e-8, tmax=20000, north_t=1.0):
+        return Case.from_dict({
+            "iteration": {"tol": tol, "tmax": tmax},
+            "scheme": {"accflag": accflag, "method": method},
+            "velmesh": {"npole": npole, "nazim": nazim}, "dg": {"deg": deg},
+            "flow": {"cv": 1.0, "vg": 1.0, "tau_r": tau_r, "tau_n": tau_n, "tau_thr": 1.0},
+            "mesh": {"file": str(mesh5)},
+            "boundaries": [{"name": "SWall", "phyid": 11, "type": south, "temp": 0.0},
+                           {"name": "NWall", "phyid": 12, "type": "thermalising", "temp": north_t},
+                           {"name": "EWall", "phyid": 13, "type": "thermalising", "temp": -0.5},
+                           {"name": "WWall", "phyid": 14, "type": "thermalising", "temp": 0.5}],
+            "output": {"field": False, "runtime_log": False, "run_record": False}}, basedir=str(tmp))
+
+    meta = {}
+    # 1. setup arrays + one sweep/moments/wall-flux/residual from seeded state
+    for deg in (1, 2, 3):
+        c = case(deg, 4, 8, 0.5, 0.05)
+        s = Solver(c)
+        ctx, it, m = s.ctx, s.integrals, s.mesh
+        rng = np.random.default_rng(100 + deg)
+        nd, nt = s.ndof, s.n_tris
+        s.mom.ts[:] = rng.standard_normal((nd, nt))
+        s.mom.qxs[:] = 0.3 * rng.standard_normal((nd, nt))
+        s.mom.qys[:] = 0.3 * rng.standard_normal((nd, nt))
+        vdf0 = rng.standard_normal(s.vdf.shape)
+        s.vdf[:] = vdf0
+        s.bcdata.update_wall_flux(s.vdf, ctx.cxv, ctx.cyv, ctx.domega, it.int_tri_fc, m)
+        fw = s.bcdata.flux_wall.copy()
+        ctx.sweep(s.mom, s.vdf)
+        vdf1 = s.vdf.copy()
+        tr = ctx.true_residual(s.mom, s.vdf)
+        from pybte.moments import compute_moments
+        compute_moments(s.vdf, ctx.cxv, ctx.cyv, ctx.domega, it.int_tri, 1.0, s.mom)
+        np.savez_compressed(
+            OUT / f"setup_sweep_deg{deg}.npz",
+            nodes=m.nodes, tri_nodes=m.tri_nodes, tri_faces=m.tri_faces, face_nodes=m.face_nodes,
+            face_bc=m.face_bc, face_tri=m.face_tri, face_lfc=m.face_lfc,
+            tri_neighbour=m.tri_neighbour, tri_normal=m.tri_normal, tri_area=m.tri_area,
+            face_len=m.face_len, tri_hmin=m.tri_hmin,
+            int_tri=it.int_tri, int_tri_tri=it.int_tri_tri, int_tri_tri_x=it.int_tri_tri_x,
+            int_tri_tri_y=it.int_tri_tri_y, int_tri_fc=it.int_tri_fc, int_tri_fc_fc=it.int_tri_fc_fc,
+            int_fc_fc=it.int_fc_fc, int_fc=it.int_fc, int_tri_tri_fc=it.int_tri_tri_fc,
+            cxv=ctx.cxv, cyv=ctx.cyv, domega=ctx.domega, order=ctx.order,
+            ts_in=np.zeros(0), vdf_in=vdf0, flux_wall=fw, vdf_out=vdf1, true_residual=tr,
+            ts_out=s.mom.ts, qxs_out=s.mom.qxs, qys_out=s.mom.qys, temp_out=s.mom.temp,
+            qx_out=s.mom.qx, qy_out=s.mom.qy,
+            ts_src=np.asarray(rng.bit_generator.state["state"]["state"] % 7))
+        meta[f"setup_sweep_deg{deg}"] = {"deg": deg, "npole": 4, "nazim": 8, "tau_r": 0.5,
+                                         "tau_n": 0.05, "seed": 100 + deg}
+        print("setup/sweep deg", deg, "true residual", tr, flush=True)
+
+    # 2. complete solves: CIS, GSIS, GMRES(30)
+    runs = {
+        "cis_deg1_adiabatic": dict(deg=1, npole=4, nazim=8, tau_r=1.0, tau_n=0.1),
+        "cis_deg2_isothermal": dict(deg=2, npole=4, nazim=8, tau_r=0.3, tau_n=0.03,
+                                    south="thermalising"),
+        "gsis_deg2_adiabatic": dict(deg=2, npole=4, nazim=8, tau_r=0.1, tau_n=0.01, accflag=1),
+        "gsis_deg1_isothermal": dict(deg=1, npole=4, nazim=8, tau_r=0.05, tau_n=0.005, accflag=1,
+                                     south="thermalising"),
+        "krylov_deg2_adiabatic": dict(deg=2, npole=4, nazim=8, tau_r=0.1, tau_n=0.01,
+                                      method="krylov"),
+    }
+    orig_cap = rkrylov.krylov_basis_cap
+    for name, kw in runs.items():
+        if kw.get("method") == "krylov":
+            rkrylov.krylov_basis_cap = lambda *a: 30
+        c = case(**kw)
+        s = Solver(c)
+        rec = s.run()
+        rkrylov.krylov_basis_cap = orig_cap
+        np.savez_compressed(OUT / f"{name}.npz", iterations=rec.iterations,
+                            converged=rec.converged, residuals=rec.residual_history,
+                            masses=rec.mass_history, temp=rec.temp, qx=rec.qx, qy=rec.qy,
+                            ts=rec.temp_dofs, qxs=rec.qx_dofs, qys=rec.qy_dofs,
+                            true_residual=s.ctx.true_residual(s.mom, s.vdf))
+        meta[name] = {**kw, "iterations": int(rec.iterations), "mass": float(rec.mass)}
+        print(name, rec.iterations, rec.converged, rec.mass, flush=True)
+
+    # 3. certified task solutions (GMRES to 1e-10 on the shipped 200-triangle mesh)
+    task = ref / "tasks" / "t01-square"
+    index = json.loads((task / "reference" / "index.json").read_text())
+    keep = {}
+    for key in ("F1_1_1", "F1_1e-1", "F2_1_1", "F2_1e-1"):
+        z = np.load(task / "reference" / f"{key}.npz")
+        keep[key] = {k: z[k] for k in ("temp", "qx", "qy", "temp_dofs")}
+        meta[f"task_{key}"] = {"iterations": index[key]["iterations"],
+                               "cis_iterations": index[key]["cis_iterations"],
+                               "mass": index[key]["mass"]}
+    np.savez_compressed(OUT / "task_solutions.npz",
+                        **{f"{k}__{f}": v for k, d in keep.items() for f, v in d.items()})
+    (OUT / "golden_meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True))
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,158 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the
+same inputs, and against the reference's golden solves.
+
+Tolerances: FP64 kernels 1e-12 relative (the GPU forms the element operators
+from the compact reference matrices and factors with reciprocal pivots, so it
+differs from the oracle by rounding only); complete FP64 solves 1e-10 on the
+fields with the iteration count exact or within 1; the mixed path 1e-8
+against the FP64 fixed point.
+"""
+import numpy as np
+import pytest
+import torch
+
+from cases import case_from_meta, golden, meta, small_case, task_case
+from oracle.oracle import Oracle
+from pbte_gb300 import Solver
+from pbte_gb300.config import square_case
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def _seed_state(s, o, seed):
+    rng = np.random.default_rng(seed)
+    for k in ("ts", "qxs", "qys"):
+        v = rng.standard_normal(getattr(o, k).shape) * (1.0 if k == "ts" else 0.3)
+        getattr(o, k)[:] = v
+        getattr(s.mom, k).copy_(torch.from_numpy(v))
+    o.vdf[:] = rng.standard_normal(o.vdf.shape)
+    s.vdf.copy_(torch.from_numpy(o.vdf))
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
+@pytest.mark.parametrize("mode", ["precomputed", "onthefly"])
+@pytest.mark.parametrize("south", ["nonthermalising", "thermalising"])
+def test_sweep_moments_flux_match_oracle(cuda, deg, mode, south):
+    case = small_case(deg, 4, 8, 0.5, 0.05, south=south, sweep_mode=mode)
+    s = Solver(case)
+    assert s.ctx.mode == mode
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 7 + deg)
+    o.wall_flux()
+    s.ctx.wall_flux(s.vdf)
+    torch.cuda.synchronize()
+    if south == "nonthermalising":
+        assert _rel(s.ctx.flux_wall.cpu().numpy(), o.flux_wall) < 1e-12
+    o.sweep()
+    s.ctx.sweep(s.mom, s.vdf)
+    torch.cuda.synchronize()
+    assert _rel(s.vdf.cpu().numpy(), o.vdf) < 1e-12
+    o.moments()
+    s.ctx.moments(s.vdf, s.mom)
+    h = s.mom.host()
+    for k in ("ts", "qxs", "qys", "temp", "qx", "qy"):
+        assert _rel(h[k], getattr(o, k)) < 1e-12, k
+    tr_o = o.true_residual()
+    tr_g = s.ctx.true_residual(s.mom, s.vdf)
+    assert abs(tr_g - tr_o) < 1e-9 * max(tr_o, 1e-12) + 1e-14
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_transport_residual_of_random_state(cuda, deg):
+    s = Solver(small_case(deg, 4, 8, 0.2, 0.02))
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 3)
+    o.wall_flux()
+    s.ctx.wall_flux(s.vdf)
+    assert s.ctx.true_residual(s.mom, s.vdf) == pytest.approx(o.true_residual(), rel=1e-11)
+
+
+def test_fp32_sweep_close_to_fp64(cuda):
+    s = Solver(small_case(2, 4, 8, 0.5, 0.05))
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 11)
+    o.wall_flux()
+    o.sweep()
+    s.ctx.wall_flux(s.vdf)
+    v32 = torch.zeros(s.vdf.shape, dtype=torch.float32, device=s.device)
+    # FP32 sweeps overwrite every element, so the upwind inflow comes from this sweep
+    s.ctx.sweep_f32((s.mom.ts, s.mom.qxs, s.mom.qys), v32, s.ctx.flux_wall)
+    torch.cuda.synchronize()
+    assert _rel(v32.double().cpu().numpy(), o.vdf) < 2e-5
+
+
+@pytest.mark.parametrize("name", ["cis_deg1_adiabatic", "cis_deg2_isothermal"])
+def test_cis_solve_matches_reference(cuda, name):
+    z = golden(name)
+    s = Solver(case_from_meta(name))
+    rec = s.run()
+    assert rec.converged
+    assert rec.iterations == int(z["iterations"])
+    assert _rel(rec.temp, z["temp"]) < 1e-10
+    assert _rel(rec.temp_dofs, z["ts"]) < 1e-10
+    assert _rel(rec.qx_dofs, z["qxs"]) < 1e-9
+    assert np.allclose(rec.residual_history, z["residuals"], rtol=1e-6, atol=1e-14)
+
+
+def test_cis_graph_stops_at_tmax(cuda):
+    s = Solver(small_case(1, 4, 8, 1.0, 0.1, tmax=45), graph_block=32)
+    rec = s.run()
+    assert rec.iterations == 45 and not rec.converged
+
+
+@pytest.mark.parametrize("name", ["gsis_deg2_adiabatic", "gsis_deg1_isothermal"])
+def test_gsis_solve_matches_reference(cuda, name):
+    z = golden(name)
+    s = Solver(case_from_meta(name))
+    rec = s.run()
+    assert rec.converged
+    assert abs(rec.iterations - int(z["iterations"])) <= 1
+    assert _rel(rec.temp, z["temp"]) < 1e-10
+    assert _rel(rec.temp_dofs, z["ts"]) < 1e-10
+
+
+def test_krylov_gmres30_matches_reference(cuda):
+    name = "krylov_deg2_adiabatic"
+    z = golden(name)
+    s = Solver(case_from_meta(name, krylov_restart=30))
+    rec = s.run()
+    assert rec.converged
+    assert abs(rec.iterations - int(z["iterations"])) <= max(1, int(0.02 * int(z["iterations"])))
+    assert _rel(rec.temp, z["temp"]) < 1e-8
+    assert rec.diagnostics["transport_residual"] < 1e-8
+
+
+@pytest.mark.parametrize("key", ["F1_1_1", "F2_1e-1"])
+def test_task_certified_solution(cuda, key):
+    fam, tau = key.split("_", 1)
+    sol = golden("task_solutions")
+    rec = Solver(task_case(fam, tau)).run()
+    assert rec.converged
+    assert abs(rec.iterations - meta()[f"task_{key}"]["iterations"]) <= 1
+    assert _rel(rec.temp, sol[f"{key}__temp"]) < 1e-9
+
+
+@pytest.mark.parametrize("method", ["source", "krylov"])
+def test_mixed_precision_reaches_fp64_fixed_point(cuda, method):
+    base = dict(deg=2, npole=4, nazim=8, tau_r=0.2, tau_n=0.02)
+    o = Oracle(Solver(small_case(**base)).disc, nthreads=4)
+    r = o.run_krylov(tol=1e-13, tmax=5000)
+    assert r["converged"]
+    s = Solver(small_case(**base, method=method, precision="mixed"))
+    rec = s.run()
+    assert rec.converged
+    assert _rel(rec.temp_dofs, o.ts) < 1e-8
+    assert _rel(rec.qx_dofs, o.qxs) < 1e-8
+    assert rec.diagnostics["fp32_sweeps"] > rec.diagnostics["fp64_sweeps"]
+
+
+def test_square_benchmark_mesh_levels(cuda):
+    s = Solver(square_case(64, 2, 8, 32, tau_r=1.0, tmax=3))
+    assert s.n_tris == 8192
+    assert s.ctx.n_classes <= 16
+    rec = s.run()
+    assert rec.iterations == 3
