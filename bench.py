@@ -1,0 +1,323 @@
+#!/usr/bin/env python
+"""Benchmark: converged solves/s of the square-cavity DG discrete-ordinates
+problem on 8192 triangles, P2, 256 ordinates (the 64 x 64 uniform grid;
+west/east isothermal at +0.5/-0.5, north/south diffuse adiabatic).
+
+One step = one converged solve, from a zero state, of one case of the step's
+Knudsen sweep (Kn_R in {10, 1, 0.1, 0.01}, Kn_N = 0.1 Kn_R, cycled), to
+<= 1e-8 relative error against the FP64 fixed point, with the
+mixed-precision solver (FP32 sweeps, FP64 defect correction, GMRES(30)
+inner solve).  The timed region of each step starts with the case's
+operators and schedule already on the device.  L2 is flushed (a 512 MB
+write) before every timed step.
+
+JSON line keys beyond the driver contract: ``roofline`` (the FP32 sweep,
+timed live with CUDA events on its stream), ``cpu_baseline`` (the C oracle on
+the host cores, one solve), ``e2e`` (the public API from host arrays:
+context creation + solve + results to host), ``fp64`` (the plain FP64 GPU
+drop-in on the same steps), ``latency_ms`` (p50/p99 of the timed steps).
+
+``--impl reference`` times the reference algorithm's CPU implementation (the
+C oracle, OpenMP over ordinates on all host cores) on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path[:0] = [str(ROOT / "ai-driven-numerical-method-exploration-for-multiscale-pbte_gb300"), str(ROOT)]
+
+import numpy as np  # noqa: E402
+
+KN = [10.0, 1.0, 0.1, 0.01]
+GRID, DEG, NPOLE, NAZIM = 64, 2, 8, 32
+METRIC = "converged solves/s (<=1e-8 rel err vs FP64, mixed precision)"
+
+
+def workload_config():
+    return {"workload": "square 64x64 grid (8192 tri), DG P2, 256 ordinates (8 polar x 32 azimuth), "
+                        "Kn_R cycled over 10/1/0.1/0.01, Kn_N=0.1 Kn_R, GMRES(30) mixed FP32/FP64",
+            "n_tris": 8192, "ndof": 6, "ndir": 256, "kn_r": KN, "method": "krylov",
+            "restart": 30, "tol": 1e-8, "l2": "flushed (512 MB write) before each timed step"}
+
+
+def make_case(kn, precision="mixed", method="krylov"):
+    from pbte_gb300.config import square_case
+    return square_case(GRID, DEG, NPOLE, NAZIM, tau_r=kn, tau_n=0.1 * kn, method=method,
+                       precision=precision, krylov_restart=30, tol=1e-8, tmax=20000)
+
+
+def read_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 7:
+                continue
+            try:
+                sm.append(float(p[0]))
+                mx.append(float(p[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def sweep_roofline(solver, peak, peak_kind, reps=20):
+    """Average duration of the FP32 sweep kernel on this case (CUDA events on
+    its stream) and its algorithmic bytes per launch."""
+    import torch
+
+    s = solver
+    v32 = torch.zeros(s.vdf.shape, dtype=torch.float32, device=s.device)
+    st = torch.cuda.Stream(device=s.device)
+    with torch.cuda.stream(st):
+        s.mom.ts.normal_()
+        s.mom.qxs.normal_()
+        s.mom.qys.normal_()
+        for _ in range(3):
+            s.ctx.sweep_f32((s.mom.ts, s.mom.qxs, s.mom.qys), v32, s.ctx.flux_wall, stream=st)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        st.synchronize()
+        a.record(st)
+        for _ in range(reps):
+            s.ctx.sweep_f32((s.mom.ts, s.mom.qxs, s.mom.qys), v32, s.ctx.flux_wall, stream=st)
+        b.record(st)
+        b.synchronize()
+    ms = a.elapsed_time(b) / reps
+    nd, nt, ndir = s.ndof, s.n_tris, s.ndir
+    algo = (4.0 * ndir * nt * nd          # write f (FP32)
+            + 4.0 * 3 * nt * nd           # moment sources (FP32)
+            + 112.0 * nt                  # element records (FP32)
+            + 4.0 * nt * s.ctx.n_classes  # level lists
+            + 8.0 * s.mesh.n_faces_b * nd)  # wall emission (FP64)
+    ach = algo / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(ach / peak, 4), "traffic": None, "kernel": "sweep_kernel<float,2>",
+            "kernel_ms": round(ms, 4), "algorithmic_bytes": int(algo), "peak_source": f"{peak_kind} hbm_gbs"}
+
+
+def cpu_solve(kn, nthreads, max_seconds=30.0):
+    """One solve of the same case with the C oracle on the host cores."""
+    from oracle.oracle import Oracle
+    from pbte_gb300.discretisation import Discretisation
+
+    disc = Discretisation.build(make_case(kn, precision="fp64"))
+    o = Oracle(disc, nthreads=nthreads)
+    t0 = time.perf_counter()
+    r = o.run_krylov(tol=1e-8, tmax=20000, max_basis=30)
+    return time.perf_counter() - t0, r
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return 0
+    from oracle import oracle as orc
+    orc.build()
+    cores = os.cpu_count() or 1
+    times = []
+    for k in range(args.warmup + args.steps):
+        kn = KN[k % len(KN)] if args.steps >= len(KN) else 1.0
+        t, r = cpu_solve(kn, cores)
+        if k >= args.warmup:
+            times.append(t)
+    total = float(sum(times))
+    v = len(times) / total
+    line = {"metric": METRIC, "value": round(v, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1e3 * total / len(times), 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (structured square mesh, seedless)", "impl": "reference",
+            "config": {**workload_config(), "method": "GMRES(30) FP64 (C oracle)"},
+            "cpu_baseline": {"value": round(v, 4), "unit": "solves/s", "cores": cores, "kind": "port",
+                             "sample": f"{len(times)} complete solves"},
+            "e2e": {"value": round(v, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=4)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, world, rank)
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(dev)
+    from pbte_gb300 import Solver, _lib
+    _lib.lib()
+
+    # cases resident on the device before timing (replicas: every rank its own copy)
+    solvers = {kn: Solver(make_case(kn), device=str(dev)) for kn in KN}
+    fp64 = {kn: Solver(make_case(kn, precision="fp64"), device=str(dev)) for kn in KN}
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def reset(s):
+        s.vdf.zero_()
+        for k in ("ts", "qxs", "qys", "temp", "qx", "qy"):
+            getattr(s.mom, k).zero_()
+        s.ctx.flux_wall.zero_()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize(dev)
+
+    def timed(pool, k, check=None):
+        kn = KN[k % len(KN)]
+        s = pool[kn]
+        reset(s)
+        flush.fill_(float(k))
+        barrier()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        rec = s.run()
+        b.record()
+        barrier()
+        if not rec.converged:
+            raise RuntimeError(f"solve at Kn_R={kn} did not converge")
+        return a.elapsed_time(b), rec
+
+    for k in range(args.warmup):
+        timed(solvers, k)
+    launches = 0
+    times = []
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            ms, rec = timed(solvers, k)
+            times.append(ms)
+            launches += 5 * (rec.diagnostics["fp64_sweeps"] + rec.diagnostics["fp32_sweeps"])
+    clocks = clk.summary()
+    total = float(sum(times))
+    if dist is not None:
+        t = torch.tensor([total], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = world * args.steps / (total * 1e-3)
+
+    # FP64 drop-in on the same steps (reported beside the headline)
+    t64 = []
+    for k in range(min(args.steps, len(KN))):
+        ms, _ = timed(fp64, k)
+        t64.append(ms)
+    fp64_rate = len(t64) / (sum(t64) * 1e-3)
+
+    # e2e: public API from host arrays -- context creation (H2D of the
+    # operators + schedule), solve, fields back to host
+    e2e_t, h2d, d2h = [], 0, 0
+    from pbte_gb300.sweep import SweepContext
+    for k in range(min(args.steps, len(KN))):
+        kn = KN[k % len(KN)]
+        s = solvers[kn]
+        barrier()
+        t0 = time.perf_counter()
+        s.ctx = SweepContext(s.disc, device=str(dev))
+        reset(s)
+        rec = s.run()
+        out = (rec.temp_dofs, rec.qx_dofs, rec.qy_dofs, rec.temp, rec.qx, rec.qy)
+        barrier()
+        e2e_t.append(time.perf_counter() - t0)
+        h2d = sum(v.nbytes for v in s.ctx._host.values())
+        d2h = sum(v.nbytes for v in out)
+    e2e = len(e2e_t) / sum(e2e_t)
+
+    peak, kind = read_peaks()
+    roof = sweep_roofline(solvers[1.0], peak, kind)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import oracle as orc
+        orc.build()
+        cores = os.cpu_count() or 1
+        t, r = cpu_solve(1.0, cores)
+        cpu = {"value": round(1.0 / t, 4), "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": f"1 complete FP64 GMRES(30) solve at Kn_R=1 ({r['iterations']} sweeps, {t:.1f} s)"}
+    if rank == 0:
+        lat = np.array(times)
+        line = {"metric": METRIC, "value": round(value, 4), "unit": "solves/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / args.steps, 3),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
+                "data": "synthetic (structured square mesh)",
+                "config": {**workload_config(), "parallelism": f"replicas x{world}"},
+                "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
+                               "p99": round(float(np.percentile(lat, 99)), 3)},
+                "fp64": {"value": round(fp64_rate, 4), "unit": "solves/s",
+                         "speedup_mixed_over_fp64": round(value / world / fp64_rate, 3)},
+                "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+                        "d2h_bytes_per_step": int(d2h)},
+                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches)}
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.barrier()
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
