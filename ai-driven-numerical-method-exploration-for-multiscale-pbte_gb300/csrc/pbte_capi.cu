@@ -63,6 +63,12 @@ int pbte_residual_iterate(pbte_ctx *c, const double *temp, double *t_old, double
     return pbte::launch_residual(c, temp, t_old, out, S(stream));
 }
 
+int pbte_set_sweep_variant(pbte_ctx *c, int variant) {
+    if (!c || variant < 0 || variant > 2) return PBTE_ERR_ARG;
+    c->sweep_variant = variant;
+    return PBTE_OK;
+}
+
 int pbte_set_done_flag(pbte_ctx *c, const int32_t *done) {
     if (!c) return PBTE_ERR_ARG;
     c->done = done;

@@ -84,7 +84,8 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
     void *ptrs[] = {c->d_cx, c->d_cy, c->d_w, c->d_cells64, c->d_cells32, c->d_ref64, c->d_ref32,
                     c->d_edofs, c->d_dir_class, c->d_class_lvl_off, c->d_class_nlev, c->d_lvl_ptr,
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
-                    c->d_piv, c->d_red, c->d_singular};
+                    c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
+                    c->d_udir_rep, c->d_udir_twin};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -232,7 +233,10 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     c->nclass = (int)class_rep.size();
     std::vector<int32_t> lvl_cells((size_t)c->nclass * nt), lvl_ptr, class_off(c->nclass),
         class_nlev(c->nclass);
-    std::vector<int32_t> level, indeg, queue, count;
+    std::vector<int32_t> level, indeg, queue, count, pos(nt);
+    // ring of upwind values in shared memory: slot (level % R) * W + position,
+    // R = 1 + the largest level gap of an in-sweep dependency, W = widest level
+    std::vector<int32_t> up_slot((size_t)c->nclass * nt * 3, -1), class_W(c->nclass), class_R(c->nclass);
     for (int k = 0; k < c->nclass; ++k) {
         int dir = class_rep[k];
         if (!levels_for(d, d->cxv[dir], d->cyv[dir], level, indeg, queue)) {
@@ -243,19 +247,67 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         for (int i = 0; i < nt; ++i) nlev = std::max(nlev, level[i] + 1);
         count.assign(nlev + 1, 0);
         for (int i = 0; i < nt; ++i) count[level[i] + 1]++;
+        int W = 0;
+        for (int L = 0; L < nlev; ++L) W = std::max(W, count[L + 1]);
         for (int L = 0; L < nlev; ++L) count[L + 1] += count[L];
         class_off[k] = (int32_t)lvl_ptr.size();
         class_nlev[k] = nlev;
         for (int L = 0; L <= nlev; ++L) lvl_ptr.push_back(count[L] + k * nt);
         std::vector<int32_t> fill(count.begin(), count.end() - 1);
-        for (int i = 0; i < nt; ++i) lvl_cells[(size_t)k * nt + fill[level[i]]++] = i;
+        for (int i = 0; i < nt; ++i) {
+            pos[i] = fill[level[i]] - count[level[i]];
+            lvl_cells[(size_t)k * nt + fill[level[i]]++] = i;
+        }
+        int R = 1;
+        const double cx = d->cxv[dir], cy = d->cyv[dir];
+        for (int i = 0; i < nt; ++i)
+            for (int il = 0; il < 3; ++il) {
+                int nb = d->upwind_tri[i * 3 + il], fc = d->tri_faces[i * 3 + il];
+                if (nb < 0 || d->face_bc[fc] >= 0) continue;
+                if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0) R = std::max(R, level[i] - level[nb] + 1);
+            }
+        class_W[k] = W;
+        class_R[k] = R;
+        for (int i = 0; i < nt; ++i) {
+            size_t p = (size_t)k * nt + count[level[i]] + pos[i];
+            for (int il = 0; il < 3; ++il) {
+                int nb = d->upwind_tri[i * 3 + il], fc = d->tri_faces[i * 3 + il];
+                if (nb < 0 || d->face_bc[fc] >= 0) continue;
+                if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0)
+                    up_slot[p * 3 + il] = (level[nb] % R) * W + pos[nb];
+            }
+        }
         c->nlev_max = std::max(c->nlev_max, nlev);
+        c->ring_W = std::max(c->ring_W, W);
+        c->ring_R = std::max(c->ring_R, R);
     }
+    // z-mirror twins: ordinates with the same in-plane velocity (and weight)
+    // see the same transport; one block sweeps the pair and stores both
+    std::vector<int32_t> urep, utwin;
+    std::vector<char> used(ndir, 0);
+    for (int a = 0; a < ndir; ++a) {
+        if (used[a]) continue;
+        used[a] = 1;
+        int tw = -1;
+        for (int b = a + 1; b < ndir && tw < 0; ++b)
+            if (!used[b] && dir_class[b] == dir_class[a] && std::fabs(d->cxv[a] - d->cxv[b]) <= 1e-12 &&
+                std::fabs(d->cyv[a] - d->cyv[b]) <= 1e-12)
+                tw = b;
+        if (tw >= 0) used[tw] = 1;
+        urep.push_back(a);
+        utwin.push_back(tw);
+    }
+    c->n_udir = (int)urep.size();
     TRY(upload(dir_class.data(), dir_class.size(), &c->d_dir_class, &c->device_bytes));
     TRY(upload(class_off.data(), class_off.size(), &c->d_class_lvl_off, &c->device_bytes));
     TRY(upload(class_nlev.data(), class_nlev.size(), &c->d_class_nlev, &c->device_bytes));
     TRY(upload(lvl_ptr.data(), lvl_ptr.size(), &c->d_lvl_ptr, &c->device_bytes));
     TRY(upload(lvl_cells.data(), lvl_cells.size(), &c->d_lvl_cells, &c->device_bytes));
+    TRY(upload(up_slot.data(), up_slot.size(), &c->d_up_slot, &c->device_bytes));
+    TRY(upload(class_W.data(), class_W.size(), &c->d_class_W, &c->device_bytes));
+    TRY(upload(class_R.data(), class_R.size(), &c->d_class_R, &c->device_bytes));
+    TRY(upload(urep.data(), urep.size(), &c->d_udir_rep, &c->device_bytes));
+    TRY(upload(utwin.data(), utwin.size(), &c->d_udir_twin, &c->device_bytes));
 
     // ---- scratch ----------------------------------------------------------
     TRY(alloc((size_t)3 * nd * nt, &c->d_S64, &c->device_bytes));

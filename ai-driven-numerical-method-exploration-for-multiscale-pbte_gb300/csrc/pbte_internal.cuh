@@ -67,6 +67,14 @@ struct pbte_ctx {
     int32_t *d_singular = nullptr;
     const int32_t *done = nullptr;  // optional device stop flag
     size_t device_bytes = 0;
+    // ring-buffered sweep: per-class upwind ring slots, widest level, deepest gap
+    int32_t *d_up_slot = nullptr;   // [nclass][n_tris in level order][3], -1: no in-sweep inflow
+    int32_t *d_class_W = nullptr, *d_class_R = nullptr;
+    int ring_W = 0, ring_R = 0;
+    // one sweep per distinct in-plane velocity: representative ordinate and its z-twin (-1 if none)
+    int32_t *d_udir_rep = nullptr, *d_udir_twin = nullptr;
+    int n_udir = 0;
+    int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
 };
 
 // launchers (pbte_kernels.cu)

@@ -1,0 +1,261 @@
+// Ring-pipelined transport sweep (the default sweep; pybte/_kernels.py:218-269).
+//
+// One thread block sweeps one distinct in-plane velocity (an ordinate and its
+// z-mirror twin share it, so the block stores the result under both).  The
+// block's threads form G groups of 128; group g owns the wavefront levels
+// L = g, g+G, ...  For its next level a group first does everything that does
+// not depend on the upwind values -- load the element records, form the
+// source and wall terms, assemble and LU-factor the element operators in
+// registers (or load the stored FP64 factors) -- and only then waits for
+// level L-1 (bar.sync on the barrier the previous group arrives at), adds the
+// upwind inflow from a shared-memory ring holding the last R levels, finishes
+// the two triangular solves, writes the ring and the global distribution, and
+// arrives on its own barrier for level L+1.  The critical path per level is
+// therefore the inflow gather plus two small triangular solves; factorisation
+// of the next levels overlaps it on the other groups.
+//
+// The ring slot of every upwind dependency, (level % R) * W + position, is
+// precomputed per direction class on the host (pbte_ctx.cu).
+#include "pbte_device.cuh"
+
+namespace pbte {
+
+constexpr int kTPG = 128;       // threads per group
+constexpr int kMaxGroups = 3;
+
+struct RingParams {
+    const int32_t *up_slot;     // [nclass * n_tris][3] absolute level-order index
+    const int32_t *class_W, *class_R;
+    const int32_t *udir_rep, *udir_twin;
+    int groups;
+};
+
+__device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void bar_arrive(int id, int n) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+
+template <typename T, int DEG, bool PRECOMP, int CPT>
+__global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepParams<T> P, RingParams Q) {
+    constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T *sref = reinterpret_cast<T *>(smem_raw);
+    T *ring = sref + 6 * NP * NP;
+    if (stopped(P.done)) return;
+    const int u = blockIdx.x;
+    const int d = Q.udir_rep[u], d2 = Q.udir_twin[u];
+    for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
+    __syncthreads();
+    const T cx = (T)P.cx[d], cy = (T)P.cy[d];
+    const int cls = P.dir_class[d];
+    const int off = P.class_off[cls], nlev = P.class_nlev[cls];
+    const int W = Q.class_W[cls], Rr = Q.class_R[cls];
+    const int G = Q.groups;
+    const int g = threadIdx.x / kTPG, t = threadIdx.x % kTPG;
+    T *f1 = P.vdf + (size_t)d * P.nt * NP;
+    T *f2 = d2 >= 0 ? P.vdf + (size_t)d2 * P.nt * NP : nullptr;
+    int sing = 0;
+    for (int L = g; L < nlev; L += G) {
+        const int beg = P.lvl_ptr[off + L], end = P.lvl_ptr[off + L + 1];
+        T A[CPT][NP][NP];
+        T b[CPT][NP];
+        int piv[CPT][NP];
+        int cell[CPT];
+        int slot[CPT][3];
+        T scin[CPT][3];
+        int emp[CPT][3][NF];
+        // ---- independent of the upwind values ------------------------------
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            const int k = beg + t + c * kTPG;
+            cell[c] = -1;
+#pragma unroll
+            for (int il = 0; il < 3; ++il) slot[c][il] = -1;
+            if (k < end) {
+                const int i = P.lvl_cells[k];
+                cell[c] = i;
+                const CellRec<T> r = P.cells[i];
+                T s[3];
+#pragma unroll
+                for (int il = 0; il < 3; ++il) s[il] = cx * r.nx[il] + cy * r.ny[il];
+                const T *S = P.S + (size_t)i * 3 * NP;
+#pragma unroll
+                for (int m = 0; m < NP; ++m) b[c][m] = P.ca * S[m] + P.cb * (cx * S[NP + m] + cy * S[2 * NP + m]);
+#pragma unroll
+                for (int il = 0; il < 3; ++il) {
+                    scin[c][il] = s[il] * r.es[il];
+#pragma unroll
+                    for (int bb = 0; bb < NF; ++bb) emp[c][il][bb] = r.emap[il][bb];
+                    if (!(s[il] < T(0))) continue;
+                    const T *R = sref + (3 + il) * NP * NP;
+                    const int kind = r.kind[il];
+                    if (kind == 0) {
+                        slot[c][il] = Q.up_slot[(size_t)k * 3 + il];
+                    } else if (kind == 3) {
+                        const double *pb = P.pbuf + ((size_t)d * P.n_faces + r.face[il]) * NP;
+#pragma unroll
+                        for (int a = 0; a < NF; ++a) {
+                            const int ma = Shape<DEG>::edof(il, a);
+                            T acc = T(0);
+#pragma unroll
+                            for (int bb = 0; bb < NF; ++bb)
+                                acc += R[ma * NP + Shape<DEG>::edof(il, bb)] * (T)pb[r.emap[il][bb]];
+                            b[c][ma] -= scin[c][il] * acc;
+                        }
+                    } else if (kind == 1) {
+                        const T sc = s[il] * r.bval[il] * P.wall_scale * r.es[il];
+#pragma unroll
+                        for (int a = 0; a < NF; ++a) {
+                            const int ma = Shape<DEG>::edof(il, a);
+                            T rs = T(0);
+#pragma unroll
+                            for (int bb = 0; bb < NF; ++bb) rs += R[ma * NP + Shape<DEG>::edof(il, bb)];
+                            b[c][ma] -= sc * rs;
+                        }
+                    } else {
+                        const double *fw = P.flux_wall + (size_t)r.face[il] * NP;
+#pragma unroll
+                        for (int m = 0; m < NP; ++m) b[c][m] -= s[il] * (-(T)fw[m]);
+                    }
+                }
+                if constexpr (PRECOMP) {
+                    const double *lu = P.lu + ((size_t)d * P.nt + i) * NP * NP;
+                    const int8_t *pv = P.piv + ((size_t)d * P.nt + i) * NP;
+#pragma unroll
+                    for (int m = 0; m < NP; ++m) {
+                        piv[c][m] = pv[m];
+#pragma unroll
+                        for (int l = 0; l < NP; ++l) A[c][m][l] = (T)lu[m * NP + l];
+                    }
+                } else {
+                    assemble<T, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A[c]);
+                    // partial pivoting (first maximum), multipliers stored below
+                    // the diagonal, 1/U_kk on it
+#pragma unroll
+                    for (int kk = 0; kk < NP; ++kk) {
+                        T big = fabs(A[c][kk][kk]);
+                        int p = kk;
+#pragma unroll
+                        for (int ii = kk + 1; ii < NP; ++ii) {
+                            const T v = fabs(A[c][ii][kk]);
+                            if (v > big) { big = v; p = ii; }
+                        }
+                        piv[c][kk] = p;
+#pragma unroll
+                        for (int ii = kk + 1; ii < NP; ++ii)
+                            if (p == ii)
+#pragma unroll
+                                for (int j = 0; j < NP; ++j) { const T tt = A[c][kk][j]; A[c][kk][j] = A[c][ii][j]; A[c][ii][j] = tt; }
+                        sing += (A[c][kk][kk] == T(0));
+                        const T rr = T(1) / A[c][kk][kk];
+#pragma unroll
+                        for (int ii = kk + 1; ii < NP; ++ii) {
+                            A[c][ii][kk] *= rr;
+#pragma unroll
+                            for (int j = kk + 1; j < NP; ++j) A[c][ii][j] -= A[c][ii][kk] * A[c][kk][j];
+                        }
+                        A[c][kk][kk] = rr;
+                    }
+                }
+            }
+        }
+        // ---- wait for level L-1, then the upwind inflow and the solves ------
+        if (G > 1 && L > 0) bar_sync(1 + (L - 1) % G, 2 * kTPG);
+        const int rbase = (L % Rr) * W;
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            if (cell[c] < 0) continue;
+#pragma unroll
+            for (int il = 0; il < 3; ++il) {
+                const int sl = slot[c][il];
+                if (sl < 0) continue;
+                const T *up = ring + (size_t)sl * NP;
+                const T *R = sref + (3 + il) * NP * NP;
+                T gv[NF];
+#pragma unroll
+                for (int bb = 0; bb < NF; ++bb) gv[bb] = up[emp[c][il][bb]];
+#pragma unroll
+                for (int a = 0; a < NF; ++a) {
+                    const int ma = Shape<DEG>::edof(il, a);
+                    T acc = T(0);
+#pragma unroll
+                    for (int bb = 0; bb < NF; ++bb) acc += R[ma * NP + Shape<DEG>::edof(il, bb)] * gv[bb];
+                    b[c][ma] -= scin[c][il] * acc;
+                }
+            }
+#pragma unroll
+            for (int kk = 0; kk < NP; ++kk) {
+                const int p = piv[c][kk];
+#pragma unroll
+                for (int j = kk + 1; j < NP; ++j)
+                    if (p == j) { const T tt = b[c][kk]; b[c][kk] = b[c][j]; b[c][j] = tt; }
+            }
+#pragma unroll
+            for (int kk = 0; kk < NP; ++kk)
+#pragma unroll
+                for (int j = kk + 1; j < NP; ++j) b[c][j] -= b[c][kk] * A[c][j][kk];
+#pragma unroll
+            for (int kk = NP - 1; kk >= 0; --kk) {
+                b[c][kk] *= A[c][kk][kk];
+#pragma unroll
+                for (int j = 0; j < kk; ++j) b[c][j] -= b[c][kk] * A[c][j][kk];
+            }
+            T *rs = ring + (size_t)(rbase + t + c * kTPG) * NP;
+            T *o1 = f1 + (size_t)cell[c] * NP;
+#pragma unroll
+            for (int m = 0; m < NP; ++m) { rs[m] = b[c][m]; o1[m] = b[c][m]; }
+            if (f2) {
+                T *o2 = f2 + (size_t)cell[c] * NP;
+#pragma unroll
+                for (int m = 0; m < NP; ++m) o2[m] = b[c][m];
+            }
+        }
+        if (G > 1) {
+            if (L + 1 < nlev) bar_arrive(1 + L % G, 2 * kTPG);
+        } else {
+            __syncthreads();
+        }
+    }
+    if (sing) atomicAdd(P.singular, sing);
+}
+
+template <typename T, int DEG, bool PRE>
+static int ring_launch_deg(pbte_ctx *c, const SweepParams<T> &P, const RingParams &Q, int cpt, size_t shm,
+                           cudaStream_t s) {
+    const int threads = Q.groups * kTPG;
+    auto go = [&](auto kern) {
+        if (shm > 48 * 1024 &&
+            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
+            return PBTE_ERR_CUDA;
+        kern<<<c->n_udir, threads, shm, s>>>(P, Q);
+        return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+    };
+    switch (cpt) {
+        case 1: return go(sweep_ring_kernel<T, DEG, PRE, 1>);
+        case 2: return go(sweep_ring_kernel<T, DEG, PRE, 2>);
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+}
+
+// Returns PBTE_ERR_UNSUPPORTED when the ring form does not fit (the caller
+// then uses the level-serial kernel).
+template <typename T, bool PRE>
+int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
+    if (c->deg > 3 || c->ring_W <= 0) return PBTE_ERR_UNSUPPORTED;
+    const int cpt = (c->ring_W + kTPG - 1) / kTPG;
+    if (cpt > 2 || (c->deg == 3 && cpt > 1)) return PBTE_ERR_UNSUPPORTED;
+    const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + (size_t)c->ring_R * c->ring_W * c->nd);
+    if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
+    RingParams Q{c->d_up_slot, c->d_class_W, c->d_class_R, c->d_udir_rep, c->d_udir_twin,
+                 c->deg <= 2 && cpt == 1 ? 3 : 2};
+    switch (c->deg) {
+        case 1: return ring_launch_deg<T, 1, PRE>(c, P, Q, cpt, shm, s);
+        case 2: return ring_launch_deg<T, 2, PRE>(c, P, Q, cpt, shm, s);
+        case 3: return ring_launch_deg<T, 3, PRE>(c, P, Q, cpt, shm, s);
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+}
+
+template int launch_ring<double, false>(pbte_ctx *, const SweepParams<double> &, cudaStream_t);
+template int launch_ring<double, true>(pbte_ctx *, const SweepParams<double> &, cudaStream_t);
+template int launch_ring<float, false>(pbte_ctx *, const SweepParams<float> &, cudaStream_t);
+
+}  // namespace pbte

@@ -16,7 +16,7 @@ REPO_ROOT = PKG_ROOT.parent
 CSRC = PKG_ROOT / "csrc"
 INCLUDE = REPO_ROOT / "include"
 LIB_PATH = PKG_ROOT / "_build" / "libpbte_gb300.so"
-SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_capi.cu"]
+SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_capi.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0
@@ -99,6 +99,7 @@ _SIGS = {
     "pbte_wall_flux_f32": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_residual_iterate": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_set_done_flag": ([_vp, _vp], ctypes.c_int),
+    "pbte_set_sweep_variant": ([_vp, ctypes.c_int], ctypes.c_int),
     "pbte_residual_check": ([_vp, _vp, ctypes.c_double, ctypes.c_int64, _vp, _vp, _vp,
                              ctypes.c_int64, _vp], ctypes.c_int),
     "pbte_transport_residual": ([_vp] * 9 + [_vp], ctypes.c_int),

@@ -81,6 +81,12 @@ typedef struct {
 int pbte_ctx_create(const pbte_case_desc *desc, int precompute, pbte_ctx **out);
 int pbte_ctx_destroy(pbte_ctx *ctx);
 
+/* Sweep kernel selection: 0 automatic (ring-pipelined when the level ring
+ * fits in shared memory, else level-serial), 1 level-serial, 2 ring only
+ * (PBTE_ERR_UNSUPPORTED from the sweep if it does not fit).  No reference
+ * counterpart (pybte's mode switch is precomputed vs on-the-fly). */
+int pbte_set_sweep_variant(pbte_ctx *ctx, int variant);
+
 /* Sizes the context was built with, and the device bytes it holds. */
 int pbte_ctx_info(const pbte_ctx *ctx, int64_t *n_levels_max, int64_t *n_classes,
                   int64_t *device_bytes);
