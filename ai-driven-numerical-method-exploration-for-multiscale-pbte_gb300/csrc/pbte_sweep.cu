@@ -231,6 +231,9 @@ static int ring_launch_deg(pbte_ctx *c, const SweepParams<T> &P, const RingParam
     switch (cpt) {
         case 1: return go(sweep_ring_kernel<T, DEG, PRE, 1>);
         case 2: return go(sweep_ring_kernel<T, DEG, PRE, 2>);
+        case 4:
+            if constexpr (sizeof(T) == 4 && DEG <= 2) return go(sweep_ring_kernel<T, DEG, PRE, 4>);
+            return PBTE_ERR_UNSUPPORTED;
         default: return PBTE_ERR_UNSUPPORTED;
     }
 }
@@ -240,8 +243,10 @@ static int ring_launch_deg(pbte_ctx *c, const SweepParams<T> &P, const RingParam
 template <typename T, bool PRE>
 int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     if (c->deg > 3 || c->ring_W <= 0) return PBTE_ERR_UNSUPPORTED;
-    const int cpt = (c->ring_W + kTPG - 1) / kTPG;
-    if (cpt > 2 || (c->deg == 3 && cpt > 1)) return PBTE_ERR_UNSUPPORTED;
+    int cpt = (c->ring_W + kTPG - 1) / kTPG;
+    if (cpt == 3) cpt = 4;
+    if (cpt > 4 || (cpt == 4 && (sizeof(T) != 4 || c->deg > 2)) || (c->deg == 3 && cpt > 1))
+        return PBTE_ERR_UNSUPPORTED;
     const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + (size_t)c->ring_R * c->ring_W * c->nd);
     if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
     RingParams Q{c->d_up_slot, c->d_class_W, c->d_class_R, c->d_udir_rep, c->d_udir_twin,

@@ -147,6 +147,10 @@ class SweepContext:
     def handle(self) -> ctypes.c_void_p:
         return self._ctx
 
+    def set_variant(self, variant: int) -> None:
+        """Sweep kernel: 0 automatic, 1 level-serial, 2 ring-pipelined only."""
+        _lib.check(_lib.lib().pbte_set_sweep_variant(self._ctx, int(variant)), "pbte_set_sweep_variant")
+
     def operator_bytes(self, n_tris: int, ndof: int) -> float:
         """Bytes of stored FP64 factors (``pybte/sweep.py:113-114``)."""
         return float(self.cxv.size) * n_tris * ndof * ndof * 8.0

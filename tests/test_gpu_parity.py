@@ -64,6 +64,41 @@ def test_sweep_moments_flux_match_oracle(cuda, deg, mode, south):
 
 
 @pytest.mark.parametrize("deg", [1, 2, 3])
+@pytest.mark.parametrize("mode", ["precomputed", "onthefly"])
+def test_ring_and_level_serial_sweeps_agree(cuda, deg, mode):
+    """The ring-pipelined kernel (one block per in-plane velocity, twins
+    stored from one solve) against the level-serial kernel and the oracle,
+    on meshes wide enough for two cells per thread (cavity 72: 10368 cells,
+    widest level ~144) where the ring supports it."""
+    mesh = "cavity:72" if deg < 3 else "cavity:24"
+    case = small_case(deg, 4, 8, 0.3, 0.03, mesh=mesh, sweep_mode=mode)
+    s = Solver(case)
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 21)
+    o.wall_flux()
+    s.ctx.wall_flux(s.vdf)
+    o.sweep()
+    out = {}
+    for variant in (1, 2):
+        s.ctx.set_variant(variant)
+        v = s.vdf.clone()
+        s.ctx.sweep(s.mom, v)
+        torch.cuda.synchronize()
+        out[variant] = v.cpu().numpy()
+        assert _rel(out[variant], o.vdf) < 1e-11, variant
+    if mode == "onthefly":
+        v32 = {}
+        for variant in (1, 2):
+            s.ctx.set_variant(variant)
+            w = torch.zeros(s.vdf.shape, dtype=torch.float32, device=s.device)
+            s.ctx.sweep_f32((s.mom.ts, s.mom.qxs, s.mom.qys), w, s.ctx.flux_wall)
+            torch.cuda.synchronize()
+            v32[variant] = w.double().cpu().numpy()
+            assert _rel(v32[variant], o.vdf) < 2e-5, variant
+    s.ctx.set_variant(0)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
 def test_transport_residual_of_random_state(cuda, deg):
     s = Solver(small_case(deg, 4, 8, 0.2, 0.02))
     o = Oracle(s.disc, nthreads=4)
