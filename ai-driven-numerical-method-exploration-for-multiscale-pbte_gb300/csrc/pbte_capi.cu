@@ -69,6 +69,20 @@ int pbte_set_sweep_variant(pbte_ctx *c, int variant) {
     return PBTE_OK;
 }
 
+int pbte_set_ring_groups(pbte_ctx *c, int groups) {
+    if (!c || groups < 0 || groups > 15) return PBTE_ERR_ARG;
+    c->ring_groups = groups;
+    return PBTE_OK;
+}
+
+int pbte_ctx_schedule(const pbte_ctx *c, int64_t *ring_w, int64_t *ring_r, int64_t *n_unique_dirs) {
+    if (!c) return PBTE_ERR_ARG;
+    if (ring_w) *ring_w = c->ring_W;
+    if (ring_r) *ring_r = c->ring_R;
+    if (n_unique_dirs) *n_unique_dirs = c->n_udir;
+    return PBTE_OK;
+}
+
 int pbte_set_done_flag(pbte_ctx *c, const int32_t *done) {
     if (!c) return PBTE_ERR_ARG;
     c->done = done;

@@ -75,6 +75,7 @@ struct pbte_ctx {
     int32_t *d_udir_rep = nullptr, *d_udir_twin = nullptr;
     int n_udir = 0;
     int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
+    int ring_groups = 0;            // thread groups of the ring pipeline (0: default)
 };
 
 // launchers (pbte_kernels.cu)

@@ -16,12 +16,14 @@
 //
 // The ring slot of every upwind dependency, (level % R) * W + position, is
 // precomputed per direction class on the host (pbte_ctx.cu).
+#include <algorithm>
+
 #include "pbte_device.cuh"
 
 namespace pbte {
 
-constexpr int kTPG = 128;       // threads per group
-constexpr int kMaxGroups = 3;
+constexpr int kTPG = 64;        // threads per group
+constexpr int kMaxGroups = 4;
 
 struct RingParams {
     const int32_t *up_slot;     // [nclass * n_tris][3] absolute level-order index
@@ -125,6 +127,25 @@ __global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepPara
 #pragma unroll
                         for (int l = 0; l < NP; ++l) A[c][m][l] = (T)lu[m * NP + l];
                     }
+                } else if constexpr (sizeof(T) == 4) {
+                    // FP32: no row interchanges.  x^T A x = |x|^2_M / tau_c +
+                    // (1/2) sum_edges |c.n| |x|^2_edge > 0, so every leading
+                    // block is non-singular; the FP64 defect correction around
+                    // the FP32 sweeps absorbs the extra rounding.
+                    assemble<T, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A[c]);
+#pragma unroll
+                    for (int kk = 0; kk < NP; ++kk) {
+                        piv[c][kk] = kk;
+                        sing += (A[c][kk][kk] == T(0));
+                        const T rr = __frcp_rn(A[c][kk][kk]);
+#pragma unroll
+                        for (int ii = kk + 1; ii < NP; ++ii) {
+                            A[c][ii][kk] *= rr;
+#pragma unroll
+                            for (int j = kk + 1; j < NP; ++j) A[c][ii][j] -= A[c][ii][kk] * A[c][kk][j];
+                        }
+                        A[c][kk][kk] = rr;
+                    }
                 } else {
                     assemble<T, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A[c]);
                     // partial pivoting (first maximum), multipliers stored below
@@ -181,12 +202,14 @@ __global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepPara
                     b[c][ma] -= scin[c][il] * acc;
                 }
             }
+            if constexpr (sizeof(T) == 8) {
 #pragma unroll
-            for (int kk = 0; kk < NP; ++kk) {
-                const int p = piv[c][kk];
+                for (int kk = 0; kk < NP; ++kk) {
+                    const int p = piv[c][kk];
 #pragma unroll
-                for (int j = kk + 1; j < NP; ++j)
-                    if (p == j) { const T tt = b[c][kk]; b[c][kk] = b[c][j]; b[c][j] = tt; }
+                    for (int j = kk + 1; j < NP; ++j)
+                        if (p == j) { const T tt = b[c][kk]; b[c][kk] = b[c][j]; b[c][j] = tt; }
+                }
             }
 #pragma unroll
             for (int kk = 0; kk < NP; ++kk)
@@ -249,8 +272,8 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
         return PBTE_ERR_UNSUPPORTED;
     const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + (size_t)c->ring_R * c->ring_W * c->nd);
     if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
-    RingParams Q{c->d_up_slot, c->d_class_W, c->d_class_R, c->d_udir_rep, c->d_udir_twin,
-                 c->deg <= 2 && cpt == 1 ? 3 : 2};
+    const int groups = c->ring_groups > 0 ? std::min(c->ring_groups, kMaxGroups) : kMaxGroups;
+    RingParams Q{c->d_up_slot, c->d_class_W, c->d_class_R, c->d_udir_rep, c->d_udir_twin, groups};
     switch (c->deg) {
         case 1: return ring_launch_deg<T, 1, PRE>(c, P, Q, cpt, shm, s);
         case 2: return ring_launch_deg<T, 2, PRE>(c, P, Q, cpt, shm, s);

@@ -100,6 +100,9 @@ _SIGS = {
     "pbte_residual_iterate": ([_vp, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_set_done_flag": ([_vp, _vp], ctypes.c_int),
     "pbte_set_sweep_variant": ([_vp, ctypes.c_int], ctypes.c_int),
+    "pbte_set_ring_groups": ([_vp, ctypes.c_int], ctypes.c_int),
+    "pbte_ctx_schedule": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
+                           ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_residual_check": ([_vp, _vp, ctypes.c_double, ctypes.c_int64, _vp, _vp, _vp,
                              ctypes.c_int64, _vp], ctypes.c_int),
     "pbte_transport_residual": ([_vp] * 9 + [_vp], ctypes.c_int),

@@ -151,6 +151,17 @@ class SweepContext:
         """Sweep kernel: 0 automatic, 1 level-serial, 2 ring-pipelined only."""
         _lib.check(_lib.lib().pbte_set_sweep_variant(self._ctx, int(variant)), "pbte_set_sweep_variant")
 
+    def set_groups(self, groups: int) -> None:
+        """Pipeline depth of the ring sweep (0: default)."""
+        _lib.check(_lib.lib().pbte_set_ring_groups(self._ctx, int(groups)), "pbte_set_ring_groups")
+
+    def schedule(self) -> dict:
+        w, r, u = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(_lib.lib().pbte_ctx_schedule(self._ctx, ctypes.byref(w), ctypes.byref(r), ctypes.byref(u)),
+                   "pbte_ctx_schedule")
+        return {"ring_W": w.value, "ring_R": r.value, "unique_dirs": u.value,
+                "levels": self.n_levels_max, "classes": self.n_classes}
+
     def operator_bytes(self, n_tris: int, ndof: int) -> float:
         """Bytes of stored FP64 factors (``pybte/sweep.py:113-114``)."""
         return float(self.cxv.size) * n_tris * ndof * ndof * 8.0

@@ -87,6 +87,14 @@ int pbte_ctx_destroy(pbte_ctx *ctx);
  * counterpart (pybte's mode switch is precomputed vs on-the-fly). */
 int pbte_set_sweep_variant(pbte_ctx *ctx, int variant);
 
+/* Pipeline depth of the ring sweep (thread groups of 64 per block, 0 =
+ * default 4, at most 4 are used); the tuning knob of the autotuner.  And the
+ * schedule the context derived: widest level, deepest upwind level gap, and
+ * the number of distinct in-plane velocities (one sweep block each). */
+int pbte_set_ring_groups(pbte_ctx *ctx, int groups);
+int pbte_ctx_schedule(const pbte_ctx *ctx, int64_t *ring_w, int64_t *ring_r,
+                      int64_t *n_unique_dirs);
+
 /* Sizes the context was built with, and the device bytes it holds. */
 int pbte_ctx_info(const pbte_ctx *ctx, int64_t *n_levels_max, int64_t *n_classes,
                   int64_t *device_bytes);
