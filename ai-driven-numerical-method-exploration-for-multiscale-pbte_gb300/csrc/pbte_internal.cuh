@@ -99,6 +99,9 @@ int launch_residual_check(pbte_ctx *c, const double *res, double tol, int64_t tm
 int launch_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
                               const double *vdf, const double *fw, const double *pbuf,
                               double *num, double *den, cudaStream_t s);
+int launch_transport_residual_scratch(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                                      const double *vdf, const double *fw, double *num, double *den,
+                                      double *S, cudaStream_t s);
 int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s);
 int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk,
                       const int32_t *tri_list, const int32_t *lfc_list, double *out,

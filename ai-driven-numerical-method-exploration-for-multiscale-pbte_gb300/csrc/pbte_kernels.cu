@@ -627,6 +627,29 @@ int launch_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, 
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
+// The same two kernels with the moment sources in caller-provided device
+// scratch of 3 * ndof * n_tris doubles instead of the context's own.
+int launch_transport_residual_scratch(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                                      const double *vdf, const double *fw, double *num, double *den,
+                                      double *S, cudaStream_t s) {
+    const int th = 128;
+    sources_kernel<double><<<(c->n_tris + th - 1) / th, th, 0, s>>>(c->d_cells64, c->d_ref64, ts, qxs, qys, S,
+                                                                   c->n_tris, c->nd, nullptr);
+    SweepParams<double> P = make_params<double>(c);
+    P.done = nullptr;
+    P.cells = c->d_cells64; P.ref = c->d_ref64; P.S = S; P.vdf = const_cast<double *>(vdf);
+    P.flux_wall = fw; P.pbuf = nullptr; P.use_pbuf = 0;
+    switch (c->deg) {
+        case 1: transport_residual_kernel<1><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        case 2: transport_residual_kernel<2><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        case 3: transport_residual_kernel<3><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        case 4: transport_residual_kernel<4><<<c->ndir, kSweepThreads, 0, s>>>(P, num, den); break;
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+    scale_by_weight_kernel<<<(c->ndir + 127) / 128, 128, 0, s>>>(num, den, c->d_w, c->ndir);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
 int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s) {
     const int th = 128;
     hot_source_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(vdf, c->d_cells64, c->d_ref64, c->d_cx, c->d_cy,

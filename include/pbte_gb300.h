@@ -140,6 +140,25 @@ int pbte_transport_residual(pbte_ctx *ctx, const double *ts, const double *qxs,
                             const double *qys, const double *vdf, const double *flux_wall,
                             const double *pbuf, double *num, double *den, void *stream);
 
+/* The same transport residual for callers that cannot allocate device memory
+ * where they call from (code running while a CUDA graph is captured in global
+ * capture mode, where cudaMalloc is illegal; hosts whose device memory belongs
+ * to their own pool) or that must leave the context's scratch to a sweep in
+ * flight.  It allocates nothing: the moment sources go to a static 4 MiB
+ * device array (524288 doubles) held by every GPU that loads the library
+ * until exit, so 3 * ndof * n_tris must be <= 524288 (else PBTE_ERR_ARG).
+ * The first call on a device looks the array up (cudaGetSymbolAddress, with
+ * that device current), which under lazy module loading is also when the
+ * runtime commits the array's memory: make that first call before any
+ * stream capture starts; later calls change no device memory.  All calls
+ * share the array, so calls that overlap on the GPU race; no state carries
+ * from one call to the next.  Periodic faces: PBTE_ERR_UNSUPPORTED.
+ * No counterpart in the reference. */
+int pbte_transport_residual_noalloc(pbte_ctx *ctx, const double *ts, const double *qxs,
+                                    const double *qys, const double *vdf,
+                                    const double *flux_wall, double *num, double *den,
+                                    void *stream);
+
 /* Device-side stop flag for graph-captured iteration: when *done != 0 every
  * sweep/moment/residual kernel launched with the context returns at once.
  * pbte_set_done_flag(ctx, ptr) installs it (NULL removes it).

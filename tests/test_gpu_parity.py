@@ -68,9 +68,9 @@ def test_sweep_moments_flux_match_oracle(cuda, deg, mode, south):
 def test_ring_and_level_serial_sweeps_agree(cuda, deg, mode):
     """The ring-pipelined kernel (one block per in-plane velocity, twins
     stored from one solve) against the level-serial kernel and the oracle,
-    on meshes wide enough for two cells per thread (cavity 72: 10368 cells,
-    widest level ~144) where the ring supports it."""
-    mesh = "cavity:72" if deg < 3 else "cavity:24"
+    on a 40 x 40 square (FP64 ring in shared memory) and, for FP32, on a
+    72 x 72 square (levels 72 wide: two cells per thread)."""
+    mesh = "cavity:40" if deg < 3 else "cavity:24"
     case = small_case(deg, 4, 8, 0.3, 0.03, mesh=mesh, sweep_mode=mode)
     s = Solver(case)
     o = Oracle(s.disc, nthreads=4)
@@ -87,6 +87,14 @@ def test_ring_and_level_serial_sweeps_agree(cuda, deg, mode):
         out[variant] = v.cpu().numpy()
         assert _rel(out[variant], o.vdf) < 1e-11, variant
     if mode == "onthefly":
+        if deg < 3:
+            s = Solver(small_case(deg, 4, 8, 0.3, 0.03, mesh="cavity:72", sweep_mode=mode))
+            assert s.ctx.schedule()["ring_W"] > 64
+            o = Oracle(s.disc, nthreads=4)
+            _seed_state(s, o, 22)
+            o.wall_flux()
+            s.ctx.wall_flux(s.vdf)
+            o.sweep()
         v32 = {}
         for variant in (1, 2):
             s.ctx.set_variant(variant)
