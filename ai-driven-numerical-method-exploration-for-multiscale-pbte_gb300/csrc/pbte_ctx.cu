@@ -85,7 +85,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_edofs, c->d_dir_class, c->d_class_lvl_off, c->d_class_nlev, c->d_lvl_ptr,
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
-                    c->d_udir_rep, c->d_udir_twin};
+                    c->d_udir_rep, c->d_udir_twin, c->d_srec64, c->d_srec32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -233,7 +233,10 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     c->nclass = (int)class_rep.size();
     std::vector<int32_t> lvl_cells((size_t)c->nclass * nt), lvl_ptr, class_off(c->nclass),
         class_nlev(c->nclass);
-    std::vector<int32_t> level, indeg, queue, count, pos(nt);
+    std::vector<int32_t> level, indeg, queue, count, pos(nt), far_idx;
+    std::vector<pbte::SweepRec<double>> srec64((size_t)c->nclass * nt);
+    std::vector<pbte::SweepRec<float>> srec32((size_t)c->nclass * nt);
+    constexpr int kNearDepth = 4;
     // ring of upwind values in shared memory: slot (level % R) * W + position,
     // R = 1 + the largest level gap of an in-sweep dependency, W = widest level
     std::vector<int32_t> up_slot((size_t)c->nclass * nt * 3, -1), class_W(c->nclass), class_R(c->nclass);
@@ -258,6 +261,9 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
             pos[i] = fill[level[i]] - count[level[i]];
             lvl_cells[(size_t)k * nt + fill[level[i]]++] = i;
         }
+        // near ring of at most kNearDepth levels; an upwind value needed further
+        // ahead (rare: near the lines where the mesh diagonals flip) is also
+        // kept in a dedicated far slot
         int R = 1;
         const double cx = d->cxv[dir], cy = d->cyv[dir];
         for (int i = 0; i < nt; ++i)
@@ -266,16 +272,38 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
                 if (nb < 0 || d->face_bc[fc] >= 0) continue;
                 if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0) R = std::max(R, level[i] - level[nb] + 1);
             }
+        R = std::min(R, kNearDepth);
         class_W[k] = W;
         class_R[k] = R;
+        far_idx.assign(nt, -1);
+        int nfar = 0;
         for (int i = 0; i < nt; ++i) {
             size_t p = (size_t)k * nt + count[level[i]] + pos[i];
             for (int il = 0; il < 3; ++il) {
                 int nb = d->upwind_tri[i * 3 + il], fc = d->tri_faces[i * 3 + il];
                 if (nb < 0 || d->face_bc[fc] >= 0) continue;
-                if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0)
-                    up_slot[p * 3 + il] = (level[nb] % R) * W + pos[nb];
+                if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0) {
+                    if (level[i] - level[nb] < R) {
+                        up_slot[p * 3 + il] = (level[nb] % R) * W + pos[nb];
+                    } else {
+                        if (far_idx[nb] < 0) far_idx[nb] = nfar++;
+                        up_slot[p * 3 + il] = -2 - far_idx[nb];
+                    }
+                }
             }
+        }
+        c->far_max = std::max(c->far_max, nfar);
+        for (int p = 0; p < nt; ++p) {
+            const int i = lvl_cells[(size_t)k * nt + p];
+            auto &s64 = srec64[(size_t)k * nt + p];
+            auto &s32 = srec32[(size_t)k * nt + p];
+            std::memset(&s64, 0, sizeof(s64));
+            std::memset(&s32, 0, sizeof(s32));
+            s64.c = r64[i];
+            s32.c = r32[i];
+            s64.cell = s32.cell = i;
+            s64.far_out = s32.far_out = far_idx[i];
+            for (int il = 0; il < 3; ++il) s64.up[il] = s32.up[il] = up_slot[((size_t)k * nt + p) * 3 + il];
         }
         c->nlev_max = std::max(c->nlev_max, nlev);
         c->ring_W = std::max(c->ring_W, W);
@@ -304,6 +332,8 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     TRY(upload(lvl_ptr.data(), lvl_ptr.size(), &c->d_lvl_ptr, &c->device_bytes));
     TRY(upload(lvl_cells.data(), lvl_cells.size(), &c->d_lvl_cells, &c->device_bytes));
     TRY(upload(up_slot.data(), up_slot.size(), &c->d_up_slot, &c->device_bytes));
+    TRY(upload(srec64.data(), srec64.size(), &c->d_srec64, &c->device_bytes));
+    TRY(upload(srec32.data(), srec32.size(), &c->d_srec32, &c->device_bytes));
     TRY(upload(class_W.data(), class_W.size(), &c->d_class_W, &c->device_bytes));
     TRY(upload(class_R.data(), class_R.size(), &c->d_class_R, &c->device_bytes));
     TRY(upload(urep.data(), urep.size(), &c->d_udir_rep, &c->device_bytes));

@@ -30,6 +30,19 @@ struct alignas(16) CellRec {
     int8_t emap[3][kMaxNf]; // neighbour DOF facing each of this element's edge DOFs
 };
 
+// Element record in a direction class's sweep order: the element's operator
+// description plus where its upwind values live during a sweep.
+// up[il]: -1 no in-sweep inflow; >= 0 slot of the near ring
+// ((level % R) * W + position); <= -2 far slot -(up + 2).
+// far_out: far slot this element's values must also be kept in, or -1.
+template <typename T>
+struct alignas(16) SweepRec {
+    CellRec<T> c;
+    int32_t cell, far_out;
+    int32_t up[3];
+    int32_t pad[3];
+};
+
 struct WallFace {
     int32_t face, tri, lfc, pad;
     double nx, ny;  // inward normal (-n_out of the adjacent element)
@@ -76,6 +89,10 @@ struct pbte_ctx {
     int n_udir = 0;
     int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
     int ring_groups = 0;            // thread groups of the ring pipeline (0: default)
+    // per-class records in sweep order ([nclass][n_tris]) and far-slot count
+    pbte::SweepRec<double> *d_srec64 = nullptr;
+    pbte::SweepRec<float> *d_srec32 = nullptr;
+    int far_max = 0;
 };
 
 // launchers (pbte_kernels.cu)
