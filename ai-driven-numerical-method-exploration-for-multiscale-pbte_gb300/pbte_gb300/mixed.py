@@ -30,10 +30,14 @@ __all__ = ["run_mixed", "MixedOptions"]
 
 
 class MixedOptions:
-    refine_tol = 1e-12      # stop on ||r|| / ||F64(u)||
-    inner_rtol = 1e-5       # inner relative accuracy per outer step
+    refine_tol = 1e-11      # stop on ||r|| / ||F64(u)||
+    inner_rtol = 1e-6       # inner relative accuracy per outer step (FP32 limits it to ~1e-6)
     max_outer = 12
     max_inner = 200_000
+    #: inner GMRES products per outer step before handing back to the FP64
+    #: defect correction (FP32 round-off can stall an inner solve short of
+    #: inner_rtol; the next outer step then starts from a fresh FP64 defect)
+    inner_budget_restarts = 4
 
 
 def run_mixed(solver, opts: MixedOptions | None = None):
@@ -74,7 +78,7 @@ def run_mixed(solver, opts: MixedOptions | None = None):
             cap = basis_cap(c, n)
             before = op32.sweeps
             d, _, _ = gmres(lambda v: v - op32.apply(v), r, tol_abs=opts.inner_rtol * rn,
-                            maxiter=opts.max_inner, max_basis=cap)
+                            maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap), max_basis=cap)
             inner_sweeps += op32.sweeps - before
         u = u + d
         fu = op64.apply(u)
