@@ -85,7 +85,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_edofs, c->d_dir_class, c->d_class_lvl_off, c->d_class_nlev, c->d_lvl_ptr,
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
-                    c->d_udir_rep, c->d_udir_twin, c->d_srec64, c->d_srec32};
+                    c->d_udir_rep, c->d_udir_twin, c->d_srec64, c->d_srec32, c->d_mom_part};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -343,6 +343,7 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     TRY(alloc((size_t)3 * nd * nt, &c->d_S64, &c->device_bytes));
     TRY(alloc((size_t)3 * nd * nt, &c->d_S32, &c->device_bytes));
     TRY(alloc((size_t)4096, &c->d_red, &c->device_bytes));
+    TRY(alloc((size_t)((ndir + 31) / 32) * 3 * nd * nt, &c->d_mom_part, &c->device_bytes));
     TRY(alloc((size_t)1, &c->d_singular, &c->device_bytes));
     if (cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
 

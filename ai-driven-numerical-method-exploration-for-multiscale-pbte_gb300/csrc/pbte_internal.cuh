@@ -93,6 +93,7 @@ struct pbte_ctx {
     pbte::SweepRec<double> *d_srec64 = nullptr;
     pbte::SweepRec<float> *d_srec32 = nullptr;
     int far_max = 0;
+    double *d_mom_part = nullptr;   // [ceil(ndir/32)][3][n_tris*ndof] moment partial sums
 };
 
 // launchers (pbte_kernels.cu)

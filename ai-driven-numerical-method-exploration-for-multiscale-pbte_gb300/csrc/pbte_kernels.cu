@@ -188,6 +188,64 @@ __global__ void moments_kernel(const T *vdf, const double *cx, const double *cy,
     qys[(size_t)l * nt + i] = ssy;
 }
 
+// Moments in two passes: partial sums over chunks of kMomChunk ordinates
+// (FP32 within a chunk for an FP32 distribution, FP64 otherwise), then a
+// fixed-order FP64 sum of the chunks -- deterministic, and wide enough to fill
+// the GPU (one thread per element DOF per chunk).
+constexpr int kMomChunk = 32;
+
+template <typename T>
+__global__ void moments_partial_kernel(const T *vdf, const double *cx, const double *cy, const double *w,
+                                       int ndir, int total, double *part, const int32_t *done) {
+    if (stopped(done)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ch = blockIdx.y;
+    if (t >= total) return;
+    const int d0 = ch * kMomChunk, d1 = min(ndir, d0 + kMomChunk);
+    double s0, sx, sy;
+    if constexpr (sizeof(T) == 8) {
+        s0 = sx = sy = 0.0;
+        for (int d = d0; d < d1; ++d) {
+            const double fw = vdf[(size_t)d * total + t] * w[d];
+            s0 += fw;
+            sx += cx[d] * fw;
+            sy += cy[d] * fw;
+        }
+    } else {
+        float a = 0.f, bx = 0.f, by = 0.f;
+        for (int d = d0; d < d1; ++d) {
+            const float fw = (float)vdf[(size_t)d * total + t] * (float)w[d];
+            a += fw;
+            bx += (float)cx[d] * fw;
+            by += (float)cy[d] * fw;
+        }
+        s0 = a; sx = bx; sy = by;
+    }
+    double *p = part + (size_t)ch * 3 * total;
+    p[t] = s0;
+    p[total + t] = sx;
+    p[2 * total + t] = sy;
+}
+
+__global__ void moments_combine_kernel(const double *part, int nch, int nt, int NP, double cv, double *ts,
+                                       double *qxs, double *qys, const int32_t *done) {
+    if (stopped(done)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int total = nt * NP;
+    if (t >= total) return;
+    double s0 = 0.0, sx = 0.0, sy = 0.0;
+    for (int ch = 0; ch < nch; ++ch) {
+        const double *p = part + (size_t)ch * 3 * total;
+        s0 += p[t];
+        sx += p[total + t];
+        sy += p[2 * total + t];
+    }
+    const int i = t / NP, l = t % NP;
+    ts[(size_t)l * nt + i] = s0 / cv;
+    qxs[(size_t)l * nt + i] = sx;
+    qys[(size_t)l * nt + i] = sy;
+}
+
 __global__ void element_integrals_kernel(const double *ts, const double *qxs, const double *qys,
                                          const double *int_tri, int nt, int NP, double cv, double *temp,
                                          double *qx, double *qy, const int32_t *done) {
@@ -564,8 +622,17 @@ template <typename T>
 static int moments_impl(pbte_ctx *c, const T *vdf, double *ts, double *qxs, double *qys, double *temp,
                         double *qx, double *qy, cudaStream_t s) {
     const int total = c->n_tris * c->nd, th = 256;
-    moments_kernel<T><<<(total + th - 1) / th, th, 0, s>>>(vdf, c->d_cx, c->d_cy, c->d_w, c->ndir, c->n_tris,
-                                                          c->nd, c->cv, ts, qxs, qys, c->done);
+    const int nch = (c->ndir + kMomChunk - 1) / kMomChunk;
+    if (c->d_mom_part) {
+        moments_partial_kernel<T><<<dim3((total + th - 1) / th, nch), th, 0, s>>>(vdf, c->d_cx, c->d_cy, c->d_w,
+                                                                                  c->ndir, total, c->d_mom_part,
+                                                                                  c->done);
+        moments_combine_kernel<<<(total + th - 1) / th, th, 0, s>>>(c->d_mom_part, nch, c->n_tris, c->nd, c->cv, ts,
+                                                                   qxs, qys, c->done);
+    } else {
+        moments_kernel<T><<<(total + th - 1) / th, th, 0, s>>>(vdf, c->d_cx, c->d_cy, c->d_w, c->ndir, c->n_tris,
+                                                              c->nd, c->cv, ts, qxs, qys, c->done);
+    }
     element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts, qxs, qys, c->d_int_tri, c->n_tris,
                                                                      c->nd, c->cv, temp, qx, qy, c->done);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;

@@ -116,6 +116,74 @@ class FixedPointOperator:
             s.ctx.flux_wall.copy_(fw)
 
 
+class ArnoldiGraphs:
+    """One Arnoldi column per CUDA graph replay.
+
+    For ``A v = v - (F(v) - g)`` (``g`` None: ``A v = v - F(v)``) the graph of
+    column ``j`` copies ``q_j`` into the operator's input, runs the sweep,
+    moments and emission, forms ``w = A q_j`` and both Gram-Schmidt passes
+    against ``q_0..q_j``, and leaves ``[h_0..h_j, ||w||]`` in a small device
+    buffer: the host reads that buffer once per product (for the Givens
+    rotations and the stopping test) instead of driving a dozen launches.
+    Graphs are captured on first use of each ``j`` and replayed across
+    restarts."""
+
+    def __init__(self, op: FixedPointOperator, g: torch.Tensor | None, m_cap: int):
+        self.op = op
+        n = op.n
+        dev = op.s.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.n = n
+        self.m_cap = m_cap
+        self.Q = torch.zeros((m_cap + 1, n), **f64)
+        self.w = torch.zeros(n, **f64)
+        self.tmp = torch.zeros(n, **f64)
+        self.c1 = torch.zeros(m_cap + 1, **f64)
+        self.c2 = torch.zeros(m_cap + 1, **f64)
+        self.h = torch.zeros(m_cap + 2, **f64)
+        self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
+        self.g = g
+        self.graphs = {}
+        self.stream = torch.cuda.Stream(device=dev)
+        self.on_product = None   # called after every product (sweep bookkeeping)
+
+    def _record(self, j: int) -> None:
+        op = self.op
+        n = self.n
+        qj = self.Q[j]
+        Qj = self.Q[:j + 1]
+        op.uin[:n].copy_(qj)
+        op._launch(torch.cuda.current_stream().cuda_stream)
+        if self.g is not None:
+            torch.sub(op.uout[:n], self.g, out=self.tmp)
+            torch.sub(qj, self.tmp, out=self.w)
+        else:
+            torch.sub(qj, op.uout[:n], out=self.w)
+        torch.mv(Qj, self.w, out=self.c1[:j + 1])
+        torch.mv(Qj.T, self.c1[:j + 1], out=self.tmp)
+        self.w.sub_(self.tmp)
+        torch.mv(Qj, self.w, out=self.c2[:j + 1])
+        torch.mv(Qj.T, self.c2[:j + 1], out=self.tmp)
+        self.w.sub_(self.tmp)
+        torch.add(self.c1[:j + 1], self.c2[:j + 1], out=self.h[:j + 1])
+        torch.linalg.vector_norm(self.w, out=self.h[j + 1])
+
+    def column(self, j: int) -> np.ndarray:
+        if j not in self.graphs:
+            torch.cuda.synchronize(self.op.s.device)
+            gr = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gr, stream=self.stream):
+                self._record(j)
+            self.graphs[j] = gr
+        self.graphs[j].replay()
+        self.h_host[:j + 2].copy_(self.h[:j + 2], non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        self.op.sweeps += 1
+        if self.on_product is not None:
+            self.on_product()
+        return self.h_host[:j + 2].numpy().copy()
+
+
 def _back_substitute(r, y):
     out = np.array(y, dtype=float)
     for i in range(out.size - 1, -1, -1):
@@ -125,13 +193,17 @@ def _back_substitute(r, y):
 
 
 def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, max_basis=None,
-          callback=None):
+          callback=None, arnoldi: ArnoldiGraphs | None = None):
     """GMRES for ``A x = b`` with device vectors (``pybte/krylov.py:150-246``).
-    Returns ``(x, converged, n_matvec)``."""
+    With ``arnoldi`` (graphs of ``A`` for the same operator) each product and
+    its orthogonalisation is one graph replay.  Returns ``(x, converged,
+    n_matvec)``."""
     n = b.numel()
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     maxiter = int(n if maxiter is None else maxiter)
     m_cap = maxiter if max_basis is None else max(1, min(int(max_basis), maxiter))
+    if arnoldi is not None and m_cap <= arnoldi.m_cap:
+        return _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, arnoldi)
     nmv = 0
     converged = halted = False
     while nmv < maxiter and not converged and not halted:
@@ -202,6 +274,68 @@ def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, 
     return x, converged, nmv
 
 
+def _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, ar: ArnoldiGraphs):
+    """The loop of :func:`gmres` with the basis in ``ar.Q`` and every Arnoldi
+    column from one graph replay; same arithmetic, same stopping."""
+    nmv = 0
+    converged = halted = False
+    Q = ar.Q
+    while nmv < maxiter and not converged and not halted:
+        if bool(torch.any(x != 0).item()):
+            r = b - matvec(x)
+            nmv += 1
+            if callback is not None and callback(float(torch.linalg.vector_norm(r).item())):
+                halted = True
+                break
+        else:
+            r = b.clone()
+        beta = float(torch.linalg.vector_norm(r).item())
+        if beta <= tol_abs:
+            converged = True
+            break
+        m = min(m_cap, maxiter - nmv)
+        if m <= 0:
+            break
+        Q[0].copy_(r / beta)
+        cols, cs, sn, gam = [], [], [], [beta]
+        for j in range(m):
+            col = ar.column(j)
+            nmv += 1
+            hn = float(col[j + 1])
+            for i in range(j):
+                t = cs[i] * col[i] + sn[i] * col[i + 1]
+                col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1]
+                col[i] = t
+            d = float(np.hypot(col[j], col[j + 1]))
+            c_, s_ = (1.0, 0.0) if d == 0.0 else (col[j] / d, col[j + 1] / d)
+            cs.append(c_)
+            sn.append(s_)
+            col[j] = d
+            cols.append(col[:j + 1].copy())
+            gam.append(-s_ * gam[j])
+            gam[j] = c_ * gam[j]
+            res = abs(gam[j + 1])
+            stop = bool(callback(res)) if callback is not None else False
+            if res <= tol_abs:
+                converged = True
+                break
+            if stop:
+                halted = True
+                break
+            if hn == 0.0:
+                break
+            if j + 1 < m:
+                torch.div(ar.w, hn, out=Q[j + 1])
+        k = len(cols)
+        if k:
+            rmat = np.zeros((k, k))
+            for j, col in enumerate(cols):
+                rmat[:j + 1, j] = col
+            y = torch.from_numpy(_back_substitute(rmat, np.asarray(gam[:k]))).to(b.device)
+            x += Q[:k].T @ y
+    return x, converged, nmv
+
+
 def basis_cap(case, n: int) -> int:
     if case.scheme.krylov_restart is not None:
         return int(case.scheme.krylov_restart)
@@ -247,6 +381,12 @@ def run_krylov(solver):
         return reached >= 0 and n - reached > max(64, reached // 4)
 
     x = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
+    ar = ArnoldiGraphs(op, g, cap) if cap <= 512 else None
+    if ar is not None:
+        def product():
+            masses.append(np.nan)
+            residuals.append(np.nan)
+        ar.on_product = product
     converged = False
     final = float("nan")
     for _ in range(c.scheme.krylov_max_rounds):
@@ -254,7 +394,8 @@ def run_krylov(solver):
         if budget <= 0:
             break
         reached = -1
-        x, _, _ = gmres(matvec, g, x0=x, tol_abs=target, maxiter=budget, max_basis=cap, callback=on_residual)
+        x, _, _ = gmres(matvec, g, x0=x, tol_abs=target, maxiter=budget, max_basis=cap, callback=on_residual,
+                        arnoldi=ar)
         sweep(x)
         op.publish()
         final = solver.ctx.true_residual(solver.mom, solver.vdf)

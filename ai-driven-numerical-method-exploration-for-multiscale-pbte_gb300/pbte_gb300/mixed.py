@@ -24,7 +24,7 @@ import time
 import numpy as np
 import torch
 
-from .krylov import FixedPointOperator, basis_cap, gmres
+from .krylov import ArnoldiGraphs, FixedPointOperator, basis_cap, gmres
 
 __all__ = ["run_mixed", "MixedOptions"]
 
@@ -51,6 +51,7 @@ def run_mixed(solver, opts: MixedOptions | None = None):
     n = op64.n
     dev = solver.device
     u = torch.zeros(n, dtype=torch.float64, device=dev)
+    ar32 = None
     history = []
     inner_sweeps = 0
     converged = False
@@ -76,9 +77,12 @@ def run_mixed(solver, opts: MixedOptions | None = None):
                     break
         else:
             cap = basis_cap(c, n)
+            if ar32 is None and cap <= 512:
+                ar32 = ArnoldiGraphs(op32, None, cap)
             before = op32.sweeps
             d, _, _ = gmres(lambda v: v - op32.apply(v), r, tol_abs=opts.inner_rtol * rn,
-                            maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap), max_basis=cap)
+                            maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap), max_basis=cap,
+                            arnoldi=ar32)
             inner_sweeps += op32.sweeps - before
         u = u + d
         fu = op64.apply(u)
