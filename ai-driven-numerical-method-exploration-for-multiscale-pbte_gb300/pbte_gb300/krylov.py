@@ -146,6 +146,14 @@ class ArnoldiGraphs:
         self.graphs = {}
         self.stream = torch.cuda.Stream(device=dev)
         self.on_product = None   # called after every product (sweep bookkeeping)
+        # run the captured library ops once outside capture (cuBLAS handle
+        # creation is not allowed while a graph is being captured)
+        self.stream.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(self.stream):
+            torch.mv(self.Q[:1], self.w, out=self.c1[:1])
+            torch.mv(self.Q[:1].T, self.c1[:1], out=self.tmp)
+            torch.linalg.vector_norm(self.w, out=self.h[0])
+        torch.cuda.synchronize(dev)
 
     def _record(self, j: int) -> None:
         op = self.op
