@@ -16,7 +16,8 @@ REPO_ROOT = PKG_ROOT.parent
 CSRC = PKG_ROOT / "csrc"
 INCLUDE = REPO_ROOT / "include"
 LIB_PATH = PKG_ROOT / "_build" / "libpbte_gb300.so"
-SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_capi.cu", "pbte_noalloc.cu"]
+SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_krylov.cu", "pbte_capi.cu",
+           "pbte_noalloc.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0
@@ -107,6 +108,7 @@ _SIGS = {
                              ctypes.c_int64, _vp], ctypes.c_int),
     "pbte_transport_residual": ([_vp] * 9 + [_vp], ctypes.c_int),
     "pbte_transport_residual_noalloc": ([_vp] * 8 + [_vp], ctypes.c_int),
+    "pbte_cgs2": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, _vp], ctypes.c_int),
     "pbte_hot_source": ([_vp, _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],

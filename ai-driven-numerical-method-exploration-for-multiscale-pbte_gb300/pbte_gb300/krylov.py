@@ -141,6 +141,9 @@ class ArnoldiGraphs:
         self.c1 = torch.zeros(m_cap + 1, **f64)
         self.c2 = torch.zeros(m_cap + 1, **f64)
         self.h = torch.zeros(m_cap + 2, **f64)
+        self.scratch = torch.zeros(610 * 64, **f64)   # pbte_cgs2 block partials
+        if m_cap + 1 > 64:
+            raise ValueError("graph-captured Arnoldi supports a basis of at most 63 vectors")
         self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
         self.g = g
         self.graphs = {}
@@ -167,14 +170,9 @@ class ArnoldiGraphs:
             torch.sub(qj, self.tmp, out=self.w)
         else:
             torch.sub(qj, op.uout[:n], out=self.w)
-        torch.mv(Qj, self.w, out=self.c1[:j + 1])
-        torch.mv(Qj.T, self.c1[:j + 1], out=self.tmp)
-        self.w.sub_(self.tmp)
-        torch.mv(Qj, self.w, out=self.c2[:j + 1])
-        torch.mv(Qj.T, self.c2[:j + 1], out=self.tmp)
-        self.w.sub_(self.tmp)
-        torch.add(self.c1[:j + 1], self.c2[:j + 1], out=self.h[:j + 1])
-        torch.linalg.vector_norm(self.w, out=self.h[j + 1])
+        _lib.check(_lib.lib().pbte_cgs2(Qj.data_ptr(), self.Q.stride(0), j + 1, self.w.data_ptr(), n,
+                                        self.h.data_ptr(), self.scratch.data_ptr(),
+                                        torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
 
     def column(self, j: int) -> np.ndarray:
         if j not in self.graphs:
@@ -389,7 +387,7 @@ def run_krylov(solver):
         return reached >= 0 and n - reached > max(64, reached // 4)
 
     x = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
-    ar = ArnoldiGraphs(op, g, cap) if cap <= 512 else None
+    ar = ArnoldiGraphs(op, g, cap) if cap <= 63 else None
     if ar is not None:
         def product():
             masses.append(np.nan)

@@ -77,7 +77,7 @@ def run_mixed(solver, opts: MixedOptions | None = None):
                     break
         else:
             cap = basis_cap(c, n)
-            if ar32 is None and cap <= 512:
+            if ar32 is None and cap <= 63:
                 ar32 = ArnoldiGraphs(op32, None, cap)
             before = op32.sweeps
             d, _, _ = gmres(lambda v: v - op32.apply(v), r, tol_abs=opts.inner_rtol * rn,

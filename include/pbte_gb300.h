@@ -172,6 +172,14 @@ int pbte_residual_check(pbte_ctx *ctx, const double *res, double tol, int64_t tm
                         int32_t *done, int64_t *count, double *hist, int64_t hist_cap,
                         void *stream);
 
+/* Classical Gram-Schmidt applied twice against the Krylov rows Q[0..rows-1]
+ * (row stride ldq doubles), FP64, in place on w, as in gmres_full
+ * (pybte/krylov.py:201-210): h[0..rows-1] = c1 + c2 and h[rows] = ||w||.
+ * Deterministic (block partial sums added in a fixed order).  `scratch`
+ * holds 610 * 64 doubles; rows <= 64. */
+int pbte_cgs2(const double *Q, int64_t ldq, int32_t rows, double *w, int64_t n, double *h,
+              double *scratch, void *stream);
+
 /* GSIS per-iteration kernels (pybte/acceleration/):
  * third-order moment source, hot_source.py:29-58 -> work[n_tris][7*ndof];
  * kinetic wall-trace moments, global_solve.py:31-53 -> out[nk][3*ndof_fc];

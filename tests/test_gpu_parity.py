@@ -201,3 +201,28 @@ def test_square_benchmark_mesh_levels(cuda):
     assert s.ctx.n_classes <= 16
     rec = s.run()
     assert rec.iterations == 3
+
+
+@pytest.mark.parametrize("rows", [1, 5, 30])
+def test_cgs2_matches_two_pass_gram_schmidt(cuda, rows):
+    """pbte_cgs2 against pybte's CGS2 step (pybte/krylov.py:201-210) in numpy."""
+    from pbte_gb300 import _lib
+    rng = np.random.default_rng(rows)
+    n = 100_003
+    Q, _ = np.linalg.qr(rng.standard_normal((n, rows)))
+    Q = np.ascontiguousarray(Q.T)
+    w = rng.standard_normal(n)
+    c1 = Q @ w
+    w1 = w - Q.T @ c1
+    c2 = Q @ w1
+    w2 = w1 - Q.T @ c2
+    Qd = torch.from_numpy(Q).cuda()
+    wd = torch.from_numpy(w).cuda()
+    h = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
+    scr = torch.zeros(610 * 64, dtype=torch.float64, device="cuda")
+    _lib.check(_lib.lib().pbte_cgs2(Qd.data_ptr(), n, rows, wd.data_ptr(), n, h.data_ptr(), scr.data_ptr(),
+                                    torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
+    hh = h.cpu().numpy()
+    assert np.allclose(hh[:rows], c1 + c2, rtol=1e-12, atol=1e-12)
+    assert hh[rows] == pytest.approx(np.linalg.norm(w2), rel=1e-12)
+    assert _rel(wd.cpu().numpy(), w2) < 1e-12
