@@ -85,7 +85,8 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_edofs, c->d_dir_class, c->d_class_lvl_off, c->d_class_nlev, c->d_lvl_ptr,
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
-                    c->d_udir_rep, c->d_udir_twin, c->d_srec64, c->d_srec32, c->d_mom_part};
+                    c->d_udir_rep, c->d_udir_twin, c->d_srec64, c->d_srec32, c->d_mom_part,
+                    c->d_cx32, c->d_cy32, c->d_w32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -173,6 +174,12 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     TRY(upload(d->cxv, (size_t)ndir, &c->d_cx, &c->device_bytes));
     TRY(upload(d->cyv, (size_t)ndir, &c->d_cy, &c->device_bytes));
     TRY(upload(d->domega, (size_t)ndir, &c->d_w, &c->device_bytes));
+    {
+        std::vector<float> a(d->cxv, d->cxv + ndir), b(d->cyv, d->cyv + ndir), w(d->domega, d->domega + ndir);
+        TRY(upload(a.data(), a.size(), &c->d_cx32, &c->device_bytes));
+        TRY(upload(b.data(), b.size(), &c->d_cy32, &c->device_bytes));
+        TRY(upload(w.data(), w.size(), &c->d_w32, &c->device_bytes));
+    }
     TRY(upload(d->int_tri, (size_t)nd * nt, &c->d_int_tri, &c->device_bytes));
 
     // ---- adiabatic wall faces -------------------------------------------

@@ -94,6 +94,7 @@ struct pbte_ctx {
     pbte::SweepRec<float> *d_srec32 = nullptr;
     int far_max = 0;
     double *d_mom_part = nullptr;   // [ceil(ndir/32)][3][n_tris*ndof] moment partial sums
+    float *d_cx32 = nullptr, *d_cy32 = nullptr, *d_w32 = nullptr;   // ordinates in FP32
 };
 
 // launchers (pbte_kernels.cu)

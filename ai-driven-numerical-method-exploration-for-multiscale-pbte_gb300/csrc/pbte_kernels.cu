@@ -196,6 +196,7 @@ constexpr int kMomChunk = 32;
 
 template <typename T>
 __global__ void moments_partial_kernel(const T *vdf, const double *cx, const double *cy, const double *w,
+                                       const float *cx32, const float *cy32, const float *w32,
                                        int ndir, int total, double *part, const int32_t *done) {
     if (stopped(done)) return;
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -214,10 +215,10 @@ __global__ void moments_partial_kernel(const T *vdf, const double *cx, const dou
     } else {
         float a = 0.f, bx = 0.f, by = 0.f;
         for (int d = d0; d < d1; ++d) {
-            const float fw = (float)vdf[(size_t)d * total + t] * (float)w[d];
+            const float fw = (float)vdf[(size_t)d * total + t] * w32[d];
             a += fw;
-            bx += (float)cx[d] * fw;
-            by += (float)cy[d] * fw;
+            bx += cx32[d] * fw;
+            by += cy32[d] * fw;
         }
         s0 = a; sx = bx; sy = by;
     }
@@ -624,9 +625,8 @@ static int moments_impl(pbte_ctx *c, const T *vdf, double *ts, double *qxs, doub
     const int total = c->n_tris * c->nd, th = 256;
     const int nch = (c->ndir + kMomChunk - 1) / kMomChunk;
     if (c->d_mom_part) {
-        moments_partial_kernel<T><<<dim3((total + th - 1) / th, nch), th, 0, s>>>(vdf, c->d_cx, c->d_cy, c->d_w,
-                                                                                  c->ndir, total, c->d_mom_part,
-                                                                                  c->done);
+        moments_partial_kernel<T><<<dim3((total + th - 1) / th, nch), th, 0, s>>>(
+            vdf, c->d_cx, c->d_cy, c->d_w, c->d_cx32, c->d_cy32, c->d_w32, c->ndir, total, c->d_mom_part, c->done);
         moments_combine_kernel<<<(total + th - 1) / th, th, 0, s>>>(c->d_mom_part, nch, c->n_tris, c->nd, c->cv, ts,
                                                                    qxs, qys, c->done);
     } else {

@@ -81,7 +81,9 @@ class SweepContext:
         mode = c.performance.sweep_mode
         if precompute is None:
             if mode == "auto":
-                precompute = (c.performance.precompute_inverse and c.performance.precision == "fp64"
+                # stored FP64 factors serve every FP64 sweep (the mixed path's
+                # defect evaluations too); FP32 sweeps always factor in registers
+                precompute = (c.performance.precompute_inverse
                               and self.operator_bytes(self.n_tris, self.ndof) <= c.performance.max_operator_bytes)
             else:
                 precompute = mode == "precomputed"
