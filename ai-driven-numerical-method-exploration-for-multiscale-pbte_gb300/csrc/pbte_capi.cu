@@ -38,13 +38,15 @@ int pbte_sweep_f32(pbte_ctx *c, const double *ts, const double *qxs, const doubl
 
 int pbte_moments(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys, double *temp,
                  double *qx, double *qy, void *stream) {
-    if (!c || !vdf || !ts || !qxs || !qys || !temp || !qx || !qy) return PBTE_ERR_ARG;
+    if (!c || !vdf || !ts || !qxs || !qys) return PBTE_ERR_ARG;
+    if ((temp == nullptr) != (qx == nullptr) || (temp == nullptr) != (qy == nullptr)) return PBTE_ERR_ARG;
     return pbte::launch_moments64(c, vdf, ts, qxs, qys, temp, qx, qy, S(stream));
 }
 
 int pbte_moments_f32(pbte_ctx *c, const float *vdf32, double *ts, double *qxs, double *qys, double *temp,
                      double *qx, double *qy, void *stream) {
-    if (!c || !vdf32 || !ts || !qxs || !qys || !temp || !qx || !qy) return PBTE_ERR_ARG;
+    if (!c || !vdf32 || !ts || !qxs || !qys) return PBTE_ERR_ARG;
+    if ((temp == nullptr) != (qx == nullptr) || (temp == nullptr) != (qy == nullptr)) return PBTE_ERR_ARG;
     return pbte::launch_moments32(c, vdf32, ts, qxs, qys, temp, qx, qy, S(stream));
 }
 

@@ -265,6 +265,23 @@ __global__ void element_integrals_kernel(const double *ts, const double *qxs, co
     qy[i] = by;
 }
 
+// Block sum of the per-thread partial emissions (fixed tree) and the result
+// -sum(u w f.fcm) / -sum(u w) of pybte/_kernels.py:385-397.
+__device__ __forceinline__ void wall_flux_reduce(double *red, const double *acc, double s2, int NP, double *out) {
+    for (int m = 0; m < NP; ++m) red[threadIdx.x * (NP + 1) + m] = acc[m];
+    red[threadIdx.x * (NP + 1) + NP] = s2;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int m = 0; m <= NP; ++m) red[threadIdx.x * (NP + 1) + m] += red[(threadIdx.x + h) * (NP + 1) + m];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double ss2 = red[NP];
+        for (int m = 0; m < NP; ++m) out[m] = -red[m] / ss2;
+    }
+}
+
 // Adiabatic-wall emission: one block per wall face, ordinates over threads.
 template <typename T>
 __global__ void wall_flux_kernel(const T *vdf, const WallFace *walls, const CellRec<double> *cells,
@@ -292,19 +309,46 @@ __global__ void wall_flux_kernel(const T *vdf, const WallFace *walls, const Cell
             s2 -= u * w[d];
         }
     }
-    for (int m = 0; m < NP; ++m) red[threadIdx.x * (NP + 1) + m] = acc[m];
-    red[threadIdx.x * (NP + 1) + NP] = s2;
-    __syncthreads();
-    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
-        if ((int)threadIdx.x < h)
-            for (int m = 0; m <= NP; ++m) red[threadIdx.x * (NP + 1) + m] += red[(threadIdx.x + h) * (NP + 1) + m];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        const double ss2 = red[NP];
-        for (int m = 0; m < NP; ++m) fw_out[(size_t)wf.face * NP + m] = -red[m] / ss2;
-    }
+    wall_flux_reduce(red, acc, s2, NP, fw_out + (size_t)wf.face * NP);
 }
+
+// The same with N_p known at compile time (registers, no local arrays) and
+// the products in the distribution's precision; the sums stay FP64.
+template <typename T, int NP>
+__global__ void wall_flux_np_kernel(const T *vdf, const WallFace *walls, const CellRec<double> *cells,
+                                    const T *ref_edge, const double *cx, const double *cy, const double *w,
+                                    int ndir, int nt, double *fw_out, const int32_t *done) {
+    if (stopped(done)) return;
+    extern __shared__ double red[];  // [blockDim][NP+1]
+    const WallFace wf = walls[blockIdx.x];
+    const T es = (T)cells[wf.tri].es[wf.lfc];
+    const T *R = ref_edge + (size_t)wf.lfc * NP * NP;
+    double acc[16];
+#pragma unroll
+    for (int m = 0; m < NP; ++m) acc[m] = 0.0;
+    double s2 = 0.0;
+    for (int d = threadIdx.x; d < ndir; d += blockDim.x) {
+        const double u = cx[d] * wf.nx + cy[d] * wf.ny;
+        if (u < 0.0) {
+            const T *f = vdf + ((size_t)d * nt + wf.tri) * NP;
+            T fl[NP];
+#pragma unroll
+            for (int l = 0; l < NP; ++l) fl[l] = f[l];
+            const double uw = u * w[d];
+#pragma unroll
+            for (int m = 0; m < NP; ++m) {
+                T a = T(0);
+#pragma unroll
+                for (int l = 0; l < NP; ++l) a += fl[l] * (es * R[m * NP + l]);
+                acc[m] += uw * (double)a;
+            }
+        } else {
+            s2 -= u * w[d];
+        }
+    }
+    wall_flux_reduce(red, acc, s2, NP, fw_out + (size_t)wf.face * NP);
+}
+
 
 // Step residual and mass; out[0] = residual, out[1] = sum(temp); t_old <- temp.
 __global__ void residual_kernel(const double *temp, double *t_old, int n, double *out, const int32_t *done) {
@@ -556,9 +600,44 @@ static SweepParams<T> make_params(pbte_ctx *c) {
     return P;
 }
 
+// Moment sources with N_p at compile time, one thread per (element, moment).
+template <typename T, int NP>
+__global__ void sources_np_kernel(const CellRec<double> *cells, const double *ref_mass, const double *ts,
+                                  const double *qxs, const double *qys, T *S, int nt, const int32_t *done) {
+    if (stopped(done)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= 3 * nt) return;
+    const int i = t % nt, q = t / nt;
+    const double *mom = q == 0 ? ts : (q == 1 ? qxs : qys);
+    double v[NP];
+#pragma unroll
+    for (int l = 0; l < NP; ++l) v[l] = mom[(size_t)l * nt + i];
+    const double a2 = cells[i].area2;
+    T *o = S + ((size_t)i * 3 + q) * NP;
+#pragma unroll
+    for (int m = 0; m < NP; ++m) {
+        double acc = 0.0;
+#pragma unroll
+        for (int l = 0; l < NP; ++l) acc += ref_mass[l * NP + m] * v[l];
+        o[m] = (T)(a2 * acc);
+    }
+}
+
 int launch_sources(pbte_ctx *c, const double *ts, const double *qxs, const double *qys, bool f32,
                    cudaStream_t s) {
     const int th = 128, bl = (c->n_tris + th - 1) / th;
+    const int bl3 = (3 * c->n_tris + th - 1) / th;
+    auto go = [&](auto k32, auto k64) {
+        if (f32) k32<<<bl3, th, 0, s>>>(c->d_cells64, c->d_ref64, ts, qxs, qys, c->d_S32, c->n_tris, c->done);
+        else k64<<<bl3, th, 0, s>>>(c->d_cells64, c->d_ref64, ts, qxs, qys, c->d_S64, c->n_tris, c->done);
+        return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+    };
+    switch (c->nd) {
+        case 3: return go(sources_np_kernel<float, 3>, sources_np_kernel<double, 3>);
+        case 6: return go(sources_np_kernel<float, 6>, sources_np_kernel<double, 6>);
+        case 10: return go(sources_np_kernel<float, 10>, sources_np_kernel<double, 10>);
+        default: break;
+    }
     if (f32)
         sources_kernel<float><<<bl, th, 0, s>>>(c->d_cells64, c->d_ref64, ts, qxs, qys, c->d_S32, c->n_tris, c->nd, c->done);
     else
@@ -633,8 +712,9 @@ static int moments_impl(pbte_ctx *c, const T *vdf, double *ts, double *qxs, doub
         moments_kernel<T><<<(total + th - 1) / th, th, 0, s>>>(vdf, c->d_cx, c->d_cy, c->d_w, c->ndir, c->n_tris,
                                                               c->nd, c->cv, ts, qxs, qys, c->done);
     }
-    element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts, qxs, qys, c->d_int_tri, c->n_tris,
-                                                                     c->nd, c->cv, temp, qx, qy, c->done);
+    if (temp)
+        element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts, qxs, qys, c->d_int_tri, c->n_tris,
+                                                                         c->nd, c->cv, temp, qx, qy, c->done);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
@@ -653,9 +733,22 @@ static int wall_flux_impl(pbte_ctx *c, const T *vdf, double *fw, cudaStream_t s)
     if (c->n_wall_ad == 0) return PBTE_OK;
     const int th = 64;
     const size_t shm = (size_t)th * (c->nd + 1) * sizeof(double);
-    wall_flux_kernel<T><<<c->n_wall_ad, th, shm, s>>>(vdf, c->d_wall_ad, c->d_cells64, c->d_ref64 + 3 * c->nd * c->nd,
-                                                      c->d_cx, c->d_cy, c->d_w, c->ndir, c->n_tris, c->nd, fw,
-                                                      c->done);
+    const T *ref_edge = nullptr;
+    if constexpr (sizeof(T) == 8) ref_edge = c->d_ref64 + 3 * c->nd * c->nd;
+    else ref_edge = c->d_ref32 + 3 * c->nd * c->nd;
+    auto go = [&](auto kern) {
+        kern<<<c->n_wall_ad, th, shm, s>>>(vdf, c->d_wall_ad, c->d_cells64, ref_edge, c->d_cx, c->d_cy, c->d_w,
+                                           c->ndir, c->n_tris, fw, c->done);
+    };
+    switch (c->nd) {
+        case 3: go(wall_flux_np_kernel<T, 3>); break;
+        case 6: go(wall_flux_np_kernel<T, 6>); break;
+        case 10: go(wall_flux_np_kernel<T, 10>); break;
+        default:
+            wall_flux_kernel<T><<<c->n_wall_ad, th, shm, s>>>(vdf, c->d_wall_ad, c->d_cells64,
+                                                              c->d_ref64 + 3 * c->nd * c->nd, c->d_cx, c->d_cy,
+                                                              c->d_w, c->ndir, c->n_tris, c->nd, fw, c->done);
+    }
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 

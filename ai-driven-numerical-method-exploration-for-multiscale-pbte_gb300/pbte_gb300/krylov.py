@@ -34,8 +34,9 @@ class FixedPointOperator:
     emission, gather (``pybte/krylov.py:64-136``).  Periodic faces are not
     supported by the GPU sweep's source-iteration form and are refused."""
 
-    def __init__(self, solver, precision: str = "fp64", homogeneous: bool = False):
+    def __init__(self, solver, precision: str = "fp64", homogeneous: bool = False, integrals: bool = True):
         s = solver
+        self.integrals = integrals
         if s.bcdata.has_periodic:
             raise NotImplementedError("periodic faces: the Krylov state needs the partner DOFs")
         self.s = s
@@ -79,9 +80,10 @@ class FixedPointOperator:
         else:
             _lib.check(L.pbte_sweep_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), self.vdf.data_ptr(),
                                         fw.data_ptr(), 0.0 if self.homogeneous else 1.0, s), "sweep_f32")
+            ints = (self.temp.data_ptr(), self.qx.data_ptr(), self.qy.data_ptr()) if self.integrals \
+                else (None, None, None)
             _lib.check(L.pbte_moments_f32(ctx, self.vdf.data_ptr(), ots.data_ptr(), oqxs.data_ptr(),
-                                          oqys.data_ptr(), self.temp.data_ptr(), self.qx.data_ptr(),
-                                          self.qy.data_ptr(), s), "moments_f32")
+                                          oqys.data_ptr(), *ints, s), "moments_f32")
             if self.wall:
                 _lib.check(L.pbte_wall_flux_f32(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux_f32")
 

@@ -47,7 +47,7 @@ def run_mixed(solver, opts: MixedOptions | None = None):
         raise NotImplementedError("mixed precision GSIS is not implemented; use precision='fp64'")
     method = "krylov" if c.scheme.method == "krylov" else "source"
     op64 = FixedPointOperator(solver, "fp64")
-    op32 = FixedPointOperator(solver, "fp32", homogeneous=True)
+    op32 = FixedPointOperator(solver, "fp32", homogeneous=True, integrals=False)
     n = op64.n
     dev = solver.device
     u = torch.zeros(n, dtype=torch.float64, device=dev)

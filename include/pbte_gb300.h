@@ -115,7 +115,10 @@ int pbte_sweep_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const dou
                    float *vdf32, const double *flux_wall, double wall_scale, void *stream);
 
 /* Angular moments and element integrals.  Replaces compute_moments
- * (pybte/moments.py:51-55 -> _kernels.moments_kernel, _kernels.py:312-338). */
+ * (pybte/moments.py:51-55 -> _kernels.moments_kernel, _kernels.py:312-338).
+ * temp, qx, qy may all be NULL to skip the element integrals.  The partial
+ * sums go to scratch in the context: calls on one context must not overlap
+ * on the GPU. */
 int pbte_moments(pbte_ctx *ctx, const double *vdf, double *ts, double *qxs, double *qys,
                  double *temp, double *qx, double *qy, void *stream);
 /* The same from an FP32 distribution, accumulated in FP32 per direction
