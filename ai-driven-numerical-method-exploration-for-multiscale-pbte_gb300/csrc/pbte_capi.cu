@@ -77,6 +77,12 @@ int pbte_set_ring_groups(pbte_ctx *c, int groups) {
     return PBTE_OK;
 }
 
+int pbte_set_ring_width(pbte_ctx *c, int threads_per_group) {
+    if (!c || (threads_per_group != 0 && threads_per_group != 64 && threads_per_group != 128)) return PBTE_ERR_ARG;
+    c->ring_width = threads_per_group;
+    return PBTE_OK;
+}
+
 int pbte_ctx_schedule(const pbte_ctx *c, int64_t *ring_w, int64_t *ring_r, int64_t *n_unique_dirs) {
     if (!c) return PBTE_ERR_ARG;
     if (ring_w) *ring_w = c->ring_W;

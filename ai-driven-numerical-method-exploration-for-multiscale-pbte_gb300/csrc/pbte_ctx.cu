@@ -310,7 +310,12 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
             s32.c = r32[i];
             s64.cell = s32.cell = i;
             s64.far_out = s32.far_out = far_idx[i];
-            for (int il = 0; il < 3; ++il) s64.up[il] = s32.up[il] = up_slot[((size_t)k * nt + p) * 3 + il];
+            for (int il = 0; il < 3; ++il) {
+                s64.up[il] = s32.up[il] = up_slot[((size_t)k * nt + p) * 3 + il];
+                uint32_t packed = 0;
+                for (int b = 0; b < nf; ++b) packed |= (uint32_t)(r64[i].emap[il][b] & 15) << (4 * b);
+                s64.emp[il] = s32.emp[il] = packed;
+            }
         }
         c->nlev_max = std::max(c->nlev_max, nlev);
         c->ring_W = std::max(c->ring_W, W);

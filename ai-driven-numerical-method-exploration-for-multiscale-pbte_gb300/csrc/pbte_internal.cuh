@@ -35,12 +35,14 @@ struct alignas(16) CellRec {
 // up[il]: -1 no in-sweep inflow; >= 0 slot of the near ring
 // ((level % R) * W + position); <= -2 far slot -(up + 2).
 // far_out: far slot this element's values must also be kept in, or -1.
+// emp[il]: c.emap[il][0..nf-1] packed four bits each (nd <= 15), so the
+// inflow gather needs one register per edge.
 template <typename T>
 struct alignas(16) SweepRec {
     CellRec<T> c;
     int32_t cell, far_out;
     int32_t up[3];
-    int32_t pad[3];
+    uint32_t emp[3];
 };
 
 struct WallFace {
@@ -89,6 +91,7 @@ struct pbte_ctx {
     int n_udir = 0;
     int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
     int ring_groups = 0;            // thread groups of the ring pipeline (0: default)
+    int ring_width = 0;             // threads per group of the ring pipeline (0: 64)
     // per-class records in sweep order ([nclass][n_tris]) and far-slot count
     pbte::SweepRec<double> *d_srec64 = nullptr;
     pbte::SweepRec<float> *d_srec32 = nullptr;

@@ -7,27 +7,33 @@
 // depend on the upwind values -- read the element records (stored in the
 // direction class's sweep order, so a level is one contiguous run), form the
 // source and wall terms, assemble and LU-factor the element operators in
-// registers (or load the stored FP64 factors), and fetch the records of its
-// next level -- and only then waits for level L-1 (bar.sync on the barrier
-// the previous group arrives at).  It then adds the upwind inflow from shared
-// memory, finishes the two triangular solves, stores the result in shared
-// memory, arrives on its own barrier for level L+1, and only after that
-// writes the distribution to global memory.  The critical path per level is
-// the inflow gather plus two small triangular solves; the factorisation of
+// registers (or load the stored FP64 factors), and prefetch the records of
+// its next level into L1 -- and only then waits for level L-1 (bar.sync on
+// the barrier the previous group arrives at).  It then adds the upwind inflow
+// from shared memory, finishes the two triangular solves, stores the result
+// in shared memory, arrives on its own barrier for level L+1, and only after
+// that writes the distribution to global memory.  The critical path per level
+// is the inflow gather plus two small triangular solves; the factorisation of
 // the next levels overlaps it on the other groups.
+//
+// Registers bound the number of groups an SM can hold, so the records are not
+// copied into registers: fields are read from L1 where they are used, and
+// only what the post-barrier part needs (upwind slot codes, packed edge maps,
+// far slot, edge factors) is carried across the barrier.
 //
 // Upwind values live in a near ring of the last R <= 4 levels (slot
 // (level % R) * W + position) and, for the few dependencies that reach
 // further back, in dedicated far slots; both are laid out on the host
-// (pbte_ctx.cu) and referenced from the records.
+// (pbte_ctx.cu) and referenced from the records.  The ring is safe for any G:
+// level L+R overwrites level L's slot only after the barrier chain has
+// passed L+R-1, and every level reads its inflow before it arrives.
 #include <algorithm>
 
 #include "pbte_device.cuh"
 
 namespace pbte {
 
-constexpr int kTPG = 64;        // threads per group
-constexpr int kMaxGroups = 4;
+constexpr int kMaxGroups = 8;
 
 struct RingParams {
     const void *recs;           // SweepRec<T>[nclass * n_tris] in sweep order
@@ -39,17 +45,19 @@ struct RingParams {
 
 __device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 __device__ __forceinline__ void bar_arrive(int id, int n) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory"); }
+__device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
 
-template <typename T, int DEG, bool PRECOMP, int CPT>
-__global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepParams<T> P, RingParams Q) {
+// TPG: threads per group; GMAX: the most groups the kernel is compiled for
+// (its launch bound)
+template <typename T, int DEG, bool PRECOMP, int CPT, int TPG, int GMAX>
+__global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P, RingParams Q) {
     constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
-    constexpr bool PF = (CPT == 1) && (sizeof(T) == 4);   // register prefetch of the next level's record
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sref = reinterpret_cast<T *>(smem_raw);
     T *ring = sref + 6 * NP * NP;
     T *far = ring + Q.far_offset;
     if (stopped(P.done)) return;
-    const SweepRec<T> *recs = reinterpret_cast<const SweepRec<T> *>(Q.recs);
+    const SweepRec<T> *__restrict__ recs = reinterpret_cast<const SweepRec<T> *>(Q.recs);
     const int u = blockIdx.x;
     const int d = Q.udir_rep[u], d2 = Q.udir_twin[u];
     for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
@@ -59,60 +67,94 @@ __global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepPara
     const int off = P.class_off[cls], nlev = P.class_nlev[cls];
     const int W = Q.class_W[cls], Rr = Q.class_R[cls];
     const int G = Q.groups;
-    const int g = threadIdx.x / kTPG, t = threadIdx.x % kTPG;
+    const int g = threadIdx.x / TPG, t = threadIdx.x % TPG;
     T *f1 = P.vdf + (size_t)d * P.nt * NP;
     T *f2 = d2 >= 0 ? P.vdf + (size_t)d2 * P.nt * NP : nullptr;
     int sing = 0;
-    SweepRec<T> nxt;
-    if constexpr (PF) {
-        if (g < nlev) {
-            const int k = P.lvl_ptr[off + g] + t;
-            if (k < P.lvl_ptr[off + g + 1]) nxt = recs[k];
-        }
-    }
+    int beg = g < nlev ? P.lvl_ptr[off + g] : 0;
+    int end = g < nlev ? P.lvl_ptr[off + g + 1] : 0;
     for (int L = g; L < nlev; L += G) {
-        const int beg = P.lvl_ptr[off + L], end = P.lvl_ptr[off + L + 1];
-        SweepRec<T> cur[CPT];
+        // the next level of this group: bounds now, records into L1
+        const int Ln = L + G;
+        const int nbeg = Ln < nlev ? P.lvl_ptr[off + Ln] : 0;
+        const int nend = Ln < nlev ? P.lvl_ptr[off + Ln + 1] : 0;
+#pragma unroll
+        for (int c = 0; c < CPT; ++c) {
+            const int k = nbeg + t + c * TPG;
+            if (k < nend) {
+                const char *p = reinterpret_cast<const char *>(recs + k);
+                prefetch_l1(p);
+                prefetch_l1(p + 128);
+                prefetch_l1(p + sizeof(SweepRec<T>) - 1);
+            }
+        }
+        const SweepRec<T> *rc[CPT];
         bool valid[CPT];
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
-            const int k = beg + t + c * kTPG;
+            const int k = beg + t + c * TPG;
             valid[c] = k < end;
-            if (valid[c]) {
-                if constexpr (PF) cur[c] = nxt;
-                else cur[c] = recs[k];
-            }
-        }
-        T Sv[CPT][3 * NP];
-#pragma unroll
-        for (int c = 0; c < CPT; ++c)
-            if (valid[c]) {
-                const T *S = P.S + (size_t)cur[c].cell * 3 * NP;
-#pragma unroll
-                for (int q = 0; q < 3 * NP; ++q) Sv[c][q] = S[q];
-            }
-        if constexpr (PF) {
-            const int Ln = L + G;
-            if (Ln < nlev) {
-                const int k = P.lvl_ptr[off + Ln] + t;
-                if (k < P.lvl_ptr[off + Ln + 1]) nxt = recs[k];
-            }
+            rc[c] = recs + (valid[c] ? k : beg);
         }
         T A[CPT][NP][NP];
         T b[CPT][NP];
         int piv[CPT][NP];
         T scin[CPT][3];
+        int code[CPT][3];
+        uint32_t emp[CPT][3];
+        int fo[CPT];
         // ---- independent of the upwind values ------------------------------
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
-            const CellRec<T> &r = cur[c].c;
-            const int i = cur[c].cell;
+            const CellRec<T> &r = rc[c]->c;
+            const int i = rc[c]->cell;
+            {
+                // the source first, so its values are dead before the factorisation
+                const T *S = P.S + (size_t)i * 3 * NP;
+#pragma unroll
+                for (int m = 0; m < NP; ++m) b[c][m] = P.ca * S[m] + P.cb * (cx * S[NP + m] + cy * S[2 * NP + m]);
+            }
             T s[3];
 #pragma unroll
             for (int il = 0; il < 3; ++il) {
                 s[il] = cx * r.nx[il] + cy * r.ny[il];
                 scin[c][il] = s[il] * r.es[il];
+                code[c][il] = rc[c]->up[il];
+                emp[c][il] = rc[c]->emp[il];
+            }
+            fo[c] = rc[c]->far_out;
+#pragma unroll
+            for (int il = 0; il < 3; ++il) {
+                if (!(s[il] < T(0))) continue;
+                const T *R = sref + (3 + il) * NP * NP;
+                const int kind = r.kind[il];
+                if (kind == 3) {
+                    const double *pb = P.pbuf + ((size_t)d * P.n_faces + r.face[il]) * NP;
+#pragma unroll
+                    for (int a = 0; a < NF; ++a) {
+                        const int ma = Shape<DEG>::edof(il, a);
+                        T acc = T(0);
+#pragma unroll
+                        for (int bb = 0; bb < NF; ++bb)
+                            acc += R[ma * NP + Shape<DEG>::edof(il, bb)] * (T)pb[(emp[c][il] >> (4 * bb)) & 15u];
+                        b[c][ma] -= scin[c][il] * acc;
+                    }
+                } else if (kind == 1) {
+                    const T sc = s[il] * r.bval[il] * P.wall_scale * r.es[il];
+#pragma unroll
+                    for (int a = 0; a < NF; ++a) {
+                        const int ma = Shape<DEG>::edof(il, a);
+                        T rs = T(0);
+#pragma unroll
+                        for (int bb = 0; bb < NF; ++bb) rs += R[ma * NP + Shape<DEG>::edof(il, bb)];
+                        b[c][ma] -= sc * rs;
+                    }
+                } else if (kind == 2) {
+                    const double *fw = P.flux_wall + (size_t)r.face[il] * NP;
+#pragma unroll
+                    for (int m = 0; m < NP; ++m) b[c][m] -= s[il] * (-(T)fw[m]);
+                }
             }
             if constexpr (PRECOMP) {
                 const double *lu = P.lu + ((size_t)d * P.nt + i) * NP * NP;
@@ -172,56 +214,22 @@ __global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepPara
                     A[c][kk][kk] = rr;
                 }
             }
-#pragma unroll
-            for (int m = 0; m < NP; ++m) b[c][m] = P.ca * Sv[c][m] + P.cb * (cx * Sv[c][NP + m] + cy * Sv[c][2 * NP + m]);
-#pragma unroll
-            for (int il = 0; il < 3; ++il) {
-                if (!(s[il] < T(0))) continue;
-                const T *R = sref + (3 + il) * NP * NP;
-                const int kind = r.kind[il];
-                if (kind == 3) {
-                    const double *pb = P.pbuf + ((size_t)d * P.n_faces + r.face[il]) * NP;
-#pragma unroll
-                    for (int a = 0; a < NF; ++a) {
-                        const int ma = Shape<DEG>::edof(il, a);
-                        T acc = T(0);
-#pragma unroll
-                        for (int bb = 0; bb < NF; ++bb) acc += R[ma * NP + Shape<DEG>::edof(il, bb)] * (T)pb[r.emap[il][bb]];
-                        b[c][ma] -= scin[c][il] * acc;
-                    }
-                } else if (kind == 1) {
-                    const T sc = s[il] * r.bval[il] * P.wall_scale * r.es[il];
-#pragma unroll
-                    for (int a = 0; a < NF; ++a) {
-                        const int ma = Shape<DEG>::edof(il, a);
-                        T rs = T(0);
-#pragma unroll
-                        for (int bb = 0; bb < NF; ++bb) rs += R[ma * NP + Shape<DEG>::edof(il, bb)];
-                        b[c][ma] -= sc * rs;
-                    }
-                } else if (kind == 2) {
-                    const double *fw = P.flux_wall + (size_t)r.face[il] * NP;
-#pragma unroll
-                    for (int m = 0; m < NP; ++m) b[c][m] -= s[il] * (-(T)fw[m]);
-                }
-            }
         }
         // ---- wait for level L-1, then the upwind inflow and the solves ------
-        if (G > 1 && L > 0) bar_sync(1 + (L - 1) % G, 2 * kTPG);
+        if (G > 1 && L > 0) bar_sync(1 + (L - 1) % G, 2 * TPG);
         const int rbase = (L % Rr) * W;
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
-            const CellRec<T> &r = cur[c].c;
 #pragma unroll
             for (int il = 0; il < 3; ++il) {
-                const int code = cur[c].up[il];
-                if (code == -1) continue;
-                const T *up = code >= 0 ? ring + (size_t)code * NP : far + (size_t)(-code - 2) * NP;
+                const int cd = code[c][il];
+                if (cd == -1) continue;
+                const T *up = cd >= 0 ? ring + (size_t)cd * NP : far + (size_t)(-cd - 2) * NP;
                 const T *R = sref + (3 + il) * NP * NP;
                 T gv[NF];
 #pragma unroll
-                for (int bb = 0; bb < NF; ++bb) gv[bb] = up[r.emap[il][bb]];
+                for (int bb = 0; bb < NF; ++bb) gv[bb] = up[(emp[c][il] >> (4 * bb)) & 15u];
 #pragma unroll
                 for (int a = 0; a < NF; ++a) {
                     const int ma = Shape<DEG>::edof(il, a);
@@ -250,17 +258,17 @@ __global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepPara
 #pragma unroll
                 for (int j = 0; j < kk; ++j) b[c][j] -= b[c][kk] * A[c][j][kk];
             }
-            T *rs = ring + (size_t)(rbase + t + c * kTPG) * NP;
+            T *rs = ring + (size_t)(rbase + t + c * TPG) * NP;
 #pragma unroll
             for (int m = 0; m < NP; ++m) rs[m] = b[c][m];
-            if (cur[c].far_out >= 0) {
-                T *fs = far + (size_t)cur[c].far_out * NP;
+            if (fo[c] >= 0) {
+                T *fs = far + (size_t)fo[c] * NP;
 #pragma unroll
                 for (int m = 0; m < NP; ++m) fs[m] = b[c][m];
             }
         }
         if (G > 1) {
-            if (L + 1 < nlev) bar_arrive(1 + L % G, 2 * kTPG);
+            if (L + 1 < nlev) bar_arrive(1 + L % G, 2 * TPG);
         } else {
             __syncthreads();
         }
@@ -269,23 +277,26 @@ __global__ void __launch_bounds__(kMaxGroups * kTPG) sweep_ring_kernel(SweepPara
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
-            T *o1 = f1 + (size_t)cur[c].cell * NP;
+            const int i = rc[c]->cell;
+            T *o1 = f1 + (size_t)i * NP;
 #pragma unroll
             for (int m = 0; m < NP; ++m) o1[m] = b[c][m];
             if (f2) {
-                T *o2 = f2 + (size_t)cur[c].cell * NP;
+                T *o2 = f2 + (size_t)i * NP;
 #pragma unroll
                 for (int m = 0; m < NP; ++m) o2[m] = b[c][m];
             }
         }
+        beg = nbeg;
+        end = nend;
     }
     if (sing) atomicAdd(P.singular, sing);
 }
 
-template <typename T, int DEG, bool PRE>
-static int ring_launch_deg(pbte_ctx *c, const SweepParams<T> &P, const RingParams &Q, int cpt, size_t shm,
+template <typename T, int DEG, bool PRE, int TPG, int GMAX>
+static int ring_launch_cpt(pbte_ctx *c, const SweepParams<T> &P, const RingParams &Q, int cpt, size_t shm,
                            cudaStream_t s) {
-    const int threads = Q.groups * kTPG;
+    const int threads = Q.groups * TPG;
     auto go = [&](auto kern) {
         if (shm > 48 * 1024 &&
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
@@ -294,34 +305,62 @@ static int ring_launch_deg(pbte_ctx *c, const SweepParams<T> &P, const RingParam
         return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
     };
     switch (cpt) {
-        case 1: return go(sweep_ring_kernel<T, DEG, PRE, 1>);
-        case 2: return go(sweep_ring_kernel<T, DEG, PRE, 2>);
+        case 1: return go(sweep_ring_kernel<T, DEG, PRE, 1, TPG, GMAX>);
+        case 2:
+            if constexpr (DEG <= 2 && TPG == 64) return go(sweep_ring_kernel<T, DEG, PRE, 2, TPG, GMAX>);
+            return PBTE_ERR_UNSUPPORTED;
         case 4:
-            if constexpr (sizeof(T) == 4 && DEG <= 2) return go(sweep_ring_kernel<T, DEG, PRE, 4>);
+            if constexpr (sizeof(T) == 4 && DEG <= 2 && TPG == 64 && GMAX <= 4)
+                return go(sweep_ring_kernel<T, DEG, PRE, 4, TPG, GMAX>);
             return PBTE_ERR_UNSUPPORTED;
         default: return PBTE_ERR_UNSUPPORTED;
     }
 }
 
 // Returns PBTE_ERR_UNSUPPORTED when the ring form does not fit (the caller
-// then uses the level-serial kernel).
+// then uses the level-serial kernel).  Block shapes compiled: groups of 64
+// with up to four groups (1, 2 or 4 elements per thread); for DEG <= 2 also
+// up to eight groups of 64 (1 or 2 elements per thread) and up to four groups
+// of 128 (1 element per thread), the 512-thread shapes whose operators fit
+// the 128 registers such a block allows.  A requested shape that is not
+// compiled for the mesh falls back to four groups of 64.
 template <typename T, bool PRE>
 int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     if (c->deg > 3 || c->ring_W <= 0) return PBTE_ERR_UNSUPPORTED;
-    int cpt = (c->ring_W + kTPG - 1) / kTPG;
-    if (cpt == 3) cpt = 4;
+    auto cpt_for = [&](int width) {
+        const int k = (c->ring_W + width - 1) / width;
+        return k == 3 ? 4 : k;
+    };
+    int width = c->ring_width == 128 ? 128 : 64;
+    int groups = c->ring_groups > 0 ? std::min(c->ring_groups, kMaxGroups) : 4;
+    if (width == 128 && (cpt_for(128) > 1 || c->deg > 2 || groups > 4)) width = 64;
+    const int cpt = cpt_for(width);
+    if (groups > 4 && (cpt > 2 || c->deg > 2)) groups = 4;
     if (cpt > 4 || (cpt == 4 && (sizeof(T) != 4 || c->deg > 2)) || (c->deg == 3 && cpt > 1))
         return PBTE_ERR_UNSUPPORTED;
     const size_t ring_vals = (size_t)c->ring_R * c->ring_W * c->nd;
     const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + ring_vals + (size_t)c->far_max * c->nd);
     if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
-    const int groups = c->ring_groups > 0 ? std::min(c->ring_groups, kMaxGroups) : kMaxGroups;
     const void *recs = sizeof(T) == 4 ? (const void *)c->d_srec32 : (const void *)c->d_srec64;
     RingParams Q{recs, c->d_class_W, c->d_class_R, c->d_udir_rep, c->d_udir_twin, groups, (int)ring_vals};
+    if (width == 128) {
+        switch (c->deg) {
+            case 1: return ring_launch_cpt<T, 1, PRE, 128, 4>(c, P, Q, cpt, shm, s);
+            case 2: return ring_launch_cpt<T, 2, PRE, 128, 4>(c, P, Q, cpt, shm, s);
+            default: return PBTE_ERR_UNSUPPORTED;
+        }
+    }
+    if (groups > 4) {
+        switch (c->deg) {
+            case 1: return ring_launch_cpt<T, 1, PRE, 64, 8>(c, P, Q, cpt, shm, s);
+            case 2: return ring_launch_cpt<T, 2, PRE, 64, 8>(c, P, Q, cpt, shm, s);
+            default: return PBTE_ERR_UNSUPPORTED;
+        }
+    }
     switch (c->deg) {
-        case 1: return ring_launch_deg<T, 1, PRE>(c, P, Q, cpt, shm, s);
-        case 2: return ring_launch_deg<T, 2, PRE>(c, P, Q, cpt, shm, s);
-        case 3: return ring_launch_deg<T, 3, PRE>(c, P, Q, cpt, shm, s);
+        case 1: return ring_launch_cpt<T, 1, PRE, 64, 4>(c, P, Q, cpt, shm, s);
+        case 2: return ring_launch_cpt<T, 2, PRE, 64, 4>(c, P, Q, cpt, shm, s);
+        case 3: return ring_launch_cpt<T, 3, PRE, 64, 4>(c, P, Q, cpt, shm, s);
         default: return PBTE_ERR_UNSUPPORTED;
     }
 }

@@ -102,6 +102,7 @@ _SIGS = {
     "pbte_set_done_flag": ([_vp, _vp], ctypes.c_int),
     "pbte_set_sweep_variant": ([_vp, ctypes.c_int], ctypes.c_int),
     "pbte_set_ring_groups": ([_vp, ctypes.c_int], ctypes.c_int),
+    "pbte_set_ring_width": ([_vp, ctypes.c_int], ctypes.c_int),
     "pbte_ctx_schedule": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                            ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_residual_check": ([_vp, _vp, ctypes.c_double, ctypes.c_int64, _vp, _vp, _vp,

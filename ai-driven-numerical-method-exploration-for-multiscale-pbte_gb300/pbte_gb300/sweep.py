@@ -153,9 +153,11 @@ class SweepContext:
         """Sweep kernel: 0 automatic, 1 level-serial, 2 ring-pipelined only."""
         _lib.check(_lib.lib().pbte_set_sweep_variant(self._ctx, int(variant)), "pbte_set_sweep_variant")
 
-    def set_groups(self, groups: int) -> None:
-        """Pipeline depth of the ring sweep (0: default)."""
+    def set_groups(self, groups: int, width: int = 0) -> None:
+        """Ring sweep block shape: pipeline depth (thread groups, 0: default)
+        and threads per group (0: 64, or 64 or 128)."""
         _lib.check(_lib.lib().pbte_set_ring_groups(self._ctx, int(groups)), "pbte_set_ring_groups")
+        _lib.check(_lib.lib().pbte_set_ring_width(self._ctx, int(width)), "pbte_set_ring_width")
 
     def schedule(self) -> dict:
         w, r, u = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

@@ -87,11 +87,15 @@ int pbte_ctx_destroy(pbte_ctx *ctx);
  * counterpart (pybte's mode switch is precomputed vs on-the-fly). */
 int pbte_set_sweep_variant(pbte_ctx *ctx, int variant);
 
-/* Pipeline depth of the ring sweep (thread groups of 64 per block, 0 =
- * default 4, at most 4 are used); the tuning knob of the autotuner.  And the
- * schedule the context derived: widest level, deepest upwind level gap, and
- * the number of distinct in-plane velocities (one sweep block each). */
+/* Shape of the ring sweep's blocks, the tuning knobs of the autotuner: the
+ * pipeline depth (thread groups per block; 0 = default 4, at most 8 are
+ * used) and the threads per group (0 = 64, or 64 or 128).  Shapes the
+ * library has no kernel for on the mesh fall back to four groups of 64.  And
+ * the schedule the context derived: widest level, deepest upwind level gap,
+ * and the number of distinct in-plane velocities (one sweep block each).
+ * No reference counterpart. */
 int pbte_set_ring_groups(pbte_ctx *ctx, int groups);
+int pbte_set_ring_width(pbte_ctx *ctx, int threads_per_group);
 int pbte_ctx_schedule(const pbte_ctx *ctx, int64_t *ring_w, int64_t *ring_r,
                       int64_t *n_unique_dirs);
 
