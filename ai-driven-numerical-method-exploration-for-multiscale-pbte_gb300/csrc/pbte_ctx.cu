@@ -85,7 +85,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_edofs, c->d_dir_class, c->d_class_lvl_off, c->d_class_nlev, c->d_lvl_ptr,
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
-                    c->d_udir_rep, c->d_udir_twin, c->d_srec64, c->d_srec32, c->d_mom_part,
+                    c->d_udir_rep, c->d_udir_twin, c->d_rf64, c->d_rf32, c->d_ri, c->d_mom_part,
                     c->d_cx32, c->d_cy32, c->d_w32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -241,8 +241,10 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     std::vector<int32_t> lvl_cells((size_t)c->nclass * nt), lvl_ptr, class_off(c->nclass),
         class_nlev(c->nclass);
     std::vector<int32_t> level, indeg, queue, count, pos(nt), far_idx;
-    std::vector<pbte::SweepRec<double>> srec64((size_t)c->nclass * nt);
-    std::vector<pbte::SweepRec<float>> srec32((size_t)c->nclass * nt);
+    const size_t M = (size_t)c->nclass * nt;   // field stride of the sweep records
+    std::vector<double> rf64(M * pbte::kNumRecReal);
+    std::vector<float> rf32(M * pbte::kNumRecReal);
+    std::vector<int32_t> ri(M * pbte::kNumRecInt);
     constexpr int kNearDepth = 4;
     // ring of upwind values in shared memory: slot (level % R) * W + position,
     // R = 1 + the largest level gap of an in-sweep dependency, W = widest level
@@ -301,21 +303,35 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         }
         c->far_max = std::max(c->far_max, nfar);
         for (int p = 0; p < nt; ++p) {
-            const int i = lvl_cells[(size_t)k * nt + p];
-            auto &s64 = srec64[(size_t)k * nt + p];
-            auto &s32 = srec32[(size_t)k * nt + p];
-            std::memset(&s64, 0, sizeof(s64));
-            std::memset(&s32, 0, sizeof(s32));
-            s64.c = r64[i];
-            s32.c = r32[i];
-            s64.cell = s32.cell = i;
-            s64.far_out = s32.far_out = far_idx[i];
+            const size_t kp = (size_t)k * nt + p;
+            const int i = lvl_cells[kp];
+            const auto &a = r64[i];
+            const auto &b32 = r32[i];
+            auto put = [&](int f, double v64, float v32) {
+                rf64[f * M + kp] = v64;
+                rf32[f * M + kp] = v32;
+            };
+            put(pbte::kRA2, a.area2, b32.area2);
+            put(pbte::kRGxa, a.gxa, b32.gxa);
+            put(pbte::kRGxb, a.gxb, b32.gxb);
+            put(pbte::kRGya, a.gya, b32.gya);
+            put(pbte::kRGyb, a.gyb, b32.gyb);
+            uint32_t kinds = 0;
             for (int il = 0; il < 3; ++il) {
-                s64.up[il] = s32.up[il] = up_slot[((size_t)k * nt + p) * 3 + il];
+                put(pbte::kREs + il, a.es[il], b32.es[il]);
+                put(pbte::kRNx + il, a.nx[il], b32.nx[il]);
+                put(pbte::kRNy + il, a.ny[il], b32.ny[il]);
+                put(pbte::kRBval + il, a.bval[il], b32.bval[il]);
+                ri[(pbte::kIUp + il) * M + kp] = up_slot[kp * 3 + il];
                 uint32_t packed = 0;
-                for (int b = 0; b < nf; ++b) packed |= (uint32_t)(r64[i].emap[il][b] & 15) << (4 * b);
-                s64.emp[il] = s32.emp[il] = packed;
+                for (int b = 0; b < nf; ++b) packed |= (uint32_t)(a.emap[il][b] & 15) << (4 * b);
+                ri[(pbte::kIEmp + il) * M + kp] = (int32_t)packed;
+                ri[(pbte::kIFace + il) * M + kp] = a.face[il];
+                kinds |= (uint32_t)(uint8_t)a.kind[il] << (8 * il);
             }
+            ri[pbte::kICell * M + kp] = i;
+            ri[pbte::kIFarOut * M + kp] = far_idx[i];
+            ri[pbte::kIKind * M + kp] = (int32_t)kinds;
         }
         c->nlev_max = std::max(c->nlev_max, nlev);
         c->ring_W = std::max(c->ring_W, W);
@@ -344,8 +360,9 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     TRY(upload(lvl_ptr.data(), lvl_ptr.size(), &c->d_lvl_ptr, &c->device_bytes));
     TRY(upload(lvl_cells.data(), lvl_cells.size(), &c->d_lvl_cells, &c->device_bytes));
     TRY(upload(up_slot.data(), up_slot.size(), &c->d_up_slot, &c->device_bytes));
-    TRY(upload(srec64.data(), srec64.size(), &c->d_srec64, &c->device_bytes));
-    TRY(upload(srec32.data(), srec32.size(), &c->d_srec32, &c->device_bytes));
+    TRY(upload(rf64.data(), rf64.size(), &c->d_rf64, &c->device_bytes));
+    TRY(upload(rf32.data(), rf32.size(), &c->d_rf32, &c->device_bytes));
+    TRY(upload(ri.data(), ri.size(), &c->d_ri, &c->device_bytes));
     TRY(upload(class_W.data(), class_W.size(), &c->d_class_W, &c->device_bytes));
     TRY(upload(class_R.data(), class_R.size(), &c->d_class_R, &c->device_bytes));
     TRY(upload(urep.data(), urep.size(), &c->d_udir_rep, &c->device_bytes));

@@ -45,9 +45,10 @@ struct SweepParams {
     T inv_tau_c, ca, cb, wall_scale;
 };
 
-// Assemble the element operator (without the volume part when PRECOMP).
-template <typename T, int DEG>
-__device__ __forceinline__ void assemble(const T *sref, const CellRec<T> &r, T cx, T cy, T inv_tau_c,
+// Assemble the element operator.  Rec: anything with the geometry members
+// of CellRec (area2, gxa, gxb, gya, gyb, es[3]).
+template <typename T, int DEG, typename Rec>
+__device__ __forceinline__ void assemble(const T *sref, const Rec &r, T cx, T cy, T inv_tau_c,
                                          const T (&s)[3], T (&A)[Shape<DEG>::NP][Shape<DEG>::NP]) {
     constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
     const T p = r.area2 * inv_tau_c;

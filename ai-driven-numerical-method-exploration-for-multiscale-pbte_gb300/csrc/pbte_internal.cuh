@@ -30,20 +30,21 @@ struct alignas(16) CellRec {
     int8_t emap[3][kMaxNf]; // neighbour DOF facing each of this element's edge DOFs
 };
 
-// Element record in a direction class's sweep order: the element's operator
-// description plus where its upwind values live during a sweep.
+// Element records of the ring sweep, field-major: field f of the element at
+// position k of a direction class's sweep order (k in [cls * n_tris,
+// (cls + 1) * n_tris)) is at f * stride + k, so a warp reading one field of
+// consecutive positions makes one coalesced access.
+//   real fields (T):  area2, gxa, gxb, gya, gyb, es[3], nx[3], ny[3], bval[3]
+//   int fields:       cell, far_out, up[3], emp[3], face[3], kind (3 bytes)
 // up[il]: -1 no in-sweep inflow; >= 0 slot of the near ring
 // ((level % R) * W + position); <= -2 far slot -(up + 2).
 // far_out: far slot this element's values must also be kept in, or -1.
-// emp[il]: c.emap[il][0..nf-1] packed four bits each (nd <= 15), so the
-// inflow gather needs one register per edge.
-template <typename T>
-struct alignas(16) SweepRec {
-    CellRec<T> c;
-    int32_t cell, far_out;
-    int32_t up[3];
-    uint32_t emp[3];
-};
+// emp[il]: emap[il][0..nf-1] packed four bits each (nd <= 15).
+// kind: kind[il] in byte il.
+enum RecReal { kRA2 = 0, kRGxa, kRGxb, kRGya, kRGyb, kREs, kRNx = kREs + 3, kRNy = kRNx + 3,
+               kRBval = kRNy + 3, kNumRecReal = kRBval + 3 };
+enum RecInt { kICell = 0, kIFarOut, kIUp, kIEmp = kIUp + 3, kIFace = kIEmp + 3, kIKind = kIFace + 3,
+              kNumRecInt };
 
 struct WallFace {
     int32_t face, tri, lfc, pad;
@@ -92,9 +93,11 @@ struct pbte_ctx {
     int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
     int ring_groups = 0;            // thread groups of the ring pipeline (0: default)
     int ring_width = 0;             // threads per group of the ring pipeline (0: 64)
-    // per-class records in sweep order ([nclass][n_tris]) and far-slot count
-    pbte::SweepRec<double> *d_srec64 = nullptr;
-    pbte::SweepRec<float> *d_srec32 = nullptr;
+    // per-class records in sweep order, field-major with stride nclass * n_tris
+    // (RecReal / RecInt), and the far-slot count
+    double *d_rf64 = nullptr;
+    float *d_rf32 = nullptr;
+    int32_t *d_ri = nullptr;
     int far_max = 0;
     double *d_mom_part = nullptr;   // [ceil(ndir/32)][3][n_tris*ndof] moment partial sums
     float *d_cx32 = nullptr, *d_cy32 = nullptr, *d_w32 = nullptr;   // ordinates in FP32

@@ -665,7 +665,7 @@ int launch_sweep64(pbte_ctx *c, double *vdf, const double *fw, const double *pbu
     P.lu = c->d_lu; P.piv = c->d_piv;
     if (c->sweep_variant != 1 && !use_pbuf) {
         const int rc = c->d_lu ? launch_ring<double, true>(c, P, s) : launch_ring<double, false>(c, P, s);
-        if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant == 2) return rc;
+        if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant >= 2) return rc;
     }
     if (c->d_lu) return sweep_dispatch<double, true>(c, P, s);
     return sweep_dispatch<double, false>(c, P, s);
@@ -677,7 +677,7 @@ int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scal
     P.flux_wall = fw; P.wall_scale = (float)wall_scale;
     if (c->sweep_variant != 1) {
         const int rc = launch_ring<float, false>(c, P, s);
-        if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant == 2) return rc;
+        if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant >= 2) return rc;
     }
     return sweep_dispatch<float, false>(c, P, s);
 }

@@ -4,22 +4,24 @@
 // z-mirror twin share it, so the block stores the result under both).  The
 // block's threads form G groups of 64; group g owns the wavefront levels
 // L = g, g+G, ...  For its level a group first does everything that does not
-// depend on the upwind values -- read the element records (stored in the
-// direction class's sweep order, so a level is one contiguous run), form the
-// source and wall terms, assemble and LU-factor the element operators in
-// registers (or load the stored FP64 factors), and prefetch the records of
-// its next level into L1 -- and only then waits for level L-1 (bar.sync on
-// the barrier the previous group arrives at).  It then adds the upwind inflow
-// from shared memory, finishes the two triangular solves, stores the result
-// in shared memory, arrives on its own barrier for level L+1, and only after
-// that writes the distribution to global memory.  The critical path per level
-// is the inflow gather plus two small triangular solves; the factorisation of
-// the next levels overlaps it on the other groups.
+// depend on the upwind values -- read the element records, form the source
+// and wall terms, assemble and LU-factor the element operators in registers
+// (or load the stored FP64 factors) -- and only then waits for level L-1
+// (bar.sync on the barrier the previous group arrives at).  It then adds the
+// upwind inflow from shared memory, finishes the two triangular solves,
+// stores the result in shared memory, arrives on its own barrier for level
+// L+1, and only after that writes the distribution to global memory and
+// prefetches the source rows of its next level into L1.  The critical path
+// per level is the inflow gather plus two small triangular solves; the
+// factorisation of the next levels overlaps it on the other groups.
 //
-// Registers bound the number of groups an SM can hold, so the records are not
-// copied into registers: fields are read from L1 where they are used, and
-// only what the post-barrier part needs (upwind slot codes, packed edge maps,
-// far slot, edge factors) is carried across the barrier.
+// The records are field-major in the direction class's sweep order (a level
+// is one contiguous run of positions), so each field read of a warp is one
+// coalesced access: per-thread records (an array of structs) made the L1
+// the busiest unit of the kernel and slowed the shared-memory traffic of the
+// critical path queued behind it.  Only what the post-barrier part needs
+// (upwind slot codes, packed edge maps, far slot, edge factors) is carried
+// across the barrier in registers.
 //
 // Upwind values live in a near ring of the last R <= 4 levels (slot
 // (level % R) * W + position) and, for the few dependencies that reach
@@ -28,6 +30,7 @@
 // level L+R overwrites level L's slot only after the barrier chain has
 // passed L+R-1, and every level reads its inflow before it arrives.
 #include <algorithm>
+#include <type_traits>
 
 #include "pbte_device.cuh"
 
@@ -36,7 +39,9 @@ namespace pbte {
 constexpr int kMaxGroups = 8;
 
 struct RingParams {
-    const void *recs;           // SweepRec<T>[nclass * n_tris] in sweep order
+    const void *rf;             // T[kNumRecReal][stride]: real record fields in sweep order
+    const int32_t *ri;          // [kNumRecInt][stride]: integer record fields
+    int64_t stride;             // nclass * n_tris
     const int32_t *class_W, *class_R;
     const int32_t *udir_rep, *udir_twin;
     int groups;
@@ -46,6 +51,50 @@ struct RingParams {
 __device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 __device__ __forceinline__ void bar_arrive(int id, int n) { asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(n) : "memory"); }
 __device__ __forceinline__ void prefetch_l1(const void *p) { asm volatile("prefetch.global.L1 [%0];" ::"l"(p)); }
+
+// geometry of one element, as assemble() reads it
+template <typename T>
+struct Geo {
+    T area2, gxa, gxb, gya, gyb, es[3];
+};
+
+// the element's three moment sources (3 * NP values, row i of P.S), in pairs
+// where the row is 8-byte aligned for every i
+template <typename T, int NP>
+__device__ __forceinline__ void load_sources(const T *S, T (&v)[3 * NP]) {
+    if constexpr (sizeof(T) == 4 && (3 * NP) % 2 == 0) {
+        const float2 *s2 = reinterpret_cast<const float2 *>(S);
+#pragma unroll
+        for (int q = 0; q < 3 * NP / 2; ++q) {
+            const float2 x = __ldg(s2 + q);
+            v[2 * q] = x.x;
+            v[2 * q + 1] = x.y;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < 3 * NP; ++q) v[q] = __ldg(S + q);
+    }
+}
+
+// one element's NP values into its row of the distribution, in pairs where
+// the row is 8-byte (float) or 16-byte (double) aligned for every element
+template <typename T, int NP>
+__device__ __forceinline__ void store_row(T *o, const T (&v)[NP]) {
+    if constexpr (NP % 2 == 0) {
+        using V2 = typename std::conditional<sizeof(T) == 4, float2, double2>::type;
+        V2 *o2 = reinterpret_cast<V2 *>(o);
+#pragma unroll
+        for (int q = 0; q < NP / 2; ++q) {
+            V2 x;
+            x.x = v[2 * q];
+            x.y = v[2 * q + 1];
+            o2[q] = x;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < NP; ++q) o[q] = v[q];
+    }
+}
 
 // TPG: threads per group; GMAX: the most groups the kernel is compiled for
 // (its launch bound)
@@ -57,7 +106,9 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
     T *ring = sref + 6 * NP * NP;
     T *far = ring + Q.far_offset;
     if (stopped(P.done)) return;
-    const SweepRec<T> *__restrict__ recs = reinterpret_cast<const SweepRec<T> *>(Q.recs);
+    const T *__restrict__ rf = reinterpret_cast<const T *>(Q.rf);
+    const int32_t *__restrict__ ri = Q.ri;
+    const int64_t M = Q.stride;
     const int u = blockIdx.x;
     const int d = Q.udir_rep[u], d2 = Q.udir_twin[u];
     for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
@@ -73,29 +124,27 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
     int sing = 0;
     int beg = g < nlev ? P.lvl_ptr[off + g] : 0;
     int end = g < nlev ? P.lvl_ptr[off + g + 1] : 0;
+    // element indices of this group's current level (read one level ahead, so
+    // the source rows can be prefetched into L1 while the level before runs)
+    int cell[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) {
+        const int k = beg + t + c * TPG;
+        cell[c] = k < end ? __ldg(ri + kICell * M + k) : 0;
+    }
     for (int L = g; L < nlev; L += G) {
-        // the next level of this group: bounds now, records into L1
         const int Ln = L + G;
         const int nbeg = Ln < nlev ? P.lvl_ptr[off + Ln] : 0;
         const int nend = Ln < nlev ? P.lvl_ptr[off + Ln + 1] : 0;
+        int ncell[CPT];
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             const int k = nbeg + t + c * TPG;
-            if (k < nend) {
-                const char *p = reinterpret_cast<const char *>(recs + k);
-                prefetch_l1(p);
-                prefetch_l1(p + 128);
-                prefetch_l1(p + sizeof(SweepRec<T>) - 1);
-            }
+            ncell[c] = k < nend ? __ldg(ri + kICell * M + k) : -1;
         }
-        const SweepRec<T> *rc[CPT];
         bool valid[CPT];
 #pragma unroll
-        for (int c = 0; c < CPT; ++c) {
-            const int k = beg + t + c * TPG;
-            valid[c] = k < end;
-            rc[c] = recs + (valid[c] ? k : beg);
-        }
+        for (int c = 0; c < CPT; ++c) valid[c] = beg + t + c * TPG < end;
         T A[CPT][NP][NP];
         T b[CPT][NP];
         int piv[CPT][NP];
@@ -107,30 +156,36 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
-            const CellRec<T> &r = rc[c]->c;
-            const int i = rc[c]->cell;
+            const int64_t k = beg + t + c * TPG;
+            const int i = cell[c];
             {
                 // the source first, so its values are dead before the factorisation
-                const T *S = P.S + (size_t)i * 3 * NP;
+                T Sv[3 * NP];
+                load_sources<T, NP>(P.S + (size_t)i * 3 * NP, Sv);
 #pragma unroll
-                for (int m = 0; m < NP; ++m) b[c][m] = P.ca * S[m] + P.cb * (cx * S[NP + m] + cy * S[2 * NP + m]);
+                for (int m = 0; m < NP; ++m) b[c][m] = P.ca * Sv[m] + P.cb * (cx * Sv[NP + m] + cy * Sv[2 * NP + m]);
             }
+            Geo<T> r;
             T s[3];
 #pragma unroll
             for (int il = 0; il < 3; ++il) {
-                s[il] = cx * r.nx[il] + cy * r.ny[il];
+                r.es[il] = __ldg(rf + (kREs + il) * M + k);
+                s[il] = cx * __ldg(rf + (kRNx + il) * M + k) + cy * __ldg(rf + (kRNy + il) * M + k);
                 scin[c][il] = s[il] * r.es[il];
-                code[c][il] = rc[c]->up[il];
-                emp[c][il] = rc[c]->emp[il];
+                code[c][il] = __ldg(ri + (kIUp + il) * M + k);
+                emp[c][il] = (uint32_t)__ldg(ri + (kIEmp + il) * M + k);
             }
-            fo[c] = rc[c]->far_out;
+            fo[c] = __ldg(ri + kIFarOut * M + k);
+            const uint32_t kinds = (uint32_t)__ldg(ri + kIKind * M + k);
 #pragma unroll
             for (int il = 0; il < 3; ++il) {
                 if (!(s[il] < T(0))) continue;
                 const T *R = sref + (3 + il) * NP * NP;
-                const int kind = r.kind[il];
+                const int kind = (kinds >> (8 * il)) & 255u;
+                if (kind == 0) continue;
+                const int face = __ldg(ri + (kIFace + il) * M + k);
                 if (kind == 3) {
-                    const double *pb = P.pbuf + ((size_t)d * P.n_faces + r.face[il]) * NP;
+                    const double *pb = P.pbuf + ((size_t)d * P.n_faces + face) * NP;
 #pragma unroll
                     for (int a = 0; a < NF; ++a) {
                         const int ma = Shape<DEG>::edof(il, a);
@@ -141,7 +196,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
                         b[c][ma] -= scin[c][il] * acc;
                     }
                 } else if (kind == 1) {
-                    const T sc = s[il] * r.bval[il] * P.wall_scale * r.es[il];
+                    const T sc = s[il] * __ldg(rf + (kRBval + il) * M + k) * P.wall_scale * r.es[il];
 #pragma unroll
                     for (int a = 0; a < NF; ++a) {
                         const int ma = Shape<DEG>::edof(il, a);
@@ -151,10 +206,17 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
                         b[c][ma] -= sc * rs;
                     }
                 } else if (kind == 2) {
-                    const double *fw = P.flux_wall + (size_t)r.face[il] * NP;
+                    const double *fw = P.flux_wall + (size_t)face * NP;
 #pragma unroll
                     for (int m = 0; m < NP; ++m) b[c][m] -= s[il] * (-(T)fw[m]);
                 }
+            }
+            if constexpr (!PRECOMP) {
+                r.area2 = __ldg(rf + kRA2 * M + k);
+                r.gxa = __ldg(rf + kRGxa * M + k);
+                r.gxb = __ldg(rf + kRGxb * M + k);
+                r.gya = __ldg(rf + kRGya * M + k);
+                r.gyb = __ldg(rf + kRGyb * M + k);
             }
             if constexpr (PRECOMP) {
                 const double *lu = P.lu + ((size_t)d * P.nt + i) * NP * NP;
@@ -277,15 +339,18 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
-            const int i = rc[c]->cell;
-            T *o1 = f1 + (size_t)i * NP;
+            store_row<T, NP>(f1 + (size_t)cell[c] * NP, b[c]);
+            if (f2) store_row<T, NP>(f2 + (size_t)cell[c] * NP, b[c]);
+        }
+        // the next level's source rows into L1
 #pragma unroll
-            for (int m = 0; m < NP; ++m) o1[m] = b[c][m];
-            if (f2) {
-                T *o2 = f2 + (size_t)i * NP;
-#pragma unroll
-                for (int m = 0; m < NP; ++m) o2[m] = b[c][m];
-            }
+        for (int c = 0; c < CPT; ++c) {
+            if (ncell[c] < 0) continue;
+            const T *S = P.S + (size_t)ncell[c] * 3 * NP;
+            prefetch_l1(S);
+            prefetch_l1(S + 3 * NP - 1);
+            if constexpr (3 * NP * sizeof(T) > 128) prefetch_l1(S + 128 / sizeof(T));
+            cell[c] = ncell[c];
         }
         beg = nbeg;
         end = nend;
@@ -333,6 +398,14 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     };
     int width = c->ring_width == 128 ? 128 : 64;
     int groups = c->ring_groups > 0 ? std::min(c->ring_groups, kMaxGroups) : 4;
+    if (c->ring_groups == 0 && c->ring_width == 0 && c->deg <= 2) {
+        // measured defaults (C2/C3 square cavities, P1/P2, 256 ordinates):
+        // levels up to 64 wide take eight groups of 64 in FP32 (four in FP64,
+        // whose operators need twice the registers), levels up to 128 wide
+        // four groups of 128
+        if (c->ring_W <= 64) groups = sizeof(T) == 4 ? 8 : 4;
+        else if (c->ring_W <= 128) width = 128;
+    }
     if (width == 128 && (cpt_for(128) > 1 || c->deg > 2 || groups > 4)) width = 64;
     const int cpt = cpt_for(width);
     if (groups > 4 && (cpt > 2 || c->deg > 2)) groups = 4;
@@ -341,8 +414,9 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     const size_t ring_vals = (size_t)c->ring_R * c->ring_W * c->nd;
     const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + ring_vals + (size_t)c->far_max * c->nd);
     if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
-    const void *recs = sizeof(T) == 4 ? (const void *)c->d_srec32 : (const void *)c->d_srec64;
-    RingParams Q{recs, c->d_class_W, c->d_class_R, c->d_udir_rep, c->d_udir_twin, groups, (int)ring_vals};
+    const void *rf = sizeof(T) == 4 ? (const void *)c->d_rf32 : (const void *)c->d_rf64;
+    RingParams Q{rf, c->d_ri, (int64_t)c->nclass * c->n_tris, c->d_class_W, c->d_class_R,
+                 c->d_udir_rep, c->d_udir_twin, groups, (int)ring_vals};
     if (width == 128) {
         switch (c->deg) {
             case 1: return ring_launch_cpt<T, 1, PRE, 128, 4>(c, P, Q, cpt, shm, s);
