@@ -86,7 +86,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
                     c->d_udir_rep, c->d_udir_twin, c->d_rf64, c->d_rf32, c->d_ri, c->d_mom_part,
-                    c->d_cx32, c->d_cy32, c->d_w32};
+                    c->d_cx32, c->d_cy32, c->d_w32, c->d_udir_of};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -354,6 +354,12 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         utwin.push_back(tw);
     }
     c->n_udir = (int)urep.size();
+    std::vector<int32_t> udir_of(ndir, 0);
+    for (int u = 0; u < c->n_udir; ++u) {
+        udir_of[urep[u]] = u;
+        if (utwin[u] >= 0) udir_of[utwin[u]] = u;
+    }
+    TRY(upload(udir_of.data(), udir_of.size(), &c->d_udir_of, &c->device_bytes));
     TRY(upload(dir_class.data(), dir_class.size(), &c->d_dir_class, &c->device_bytes));
     TRY(upload(class_off.data(), class_off.size(), &c->d_class_lvl_off, &c->device_bytes));
     TRY(upload(class_nlev.data(), class_nlev.size(), &c->d_class_nlev, &c->device_bytes));
@@ -377,8 +383,8 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     if (cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
 
     if (precompute) {
-        TRY(alloc((size_t)ndir * nt * nd * nd, &c->d_lu, &c->device_bytes));
-        TRY(alloc((size_t)ndir * nt * nd, &c->d_piv, &c->device_bytes));
+        TRY(alloc(pbte::factor_count(c->n_udir, nt, nd * nd), &c->d_lu, &c->device_bytes));
+        TRY(alloc(pbte::factor_count(c->n_udir, nt, nd), &c->d_piv, &c->device_bytes));
         TRY(pbte::launch_factorise(c, 0));
         int32_t bad = 0;
         if (cudaMemcpy(&bad, c->d_singular, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) {

@@ -37,8 +37,9 @@ struct SweepParams {
     int use_pbuf;
     const double *cx, *cy;
     const int32_t *dir_class, *class_off, *class_nlev, *lvl_ptr, *lvl_cells;
-    const double *lu;
+    const double *lu;       // stored factors, factor_base() layout
     const int8_t *piv;
+    const int32_t *udir_of; // ordinate -> distinct in-plane velocity (factor owner)
     int32_t *singular;
     const int32_t *done;
     int nt, n_faces;

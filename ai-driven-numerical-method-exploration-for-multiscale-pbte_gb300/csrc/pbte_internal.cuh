@@ -46,6 +46,20 @@ enum RecReal { kRA2 = 0, kRGxa, kRGxb, kRGya, kRGyb, kREs, kRNx = kREs + 3, kRNy
 enum RecInt { kICell = 0, kIFarOut, kIUp, kIEmp = kIUp + 3, kIFace = kIEmp + 3, kIKind = kIFace + 3,
               kNumRecInt };
 
+// Stored FP64 factors are kept once per distinct in-plane velocity u (z-mirror
+// twins share them), in the direction class's sweep order and interleaved by
+// 32 positions: entry e (of NP*NP, or of NP pivots) of the element at sweep
+// position p (0 <= p < nt) is at factor_base(u, p, nt, n) + 32 * e, n = NP*NP
+// or NP.  A warp reading one entry of consecutive positions makes one
+// coalesced access.
+__host__ __device__ __forceinline__ size_t factor_base(int u, int p, int nt, int n) {
+    const int nblk = (nt + 31) >> 5;
+    return ((size_t)u * nblk + (size_t)(p >> 5)) * (size_t)n * 32 + (size_t)(p & 31);
+}
+__host__ __device__ __forceinline__ size_t factor_count(int n_udir, int nt, int n) {
+    return (size_t)n_udir * (size_t)((nt + 31) >> 5) * (size_t)n * 32;
+}
+
 struct WallFace {
     int32_t face, tri, lfc, pad;
     double nx, ny;  // inward normal (-n_out of the adjacent element)
@@ -77,7 +91,7 @@ struct pbte_ctx {
     pbte::WallFace *d_wall_ad = nullptr;
     double *d_S64 = nullptr;  // [3][nd][n_tris] moment sources of the current sweep
     float *d_S32 = nullptr;
-    double *d_lu = nullptr;   // [ndir][n_tris][nd][nd] precomputed factors (optional)
+    double *d_lu = nullptr;   // precomputed factors (optional), factor_base() layout
     int8_t *d_piv = nullptr;
     double *d_red = nullptr;  // reduction scratch
     int32_t *d_singular = nullptr;
@@ -89,6 +103,7 @@ struct pbte_ctx {
     int ring_W = 0, ring_R = 0;
     // one sweep per distinct in-plane velocity: representative ordinate and its z-twin (-1 if none)
     int32_t *d_udir_rep = nullptr, *d_udir_twin = nullptr;
+    int32_t *d_udir_of = nullptr;   // [ndir]: the distinct velocity an ordinate belongs to
     int n_udir = 0;
     int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
     int ring_groups = 0;            // thread groups of the ring pipeline (0: default)

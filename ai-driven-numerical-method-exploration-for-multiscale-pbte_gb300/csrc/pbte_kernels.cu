@@ -43,24 +43,25 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(SweepParams<T> P) 
             T b[NP];
             rhs<T, DEG>(P, sref, r, i, d, cx, cy, s, f, b);
             if constexpr (PRECOMP) {
-                const double *lu = P.lu + ((size_t)d * P.nt + i) * NP * NP;
-                const int8_t *pv = P.piv + ((size_t)d * P.nt + i) * NP;
+                const int u = P.udir_of[d], p = k - cls * P.nt;
+                const double *lu = P.lu + factor_base(u, p, P.nt, NP * NP);
+                const int8_t *pv = P.piv + factor_base(u, p, P.nt, NP);
 #pragma unroll
                 for (int k2 = 0; k2 < NP; ++k2) {
-                    const int p = pv[k2];
+                    const int pr = pv[32 * k2];
 #pragma unroll
                     for (int j = k2 + 1; j < NP; ++j)
-                        if (p == j) { const T t = b[k2]; b[k2] = b[j]; b[j] = t; }
+                        if (pr == j) { const T t = b[k2]; b[k2] = b[j]; b[j] = t; }
                 }
 #pragma unroll
                 for (int k2 = 0; k2 < NP; ++k2)
 #pragma unroll
-                    for (int j = k2 + 1; j < NP; ++j) b[j] -= b[k2] * (T)lu[j * NP + k2];
+                    for (int j = k2 + 1; j < NP; ++j) b[j] -= b[k2] * (T)lu[32 * (j * NP + k2)];
 #pragma unroll
                 for (int k2 = NP - 1; k2 >= 0; --k2) {
-                    b[k2] *= (T)lu[k2 * NP + k2];  // stored as 1/U_kk
+                    b[k2] *= (T)lu[32 * (k2 * NP + k2)];  // stored as 1/U_kk
 #pragma unroll
-                    for (int j = 0; j < k2; ++j) b[j] -= b[k2] * (T)lu[j * NP + k2];
+                    for (int j = 0; j < k2; ++j) b[j] -= b[k2] * (T)lu[32 * (j * NP + k2)];
                 }
             } else {
                 T A[NP][NP];
@@ -78,17 +79,21 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(SweepParams<T> P) 
 
 // Stored factors for the precomputed FP64 mode: LU with the row interchanges
 // of partial pivoting, unit-lower multipliers below the diagonal, U above it
-// and 1/U_kk on it; ipiv as in DGETF2.
+// and 1/U_kk on it; ipiv as in DGETF2.  One thread per (distinct in-plane
+// velocity, sweep position), written in the factor_base() layout.
 template <int DEG>
-__global__ void factorise_kernel(SweepParams<double> P, double *lu_out, int8_t *piv_out, int ndir) {
+__global__ void factorise_kernel(SweepParams<double> P, double *lu_out, int8_t *piv_out,
+                                 const int32_t *udir_rep, int n_udir) {
     constexpr int NP = Shape<DEG>::NP;
     __shared__ double sref[6 * NP * NP];
     for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
     __syncthreads();
-    const size_t total = (size_t)ndir * P.nt;
+    const size_t total = (size_t)n_udir * P.nt;
     int sing = 0;
     for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
-        const int d = (int)(t / P.nt), i = (int)(t % P.nt);
+        const int u = (int)(t / P.nt), p = (int)(t % P.nt);
+        const int d = udir_rep[u];
+        const int i = P.lvl_cells[(size_t)P.dir_class[d] * P.nt + p];
         const double cx = P.cx[d], cy = P.cy[d];
         const CellRec<double> r = P.cells[i];
         double s[3];
@@ -121,13 +126,14 @@ __global__ void factorise_kernel(SweepParams<double> P, double *lu_out, int8_t *
             }
             A[k][k] = rr;
         }
-        double *o = lu_out + t * NP * NP;
+        double *o = lu_out + factor_base(u, p, P.nt, NP * NP);
 #pragma unroll
         for (int m = 0; m < NP; ++m)
 #pragma unroll
-            for (int l = 0; l < NP; ++l) o[m * NP + l] = A[m][l];
+            for (int l = 0; l < NP; ++l) o[32 * (m * NP + l)] = A[m][l];
+        int8_t *po = piv_out + factor_base(u, p, P.nt, NP);
 #pragma unroll
-        for (int m = 0; m < NP; ++m) piv_out[t * NP + m] = pv[m];
+        for (int m = 0; m < NP; ++m) po[32 * m] = pv[m];
     }
     if (sing) atomicAdd(P.singular, sing);
 }
@@ -591,6 +597,7 @@ static SweepParams<T> make_params(pbte_ctx *c) {
     P.cx = c->d_cx; P.cy = c->d_cy;
     P.dir_class = c->d_dir_class; P.class_off = c->d_class_lvl_off; P.class_nlev = c->d_class_nlev;
     P.lvl_ptr = c->d_lvl_ptr; P.lvl_cells = c->d_lvl_cells;
+    P.udir_of = c->d_udir_of;
     P.singular = c->d_singular; P.done = c->done;
     P.nt = c->n_tris; P.n_faces = c->n_faces;
     P.inv_tau_c = (T)(1.0 / c->tau_c);
@@ -686,13 +693,14 @@ int launch_factorise(pbte_ctx *c, cudaStream_t s) {
     SweepParams<double> P = make_params<double>(c);
     P.cells = c->d_cells64; P.ref = c->d_ref64;
     const int th = 128;
-    const size_t total = (size_t)c->ndir * c->n_tris;
+    const size_t total = (size_t)c->n_udir * c->n_tris;
     const int bl = (int)std::min<size_t>((total + th - 1) / th, 152 * 16);
+    const int32_t *rep = c->d_udir_rep;
     switch (c->deg) {
-        case 1: factorise_kernel<1><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
-        case 2: factorise_kernel<2><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
-        case 3: factorise_kernel<3><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
-        case 4: factorise_kernel<4><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, c->ndir); break;
+        case 1: factorise_kernel<1><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, rep, c->n_udir); break;
+        case 2: factorise_kernel<2><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, rep, c->n_udir); break;
+        case 3: factorise_kernel<3><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, rep, c->n_udir); break;
+        case 4: factorise_kernel<4><<<bl, th, 0, s>>>(P, c->d_lu, c->d_piv, rep, c->n_udir); break;
         default: return PBTE_ERR_UNSUPPORTED;
     }
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;

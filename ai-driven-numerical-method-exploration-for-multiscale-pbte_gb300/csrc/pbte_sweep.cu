@@ -219,13 +219,14 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
                 r.gyb = __ldg(rf + kRGyb * M + k);
             }
             if constexpr (PRECOMP) {
-                const double *lu = P.lu + ((size_t)d * P.nt + i) * NP * NP;
-                const int8_t *pv = P.piv + ((size_t)d * P.nt + i) * NP;
+                const int p = (int)(k - (int64_t)cls * P.nt);
+                const double *lu = P.lu + factor_base(u, p, P.nt, NP * NP);
+                const int8_t *pv = P.piv + factor_base(u, p, P.nt, NP);
 #pragma unroll
                 for (int m = 0; m < NP; ++m) {
-                    piv[c][m] = pv[m];
+                    piv[c][m] = __ldg(pv + 32 * m);
 #pragma unroll
-                    for (int l = 0; l < NP; ++l) A[c][m][l] = (T)lu[m * NP + l];
+                    for (int l = 0; l < NP; ++l) A[c][m][l] = (T)__ldg(lu + 32 * (m * NP + l));
                 }
             } else if constexpr (sizeof(T) == 4) {
                 // FP32: no row interchanges.  x^T A x = |x|^2_M / tau_c +
