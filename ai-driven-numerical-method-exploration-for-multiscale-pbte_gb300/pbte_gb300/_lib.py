@@ -110,6 +110,7 @@ _SIGS = {
     "pbte_transport_residual": ([_vp] * 9 + [_vp], ctypes.c_int),
     "pbte_transport_residual_noalloc": ([_vp] * 8 + [_vp], ctypes.c_int),
     "pbte_cgs2": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_cgs2_f32": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, _vp], ctypes.c_int),
     "pbte_hot_source": ([_vp, _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],

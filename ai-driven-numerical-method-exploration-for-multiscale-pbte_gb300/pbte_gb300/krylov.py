@@ -128,37 +128,36 @@ class ArnoldiGraphs:
     buffer: the host reads that buffer once per product (for the Givens
     rotations and the stopping test) instead of driving a dozen launches.
     Graphs are captured on first use of each ``j`` and replayed across
-    restarts."""
+    restarts.
 
-    def __init__(self, op: FixedPointOperator, g: torch.Tensor | None, m_cap: int):
+    ``dtype`` is the storage of the basis and of ``w``: float64, or float32
+    for the inner solve of the mixed-precision mode, whose operator is an
+    FP32 sweep (``pbte_cgs2_f32``).  ``g`` is copied into a buffer the graphs
+    read, so the graphs stay valid for a new ``g`` (:meth:`set_g`)."""
+
+    def __init__(self, op: FixedPointOperator, g: torch.Tensor | None, m_cap: int, dtype=torch.float64):
         self.op = op
         n = op.n
         dev = op.s.device
         f64 = dict(dtype=torch.float64, device=dev)
-        self.n = n
-        self.m_cap = m_cap
-        self.Q = torch.zeros((m_cap + 1, n), **f64)
-        self.w = torch.zeros(n, **f64)
-        self.tmp = torch.zeros(n, **f64)
-        self.c1 = torch.zeros(m_cap + 1, **f64)
-        self.c2 = torch.zeros(m_cap + 1, **f64)
-        self.h = torch.zeros(m_cap + 2, **f64)
-        self.scratch = torch.zeros(610 * 64, **f64)   # pbte_cgs2 block partials
         if m_cap + 1 > 64:
             raise ValueError("graph-captured Arnoldi supports a basis of at most 63 vectors")
+        self.n = n
+        self.m_cap = m_cap
+        self.dtype = dtype
+        self.Q = torch.zeros((m_cap + 1, n), dtype=dtype, device=dev)
+        self.w = torch.zeros(n, dtype=dtype, device=dev)
+        self.tmp = torch.zeros(n, **f64)
+        self.h = torch.zeros(m_cap + 2, **f64)
+        self.scratch = torch.zeros(610 * 64, **f64)   # pbte_cgs2 block partials and ticket
         self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
-        self.g = g
+        self.g = None if g is None else g.detach().clone()
         self.graphs = {}
         self.stream = torch.cuda.Stream(device=dev)
         self.on_product = None   # called after every product (sweep bookkeeping)
-        # run the captured library ops once outside capture (cuBLAS handle
-        # creation is not allowed while a graph is being captured)
-        self.stream.wait_stream(torch.cuda.current_stream())
-        with torch.cuda.stream(self.stream):
-            torch.mv(self.Q[:1], self.w, out=self.c1[:1])
-            torch.mv(self.Q[:1].T, self.c1[:1], out=self.tmp)
-            torch.linalg.vector_norm(self.w, out=self.h[0])
-        torch.cuda.synchronize(dev)
+
+    def set_g(self, g: torch.Tensor) -> None:
+        self.g.copy_(g)
 
     def _record(self, j: int) -> None:
         op = self.op
@@ -172,9 +171,9 @@ class ArnoldiGraphs:
             torch.sub(qj, self.tmp, out=self.w)
         else:
             torch.sub(qj, op.uout[:n], out=self.w)
-        _lib.check(_lib.lib().pbte_cgs2(Qj.data_ptr(), self.Q.stride(0), j + 1, self.w.data_ptr(), n,
-                                        self.h.data_ptr(), self.scratch.data_ptr(),
-                                        torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
+        fn = _lib.lib().pbte_cgs2_f32 if self.dtype == torch.float32 else _lib.lib().pbte_cgs2
+        _lib.check(fn(Qj.data_ptr(), self.Q.stride(0), j + 1, self.w.data_ptr(), n, self.h.data_ptr(),
+                      self.scratch.data_ptr(), torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
 
     def column(self, j: int) -> np.ndarray:
         if j not in self.graphs:
@@ -339,9 +338,21 @@ def _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, ar: ArnoldiGr
             rmat = np.zeros((k, k))
             for j, col in enumerate(cols):
                 rmat[:j + 1, j] = col
-            y = torch.from_numpy(_back_substitute(rmat, np.asarray(gam[:k]))).to(b.device)
+            y = torch.from_numpy(_back_substitute(rmat, np.asarray(gam[:k]))).to(device=b.device, dtype=Q.dtype)
             x += Q[:k].T @ y
     return x, converged, nmv
+
+
+def cached(solver, key, make):
+    """Operators and Arnoldi graphs kept on the solver across runs: their
+    CUDA graphs hold the context's and the solver's buffers, so an entry is
+    rebuilt when the solver has a new context or distribution buffer."""
+    cache = solver.__dict__.setdefault("_krylov_cache", {})
+    hit = cache.get(key)
+    if hit is None or hit[0] is not solver.ctx or hit[1] != solver.vdf.data_ptr():
+        hit = (solver.ctx, solver.vdf.data_ptr(), make())
+        cache[key] = hit
+    return hit[2]
 
 
 def basis_cap(case, n: int) -> int:
@@ -355,7 +366,8 @@ def run_krylov(solver):
     """``pybte/krylov.py:257-363`` on the device."""
     c = solver.case
     tol, tmax = c.iteration.tol, c.iteration.tmax
-    op = FixedPointOperator(solver)
+    op = cached(solver, "fp64", lambda: FixedPointOperator(solver))
+    op.sweeps = 0
     residuals, masses = [], []
 
     def sweep(u):
@@ -389,8 +401,9 @@ def run_krylov(solver):
         return reached >= 0 and n - reached > max(64, reached // 4)
 
     x = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
-    ar = ArnoldiGraphs(op, g, cap) if cap <= 63 else None
+    ar = cached(solver, ("arnoldi64", cap), lambda: ArnoldiGraphs(op, g, cap)) if cap <= 63 else None
     if ar is not None:
+        ar.set_g(g)
         def product():
             masses.append(np.nan)
             residuals.append(np.nan)

@@ -24,7 +24,7 @@ import time
 import numpy as np
 import torch
 
-from .krylov import ArnoldiGraphs, FixedPointOperator, basis_cap, gmres
+from .krylov import ArnoldiGraphs, FixedPointOperator, basis_cap, cached, gmres
 
 __all__ = ["run_mixed", "MixedOptions"]
 
@@ -46,8 +46,9 @@ def run_mixed(solver, opts: MixedOptions | None = None):
     if solver.acc is not None:
         raise NotImplementedError("mixed precision GSIS is not implemented; use precision='fp64'")
     method = "krylov" if c.scheme.method == "krylov" else "source"
-    op64 = FixedPointOperator(solver, "fp64")
-    op32 = FixedPointOperator(solver, "fp32", homogeneous=True, integrals=False)
+    op64 = cached(solver, "fp64", lambda: FixedPointOperator(solver, "fp64"))
+    op32 = cached(solver, "fp32h", lambda: FixedPointOperator(solver, "fp32", homogeneous=True, integrals=False))
+    op64.sweeps = op32.sweeps = 0
     n = op64.n
     dev = solver.device
     u = torch.zeros(n, dtype=torch.float64, device=dev)
@@ -78,7 +79,9 @@ def run_mixed(solver, opts: MixedOptions | None = None):
         else:
             cap = basis_cap(c, n)
             if ar32 is None and cap <= 63:
-                ar32 = ArnoldiGraphs(op32, None, cap)
+                bdt = torch.float32 if c.performance.inner_basis == "fp32" else torch.float64
+                ar32 = cached(solver, ("arnoldi_inner", cap, bdt),
+                              lambda: ArnoldiGraphs(op32, None, cap, dtype=bdt))
             before = op32.sweeps
             d, _, _ = gmres(lambda v: v - op32.apply(v), r, tol_abs=opts.inner_rtol * rn,
                             maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap), max_basis=cap,

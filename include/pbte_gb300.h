@@ -180,12 +180,19 @@ int pbte_residual_check(pbte_ctx *ctx, const double *res, double tol, int64_t tm
                         void *stream);
 
 /* Classical Gram-Schmidt applied twice against the Krylov rows Q[0..rows-1]
- * (row stride ldq doubles), FP64, in place on w, as in gmres_full
+ * (row stride ldq elements), in place on w, as in gmres_full
  * (pybte/krylov.py:201-210): h[0..rows-1] = c1 + c2 and h[rows] = ||w||.
  * Deterministic (block partial sums added in a fixed order).  `scratch`
- * holds 610 * 64 doubles; rows <= 64. */
+ * holds 307 * 64 doubles, all zero before its first use; a call leaves it
+ * ready for the next one, and concurrent calls need separate scratch.
+ * rows <= 64.  pbte_cgs2 keeps the basis and w in FP64; pbte_cgs2_f32 keeps
+ * them in FP32 (FP32 products and warp sums, FP64 block and cross-block
+ * sums; no reference counterpart: the inner solve of the mixed-precision
+ * mode, whose operator is an FP32 sweep). */
 int pbte_cgs2(const double *Q, int64_t ldq, int32_t rows, double *w, int64_t n, double *h,
               double *scratch, void *stream);
+int pbte_cgs2_f32(const float *Q, int64_t ldq, int32_t rows, float *w, int64_t n, double *h,
+                  double *scratch, void *stream);
 
 /* GSIS per-iteration kernels (pybte/acceleration/):
  * third-order moment source, hot_source.py:29-58 -> work[n_tris][7*ndof];

@@ -203,26 +203,39 @@ def test_square_benchmark_mesh_levels(cuda):
     assert rec.iterations == 3
 
 
-@pytest.mark.parametrize("rows", [1, 5, 30])
-def test_cgs2_matches_two_pass_gram_schmidt(cuda, rows):
-    """pbte_cgs2 against pybte's CGS2 step (pybte/krylov.py:201-210) in numpy."""
+@pytest.mark.parametrize("rows", [1, 5, 30, 64])
+@pytest.mark.parametrize("f32", [False, True])
+def test_cgs2_matches_two_pass_gram_schmidt(cuda, rows, f32):
+    """pbte_cgs2 / pbte_cgs2_f32 against pybte's CGS2 step
+    (pybte/krylov.py:201-210) in numpy, on the same scratch twice in a row
+    (the cross-block ticket must be back at zero after each call).  FP64:
+    1e-12.  FP32 basis: the numpy reference runs on the FP32-rounded basis
+    and vector in FP64; FP32 products and warp sums leave ~1e-6."""
     from pbte_gb300 import _lib
     rng = np.random.default_rng(rows)
     n = 100_003
     Q, _ = np.linalg.qr(rng.standard_normal((n, rows)))
     Q = np.ascontiguousarray(Q.T)
     w = rng.standard_normal(n)
+    dt = torch.float32 if f32 else torch.float64
+    if f32:
+        Q = Q.astype(np.float32).astype(np.float64)
+        w = w.astype(np.float32).astype(np.float64)
     c1 = Q @ w
     w1 = w - Q.T @ c1
     c2 = Q @ w1
     w2 = w1 - Q.T @ c2
-    Qd = torch.from_numpy(Q).cuda()
-    wd = torch.from_numpy(w).cuda()
-    h = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
     scr = torch.zeros(610 * 64, dtype=torch.float64, device="cuda")
-    _lib.check(_lib.lib().pbte_cgs2(Qd.data_ptr(), n, rows, wd.data_ptr(), n, h.data_ptr(), scr.data_ptr(),
-                                    torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
-    hh = h.cpu().numpy()
-    assert np.allclose(hh[:rows], c1 + c2, rtol=1e-12, atol=1e-12)
-    assert hh[rows] == pytest.approx(np.linalg.norm(w2), rel=1e-12)
-    assert _rel(wd.cpu().numpy(), w2) < 1e-12
+    fn = _lib.lib().pbte_cgs2_f32 if f32 else _lib.lib().pbte_cgs2
+    tol = 2e-5 if f32 else 1e-12
+    for _ in range(2):
+        Qd = torch.from_numpy(Q).to("cuda", dt)
+        wd = torch.from_numpy(w).to("cuda", dt)
+        h = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
+        _lib.check(fn(Qd.data_ptr(), n, rows, wd.data_ptr(), n, h.data_ptr(), scr.data_ptr(),
+                      torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
+        hh = h.cpu().numpy()
+        scale = np.linalg.norm(w)
+        assert np.abs(hh[:rows] - (c1 + c2)).max() <= tol * scale
+        assert hh[rows] == pytest.approx(np.linalg.norm(w2), rel=tol, abs=tol * scale)
+        assert np.abs(wd.double().cpu().numpy() - w2).max() <= tol * scale
