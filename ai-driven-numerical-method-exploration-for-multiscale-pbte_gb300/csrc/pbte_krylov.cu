@@ -4,13 +4,15 @@
 //   c1 = Q w;  w -= Q^T c1;  c2 = Q w;  w -= Q^T c2;  h = c1 + c2;  h[j+1] = ||w||
 //
 // Three launches: pass 1 (c1), pass 2 (update by c1, then c2 and h), and the
-// last update fused with the norm.  Each launch splits n over kBlocks
-// blocks: each thread accumulates all rows over its stride, each warp
-// reduces its accumulators with shuffles, and the block's warps are summed in
-// warp order into one partial per (block, row).  The last block to finish
-// (a fence, then a ticket from an atomic counter -- nothing waits on it) adds
-// the block partials per row in block order with a fixed warp tree, so the
-// result is deterministic and no separate reduction launch is needed.
+// last update fused with the norm.  A block owns chunks of kT * kE
+// consecutive entries; a thread keeps its kE entries of w in registers while
+// the rows stream past in batches of kRB (so registers do not grow with the
+// row count, and a batch's loads are in flight together).  Per row, each
+// warp reduces with shuffles and the block's warps are added in warp order
+// into one partial per (block, row).  The last block to finish (a fence,
+// then a ticket from an atomic counter -- nothing waits on it) adds the
+// block partials per row in block order with a fixed warp tree, so the result
+// is deterministic and no separate reduction launch is needed.
 //
 // Two storage types: FP64 basis (V = double, the FP64 GMRES) and FP32 basis
 // (V = float, the inner GMRES of the mixed-precision solve, whose operator
@@ -18,6 +20,8 @@
 // products made the FP64 basis the largest cost of an inner Arnoldi column;
 // in the FP32 form the products, the per-thread and the warp sums are FP32
 // and only the block partials and the cross-block sums are FP64.
+#include <algorithm>
+
 #include <cuda_runtime.h>
 
 #include "pbte_internal.cuh"
@@ -26,7 +30,9 @@ namespace {
 
 constexpr int kT = 256;
 constexpr int kWarps = kT / 32;
-constexpr int kBlocks = 304;     // 2 x 152 SMs
+constexpr int kE = 4;              // entries per thread per chunk
+constexpr int kRB = 8;             // rows per batch
+constexpr int kMaxBlocks = 1216;   // 8 x 152 SMs
 constexpr int kMaxRows = 64;
 
 template <typename V>
@@ -36,7 +42,7 @@ __device__ __forceinline__ V warp_sum(V v) {
     return v;
 }
 
-// Scratch layout (doubles): part[kBlocks][kMaxRows], c1[kMaxRows],
+// Scratch layout (doubles): part[kMaxBlocks][kMaxRows], c1[kMaxRows],
 // c2[kMaxRows], then the ticket counter (one unsigned, kept at zero between
 // calls).
 struct Scratch {
@@ -47,34 +53,47 @@ struct Scratch {
 __host__ __device__ inline Scratch scratch_of(double *s) {
     Scratch r;
     r.part = s;
-    r.c1 = s + (size_t)kBlocks * kMaxRows;
+    r.c1 = s + (size_t)kMaxBlocks * kMaxRows;
     r.c2 = r.c1 + kMaxRows;
     r.ticket = reinterpret_cast<unsigned int *>(r.c2 + kMaxRows);
     return r;
 }
 
-// Called by every block after it wrote its partials; returns true in the
-// one block that arrives last (which then owns the cross-block sums).
+// After the block's partials are stored: one fence and one ticket per
+// block.  Returns true in the one block that arrives last (which then owns
+// the cross-block sums).
 __device__ __forceinline__ bool last_block(unsigned int *ticket) {
     __shared__ bool is_last;
-    __threadfence();
     __syncthreads();
-    if (threadIdx.x == 0) is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    if (threadIdx.x == 0) {
+        __threadfence();
+        is_last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    }
     __syncthreads();
     if (is_last) __threadfence();
     return is_last;
 }
 
 // sum over blocks of part[b][k] in a fixed order: warp wid handles rows
-// wid, wid + kWarps, ...; lane l adds blocks l, l + 32, ... then the warp
-// tree.  Writes out[k] (and out_plus[k] = out[k] + add[k] when given, or the
-// square root when `root`).
+// wid, wid + kWarps, ...; lane l adds blocks l, l + 32, ... (loads of a
+// round of 8 first) then the warp tree.  Writes out[k] (and out_plus[k] =
+// out[k] + add[k] when given), or the square root when `root`.
 __device__ void finish_rows(const double *part, int rows, double *out, const double *add, double *out_plus,
                             bool root) {
     const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+    const int nb = gridDim.x;
     for (int k = wid; k < rows; k += kWarps) {
         double s = 0.0;
-        for (int b = lane; b < kBlocks; b += 32) s += __ldcg(part + (size_t)b * kMaxRows + k);
+        for (int b0 = 0; b0 < nb; b0 += 256) {
+            double v[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) {
+                const int b = b0 + lane + 32 * i;
+                v[i] = b < nb ? __ldcg(part + (size_t)b * kMaxRows + k) : 0.0;
+            }
+#pragma unroll
+            for (int i = 0; i < 8; ++i) s += v[i];
+        }
         s = warp_sum(s);
         if (lane == 0) {
             if (root) {
@@ -87,114 +106,193 @@ __device__ void finish_rows(const double *part, int rows, double *out, const dou
     }
 }
 
-// part[b][k] = sum over this block's entries of Q[k] .* x, where x = w - Q^T c
-// when `c` is given (and then w <- x is stored), else x = w.  The last block
-// forms out[k] = sum_b part[b][k] (and out_plus = out + add).
-template <typename V, int R>
-__global__ void __launch_bounds__(kT) multidot_kernel(const V *__restrict__ Q, long long ldq, int rows,
-                                                      V *__restrict__ w, const double *__restrict__ c,
-                                                      long long n, double *scratch, double *out,
-                                                      const double *add, double *out_plus) {
-    __shared__ double wsum[kWarps][R];
-    const Scratch S = scratch_of(scratch);
-    V acc[R];
+// x[e] -= sum_k Q[k][t_e] c[k] over the rows, batches of kRB loads in flight
+template <typename V>
+__device__ __forceinline__ void subtract_rows(const V *__restrict__ Q, long long ldq, int rows, const V *csh,
+                                              long long base, long long n, V (&x)[kE]) {
+    int k = 0;
+    for (; k + kRB <= rows; k += kRB) {
+        V qv[kRB][kE];
 #pragma unroll
-    for (int k = 0; k < R; ++k) acc[k] = V(0);
-    V cc[R];
+        for (int r = 0; r < kRB; ++r)
 #pragma unroll
-    for (int k = 0; k < R; ++k) cc[k] = (c && k < rows) ? (V)c[k] : V(0);
-    for (long long t = (long long)blockIdx.x * kT + threadIdx.x; t < n; t += (long long)gridDim.x * kT) {
-        V x = w[t];
-        if (c) {
+            for (int e = 0; e < kE; ++e) {
+                const long long t = base + (long long)e * kT;
+                qv[r][e] = t < n ? Q[(k + r) * ldq + t] : V(0);
+            }
 #pragma unroll
-            for (int k = 0; k < R; ++k)
-                if (k < rows) x -= Q[k * ldq + t] * cc[k];
-            w[t] = x;
+        for (int r = 0; r < kRB; ++r) {
+            const V ck = csh[k + r];
+#pragma unroll
+            for (int e = 0; e < kE; ++e) x[e] -= qv[r][e] * ck;
+        }
+    }
+    for (; k < rows; ++k) {
+        const V ck = csh[k];
+#pragma unroll
+        for (int e = 0; e < kE; ++e) {
+            const long long t = base + (long long)e * kT;
+            if (t < n) x[e] -= Q[k * ldq + t] * ck;
+        }
+    }
+}
+
+// wsum[wid][k] += warp sum of sum_e Q[k][t_e] x[e], for every row
+template <typename V>
+__device__ __forceinline__ void dot_rows(const V *__restrict__ Q, long long ldq, int rows, long long base,
+                                         long long n, const V (&x)[kE], double (*wsum)[kMaxRows]) {
+    const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+    int k = 0;
+    for (; k + kRB <= rows; k += kRB) {
+        V a[kRB];
+#pragma unroll
+        for (int r = 0; r < kRB; ++r) {
+            a[r] = V(0);
+#pragma unroll
+            for (int e = 0; e < kE; ++e) {
+                const long long t = base + (long long)e * kT;
+                if (t < n) a[r] += Q[(k + r) * ldq + t] * x[e];
+            }
         }
 #pragma unroll
-        for (int k = 0; k < R; ++k)
-            if (k < rows) acc[k] += Q[k * ldq + t] * x;
-    }
-    const int lane = threadIdx.x % 32, wid = threadIdx.x / 32;
+        for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
-    for (int k = 0; k < R; ++k) {
-        const V v = warp_sum(acc[k]);
-        if (lane == 0) wsum[wid][k] = (double)v;
+            for (int r = 0; r < kRB; ++r) a[r] += __shfl_xor_sync(0xffffffffu, a[r], o);
+        if (lane == 0)
+#pragma unroll
+            for (int r = 0; r < kRB; ++r) wsum[wid][k + r] += (double)a[r];
+    }
+    for (; k < rows; ++k) {
+        V a = V(0);
+#pragma unroll
+        for (int e = 0; e < kE; ++e) {
+            const long long t = base + (long long)e * kT;
+            if (t < n) a += Q[k * ldq + t] * x[e];
+        }
+        a = warp_sum(a);
+        if (lane == 0) wsum[wid][k] += (double)a;
+    }
+}
+
+// MODE 0: x = w (or, with uout, x = qj - (uout - g), stored into w), then
+//         out[k] = sum_t Q[k][t] x[t].
+// MODE 1: x = w - Q^T c, stored into w, then out[k] = Q[k] . x and
+//         out_plus[k] = out[k] + add[k].
+// MODE 2: x = w - Q^T c, stored into w, then out[0] = ||x||.
+template <typename V, int MODE>
+__global__ void __launch_bounds__(kT) cgs2_pass_kernel(const V *__restrict__ Q, long long ldq, int rows,
+                                                       V *__restrict__ w, const double *__restrict__ c, long long n,
+                                                       double *scratch, double *out, const double *add,
+                                                       double *out_plus, const V *__restrict__ qj,
+                                                       const double *__restrict__ uout,
+                                                       const double *__restrict__ g) {
+    __shared__ double wsum[kWarps][kMaxRows];
+    __shared__ V csh[kMaxRows];
+    const Scratch S = scratch_of(scratch);
+    const int nrow = MODE == 2 ? 1 : rows;
+    for (int i = threadIdx.x; i < kWarps * kMaxRows; i += kT) (&wsum[0][0])[i] = 0.0;
+    if (MODE > 0 && (int)threadIdx.x < rows) csh[threadIdx.x] = (V)c[threadIdx.x];
+    __syncthreads();
+    const long long chunk = (long long)kT * kE;
+    const long long nchunk = (n + chunk - 1) / chunk;
+    V nrm = V(0);
+    for (long long ch = blockIdx.x; ch < nchunk; ch += gridDim.x) {
+        const long long base = ch * chunk + threadIdx.x;
+        V x[kE];
+#pragma unroll
+        for (int e = 0; e < kE; ++e) {
+            const long long t = base + (long long)e * kT;
+            if (t >= n) {
+                x[e] = V(0);
+            } else if (MODE == 0 && uout) {
+                double y = uout[t];
+                if (g) y -= g[t];
+                x[e] = (V)((double)qj[t] - y);
+                w[t] = x[e];
+            } else {
+                x[e] = w[t];
+            }
+        }
+        if (MODE > 0) {
+            subtract_rows<V>(Q, ldq, rows, csh, base, n, x);
+#pragma unroll
+            for (int e = 0; e < kE; ++e) {
+                const long long t = base + (long long)e * kT;
+                if (t < n) w[t] = x[e];
+            }
+        }
+        if (MODE < 2) {
+            dot_rows<V>(Q, ldq, rows, base, n, x, wsum);
+        } else {
+#pragma unroll
+            for (int e = 0; e < kE; ++e) nrm += x[e] * x[e];
+        }
+    }
+    if (MODE == 2) {
+        nrm = warp_sum(nrm);
+        if (threadIdx.x % 32 == 0) wsum[threadIdx.x / 32][0] = (double)nrm;
     }
     __syncthreads();
-    if ((int)threadIdx.x < rows) {
+    if ((int)threadIdx.x < nrow) {
         double s = 0.0;
 #pragma unroll
         for (int q = 0; q < kWarps; ++q) s += wsum[q][threadIdx.x];
         S.part[(size_t)blockIdx.x * kMaxRows + threadIdx.x] = s;
     }
     if (last_block(S.ticket)) {
-        finish_rows(S.part, rows, out, add, out_plus, false);
+        finish_rows(S.part, nrow, out, add, out_plus, MODE == 2);
         if (threadIdx.x == 0) *S.ticket = 0u;
     }
 }
 
-// w -= Q^T c, and the last block forms ||w|| into *norm.
-template <typename V, int R>
-__global__ void __launch_bounds__(kT) update_norm_kernel(const V *__restrict__ Q, long long ldq, int rows,
-                                                         V *__restrict__ w, const double *__restrict__ c,
-                                                         long long n, double *scratch, double *norm) {
-    __shared__ double wsum[kWarps];
-    const Scratch S = scratch_of(scratch);
-    V cc[R];
-#pragma unroll
-    for (int k = 0; k < R; ++k) cc[k] = k < rows ? (V)c[k] : V(0);
-    V acc = V(0);
-    for (long long t = (long long)blockIdx.x * kT + threadIdx.x; t < n; t += (long long)gridDim.x * kT) {
-        V x = w[t];
-#pragma unroll
-        for (int k = 0; k < R; ++k)
-            if (k < rows) x -= Q[k * ldq + t] * cc[k];
-        w[t] = x;
-        acc += x * x;
-    }
-    const V v = warp_sum(acc);
-    if (threadIdx.x % 32 == 0) wsum[threadIdx.x / 32] = (double)v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-#pragma unroll
-        for (int q = 0; q < kWarps; ++q) s += wsum[q];
-        S.part[(size_t)blockIdx.x * kMaxRows] = s;
-    }
-    if (last_block(S.ticket)) {
-        finish_rows(S.part, 1, norm, nullptr, nullptr, true);
-        if (threadIdx.x == 0) *S.ticket = 0u;
-    }
-}
-
+// uout == nullptr: CGS2 of w in place.  Otherwise pass 1 first forms
+// w = Q[rows-1] - (uout - g) (the Arnoldi product of the newest basis vector).
 template <typename V>
-int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, double *scratch, void *stream) {
+int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
+         const double *uout, const double *g, void *stream) {
     if (!Q || !w || !h || !scratch || rows < 1 || rows > kMaxRows || n < 1 || ldq < n) return PBTE_ERR_ARG;
+    if (scratch_len < PBTE_CGS2_SCRATCH) return PBTE_ERR_ARG;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
     const Scratch S = scratch_of(scratch);
-    auto go = [&](auto mdot, auto upd) {
-        mdot<<<kBlocks, kT, 0, s>>>(Q, ldq, rows, w, nullptr, n, scratch, S.c1, nullptr, nullptr);
-        mdot<<<kBlocks, kT, 0, s>>>(Q, ldq, rows, w, S.c1, n, scratch, S.c2, S.c1, h);   // h = c1 + c2
-        upd<<<kBlocks, kT, 0, s>>>(Q, ldq, rows, w, S.c2, n, scratch, h + rows);
-        return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
-    };
-    if (rows <= 8) return go(multidot_kernel<V, 8>, update_norm_kernel<V, 8>);
-    if (rows <= 16) return go(multidot_kernel<V, 16>, update_norm_kernel<V, 16>);
-    if (rows <= 32) return go(multidot_kernel<V, 32>, update_norm_kernel<V, 32>);
-    return go(multidot_kernel<V, 64>, update_norm_kernel<V, 64>);
+    const V *qj = Q + (size_t)(rows - 1) * ldq;
+    const long long nchunk = (n + (long long)kT * kE - 1) / ((long long)kT * kE);
+    const int nb = (int)std::min<long long>(nchunk, kMaxBlocks);
+    cgs2_pass_kernel<V, 0><<<nb, kT, 0, s>>>(Q, ldq, rows, w, nullptr, n, scratch, S.c1, nullptr, nullptr, qj,
+                                             uout, g);
+    cgs2_pass_kernel<V, 1><<<nb, kT, 0, s>>>(Q, ldq, rows, w, S.c1, n, scratch, S.c2, S.c1, h,   // h = c1 + c2
+                                             nullptr, nullptr, nullptr);
+    cgs2_pass_kernel<V, 2><<<nb, kT, 0, s>>>(Q, ldq, rows, w, S.c2, n, scratch, h + rows, nullptr, nullptr,
+                                             nullptr, nullptr, nullptr);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
 }  // namespace
 
 // h[0..rows-1] = c1 + c2 and h[rows] = ||w|| after the two passes; `scratch`
-// holds (kBlocks + 3) * 64 doubles, zero before the first call.  rows <= 64.
+// holds scratch_len >= PBTE_CGS2_SCRATCH doubles, zero before the first call.
+// rows <= 64.
 extern "C" int pbte_cgs2(const double *Q, int64_t ldq, int32_t rows, double *w, int64_t n, double *h,
-                         double *scratch, void *stream) {
-    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, stream);
+                         double *scratch, int64_t scratch_len, void *stream) {
+    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, scratch_len, nullptr, nullptr, stream);
 }
 
 extern "C" int pbte_cgs2_f32(const float *Q, int64_t ldq, int32_t rows, float *w, int64_t n, double *h,
-                             double *scratch, void *stream) {
-    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, stream);
+                             double *scratch, int64_t scratch_len, void *stream) {
+    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, nullptr, nullptr, stream);
 }
+
+extern "C" int pbte_arnoldi_column(const double *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
+                                   double *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
+                                   void *stream) {
+    if (!uout) return PBTE_ERR_ARG;
+    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, stream);
+}
+
+extern "C" int pbte_arnoldi_column_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout,
+                                       const double *g, float *w, int64_t n, double *h, double *scratch,
+                                       int64_t scratch_len, void *stream) {
+    if (!uout) return PBTE_ERR_ARG;
+    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, stream);
+}
+
+static_assert((size_t)kMaxBlocks * kMaxRows + 3 * kMaxRows <= PBTE_CGS2_SCRATCH, "scratch size");

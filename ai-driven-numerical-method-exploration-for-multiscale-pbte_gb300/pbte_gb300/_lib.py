@@ -21,6 +21,7 @@ SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_krylov.cu", 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0
+CGS2_SCRATCH = 1220 * 64   # PBTE_CGS2_SCRATCH
 ERRORS = {-1: "bad argument", -2: "CUDA runtime error", -3: "sweep graph has a cycle",
           -4: "configuration not supported", -5: "device wait timed out",
           -6: "singular element operator", -7: "device allocation failed"}
@@ -109,8 +110,14 @@ _SIGS = {
                              ctypes.c_int64, _vp], ctypes.c_int),
     "pbte_transport_residual": ([_vp] * 9 + [_vp], ctypes.c_int),
     "pbte_transport_residual_noalloc": ([_vp] * 8 + [_vp], ctypes.c_int),
-    "pbte_cgs2": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, _vp], ctypes.c_int),
-    "pbte_cgs2_f32": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_cgs2": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int64, _vp],
+                  ctypes.c_int),
+    "pbte_cgs2_f32": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int64, _vp],
+                      ctypes.c_int),
+    "pbte_arnoldi_column": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, _vp,
+                             ctypes.c_int64, _vp], ctypes.c_int),
+    "pbte_arnoldi_column_f32": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, _vp,
+                                 ctypes.c_int64, _vp], ctypes.c_int),
     "pbte_hot_source": ([_vp, _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],

@@ -149,7 +149,7 @@ class ArnoldiGraphs:
         self.w = torch.zeros(n, dtype=dtype, device=dev)
         self.tmp = torch.zeros(n, **f64)
         self.h = torch.zeros(m_cap + 2, **f64)
-        self.scratch = torch.zeros(610 * 64, **f64)   # pbte_cgs2 block partials and ticket
+        self.scratch = torch.zeros(_lib.CGS2_SCRATCH, **f64)   # block partials and ticket
         self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
         self.g = None if g is None else g.detach().clone()
         self.graphs = {}
@@ -166,14 +166,12 @@ class ArnoldiGraphs:
         Qj = self.Q[:j + 1]
         op.uin[:n].copy_(qj)
         op._launch(torch.cuda.current_stream().cuda_stream)
-        if self.g is not None:
-            torch.sub(op.uout[:n], self.g, out=self.tmp)
-            torch.sub(qj, self.tmp, out=self.w)
-        else:
-            torch.sub(qj, op.uout[:n], out=self.w)
-        fn = _lib.lib().pbte_cgs2_f32 if self.dtype == torch.float32 else _lib.lib().pbte_cgs2
-        _lib.check(fn(Qj.data_ptr(), self.Q.stride(0), j + 1, self.w.data_ptr(), n, self.h.data_ptr(),
-                      self.scratch.data_ptr(), torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
+        L = _lib.lib()
+        fn = L.pbte_arnoldi_column_f32 if self.dtype == torch.float32 else L.pbte_arnoldi_column
+        g = self.g.data_ptr() if self.g is not None else None
+        _lib.check(fn(Qj.data_ptr(), self.Q.stride(0), j + 1, op.uout.data_ptr(), g, self.w.data_ptr(), n,
+                      self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(),
+                      torch.cuda.current_stream().cuda_stream), "pbte_arnoldi_column")
 
     def column(self, j: int) -> np.ndarray:
         if j not in self.graphs:

@@ -37,6 +37,9 @@ extern "C" {
 #define PBTE_ERR_SINGULAR (-6)     /* singular element operator(s)           */
 #define PBTE_ERR_NOMEM (-7)        /* device allocation failed               */
 
+/* doubles of scratch a pbte_cgs2 / pbte_arnoldi_column call needs */
+#define PBTE_CGS2_SCRATCH (1220 * 64)
+
 /* precision of the sweep arithmetic */
 #define PBTE_FP64 0
 #define PBTE_FP32 1
@@ -183,16 +186,29 @@ int pbte_residual_check(pbte_ctx *ctx, const double *res, double tol, int64_t tm
  * (row stride ldq elements), in place on w, as in gmres_full
  * (pybte/krylov.py:201-210): h[0..rows-1] = c1 + c2 and h[rows] = ||w||.
  * Deterministic (block partial sums added in a fixed order).  `scratch`
- * holds 307 * 64 doubles, all zero before its first use; a call leaves it
- * ready for the next one, and concurrent calls need separate scratch.
+ * holds scratch_len >= PBTE_CGS2_SCRATCH doubles (PBTE_ERR_ARG otherwise),
+ * all zero before its first use; a call leaves it ready for the next one,
+ * and concurrent calls need separate scratch.
  * rows <= 64.  pbte_cgs2 keeps the basis and w in FP64; pbte_cgs2_f32 keeps
  * them in FP32 (FP32 products and warp sums, FP64 block and cross-block
  * sums; no reference counterpart: the inner solve of the mixed-precision
  * mode, whose operator is an FP32 sweep). */
 int pbte_cgs2(const double *Q, int64_t ldq, int32_t rows, double *w, int64_t n, double *h,
-              double *scratch, void *stream);
+              double *scratch, int64_t scratch_len, void *stream);
 int pbte_cgs2_f32(const float *Q, int64_t ldq, int32_t rows, float *w, int64_t n, double *h,
-                  double *scratch, void *stream);
+                  double *scratch, int64_t scratch_len, void *stream);
+
+/* One Arnoldi column after the product F(q_j) is in uout (the operator's
+ * output, FP64, first n entries): w = q_j - (uout - g) with q_j = Q[rows-1]
+ * (g may be NULL: w = q_j - uout), then the CGS2 of pbte_cgs2 /
+ * pbte_cgs2_f32 -- gmres_full's product and orthogonalisation
+ * (pybte/krylov.py:195-210) in three launches. */
+int pbte_arnoldi_column(const double *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
+                        double *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
+                        void *stream);
+int pbte_arnoldi_column_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout,
+                            const double *g, float *w, int64_t n, double *h, double *scratch,
+                            int64_t scratch_len, void *stream);
 
 /* GSIS per-iteration kernels (pybte/acceleration/):
  * third-order moment source, hot_source.py:29-58 -> work[n_tris][7*ndof];

@@ -43,3 +43,17 @@ def test_case_desc_matches_header_field_count():
     n = sum(len(re.findall(r"\*?\s*(\w+)\s*[,;]", line)) for line in decl.splitlines()
             if re.match(r"\s*(const\s+)?(int32_t|double)", line))
     assert n == len(_lib.CaseDesc._fields_)
+
+
+def test_cgs2_rejects_short_scratch_on_the_host():
+    """An undersized CGS2 scratch is refused before any launch (PBTE_ERR_ARG),
+    so this runs without a GPU."""
+    L = _lib.lib()
+    buf = (ctypes.c_double * 16)()
+    p = ctypes.cast(buf, ctypes.c_void_p)
+    short = _lib.CGS2_SCRATCH - 1
+    assert f"PBTE_CGS2_SCRATCH ({_lib.CGS2_SCRATCH // 64} * 64)" in HEADER.read_text()
+    for fn in (L.pbte_cgs2, L.pbte_cgs2_f32):
+        assert fn(p, 4, 1, p, 4, p, p, short, None) == -1
+    for fn in (L.pbte_arnoldi_column, L.pbte_arnoldi_column_f32):
+        assert fn(p, 4, 1, p, None, p, 4, p, p, short, None) == -1

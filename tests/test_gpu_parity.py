@@ -225,17 +225,46 @@ def test_cgs2_matches_two_pass_gram_schmidt(cuda, rows, f32):
     w1 = w - Q.T @ c1
     c2 = Q @ w1
     w2 = w1 - Q.T @ c2
-    scr = torch.zeros(610 * 64, dtype=torch.float64, device="cuda")
+    scr = torch.zeros(_lib.CGS2_SCRATCH, dtype=torch.float64, device="cuda")
     fn = _lib.lib().pbte_cgs2_f32 if f32 else _lib.lib().pbte_cgs2
     tol = 2e-5 if f32 else 1e-12
     for _ in range(2):
         Qd = torch.from_numpy(Q).to("cuda", dt)
         wd = torch.from_numpy(w).to("cuda", dt)
         h = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
-        _lib.check(fn(Qd.data_ptr(), n, rows, wd.data_ptr(), n, h.data_ptr(), scr.data_ptr(),
+        _lib.check(fn(Qd.data_ptr(), n, rows, wd.data_ptr(), n, h.data_ptr(), scr.data_ptr(), scr.numel(),
                       torch.cuda.current_stream().cuda_stream), "pbte_cgs2")
         hh = h.cpu().numpy()
         scale = np.linalg.norm(w)
         assert np.abs(hh[:rows] - (c1 + c2)).max() <= tol * scale
         assert hh[rows] == pytest.approx(np.linalg.norm(w2), rel=tol, abs=tol * scale)
         assert np.abs(wd.double().cpu().numpy() - w2).max() <= tol * scale
+
+
+@pytest.mark.parametrize("f32", [False, True])
+@pytest.mark.parametrize("with_g", [False, True])
+def test_arnoldi_column_forms_product_then_cgs2(cuda, f32, with_g):
+    """pbte_arnoldi_column(_f32): w = q_j - (uout - g), then CGS2 -- the same
+    numbers as the separate subtraction followed by pbte_cgs2(_f32)."""
+    from pbte_gb300 import _lib
+    rng = np.random.default_rng(7)
+    n, rows = 50_001, 12
+    dt = torch.float32 if f32 else torch.float64
+    Q = torch.from_numpy(np.linalg.qr(rng.standard_normal((n, rows)))[0].T.copy()).to("cuda", dt)
+    uout = torch.from_numpy(rng.standard_normal(n + 7)).cuda()
+    g = torch.from_numpy(rng.standard_normal(n)).cuda() if with_g else None
+    L = _lib.lib()
+    s = torch.cuda.current_stream().cuda_stream
+    w_ref = (Q[rows - 1].double() - (uout[:n] - g if with_g else uout[:n])).to(dt)
+    h_ref = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
+    scr = torch.zeros(_lib.CGS2_SCRATCH, dtype=torch.float64, device="cuda")
+    cg = L.pbte_cgs2_f32 if f32 else L.pbte_cgs2
+    _lib.check(cg(Q.data_ptr(), n, rows, w_ref.data_ptr(), n, h_ref.data_ptr(), scr.data_ptr(), scr.numel(), s),
+               "cgs2")
+    w = torch.zeros(n, dtype=dt, device="cuda")
+    h = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
+    ac = L.pbte_arnoldi_column_f32 if f32 else L.pbte_arnoldi_column
+    _lib.check(ac(Q.data_ptr(), n, rows, uout.data_ptr(), g.data_ptr() if with_g else None, w.data_ptr(), n,
+                  h.data_ptr(), scr.data_ptr(), scr.numel(), s), "arnoldi_column")
+    assert torch.equal(w, w_ref)
+    assert torch.equal(h, h_ref)
