@@ -22,6 +22,7 @@ import numpy as np
 import torch
 
 from . import _lib
+from .device import sync
 
 __all__ = ["FixedPointOperator", "gmres", "run_krylov"]
 
@@ -90,17 +91,16 @@ class FixedPointOperator:
     def _capture(self):
         torch.cuda.synchronize(self.s.device)
         g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=self.stream):
+        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
             self._launch(torch.cuda.current_stream().cuda_stream)
         self.graph = g
 
     def apply(self, u: torch.Tensor) -> torch.Tensor:
+        """F(u), stream-ordered on the current stream."""
         if self.graph is None:
             self._capture()
         self.uin[:self.n].copy_(u)
-        torch.cuda.current_stream().synchronize()
         self.graph.replay()
-        self.stream.synchronize()
         self.sweeps += 1
         return self.uout[:self.n].clone()
 
@@ -147,7 +147,6 @@ class ArnoldiGraphs:
         self.dtype = dtype
         self.Q = torch.zeros((m_cap + 1, n), dtype=dtype, device=dev)
         self.w = torch.zeros(n, dtype=dtype, device=dev)
-        self.tmp = torch.zeros(n, **f64)
         self.h = torch.zeros(m_cap + 2, **f64)
         self.scratch = torch.zeros(_lib.CGS2_SCRATCH, **f64)   # block partials and ticket
         self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
@@ -173,13 +172,23 @@ class ArnoldiGraphs:
                       self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(),
                       torch.cuda.current_stream().cuda_stream), "pbte_arnoldi_column")
 
+    def _capture(self, j: int) -> None:
+        torch.cuda.synchronize(self.op.s.device)
+        gr = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(gr, stream=self.stream, capture_error_mode="thread_local"):
+            self._record(j)
+        self.graphs[j] = gr
+
+    def capture_all(self) -> None:
+        """Capture every column's graph now (capturing synchronises the
+        device, which concurrent solves should not meet mid-run)."""
+        for j in range(self.m_cap):
+            if j not in self.graphs:
+                self._capture(j)
+
     def column(self, j: int) -> np.ndarray:
         if j not in self.graphs:
-            torch.cuda.synchronize(self.op.s.device)
-            gr = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(gr, stream=self.stream):
-                self._record(j)
-            self.graphs[j] = gr
+            self._capture(j)
         self.graphs[j].replay()
         self.h_host[:j + 2].copy_(self.h[:j + 2], non_blocking=True)
         torch.cuda.current_stream().synchronize()
@@ -374,7 +383,7 @@ def run_krylov(solver):
         residuals.append(np.nan)
         return out
 
-    torch.cuda.synchronize(solver.device)
+    sync(solver.device)
     t0 = time.perf_counter()
     zero = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
     g = sweep(zero)
@@ -423,7 +432,7 @@ def run_krylov(solver):
         if converged or len(residuals) >= tmax:
             break
         target = max(target * 1.0e-3, _FLOOR * scale)
-    torch.cuda.synchronize(solver.device)
+    sync(solver.device)
     wall = time.perf_counter() - t0
     solver.ctx.sweep_count += op.sweeps
     masses = [solver.mom.mass] * len(residuals)

@@ -26,6 +26,7 @@ import torch
 
 from . import _lib
 from .config import Case
+from .device import sync
 from .discretisation import Discretisation
 from .sweep import Moments, SweepContext
 
@@ -92,6 +93,15 @@ class Solver:
         torch.cuda.synchronize(self.device)
         self.setup_seconds = time.perf_counter() - t0
 
+    def reset(self) -> None:
+        """Back to the zero initial state of a fresh solve (on the current
+        stream)."""
+        self.vdf.zero_()
+        for k in ("ts", "qxs", "qys", "temp", "qx", "qy"):
+            getattr(self.mom, k).zero_()
+        self.t_old.zero_()
+        self.ctx.flux_wall.zero_()
+
     # -- one outer iteration (pybte/driver.py:149-161) -----------------------
     def step(self, stream=None) -> None:
         if self.bcdata.has_nonthermalising:
@@ -142,7 +152,7 @@ class Solver:
         _lib.check(L.pbte_set_done_flag(self.ctx.handle, done.data_ptr()), "set_done_flag")
         K = max(1, min(self.graph_block, int(tmax)))
         stream = torch.cuda.Stream(device=dev)
-        torch.cuda.synchronize(dev)
+        sync(dev)
         t0 = time.perf_counter()
         try:
             g = torch.cuda.CUDAGraph()
@@ -157,7 +167,7 @@ class Solver:
                     break
         finally:
             _lib.check(L.pbte_set_done_flag(self.ctx.handle, None), "set_done_flag")
-        torch.cuda.synchronize(dev)
+        sync(dev)
         wall = time.perf_counter() - t0
         n = int(count.item())
         flag = int(done.item())
@@ -171,7 +181,7 @@ class Solver:
         tol, tmax = c.iteration.tol, c.iteration.tmax
         L = _lib.lib()
         residuals, masses = [], []
-        torch.cuda.synchronize(self.device)
+        sync(self.device)
         t0 = time.perf_counter()
         step, converged = 0, False
         s = torch.cuda.current_stream().cuda_stream
@@ -188,7 +198,7 @@ class Solver:
                 break
             if step >= tmax:
                 break
-        torch.cuda.synchronize(self.device)
+        sync(self.device)
         wall = time.perf_counter() - t0
         return self._record(step, converged, np.array(residuals), np.array(masses), wall, scheme)
 

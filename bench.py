@@ -197,9 +197,9 @@ def main():
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    from pbte_gb300.replicas import barrier as rank_barrier, max_over_ranks, rank_info, replica_throughput
+    info = rank_info()
+    world, rank, local = info.world, info.rank, info.local
     if args.impl == "reference":
         return run_reference(args, world, rank)
 
@@ -220,14 +220,10 @@ def main():
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
     def reset(s):
-        s.vdf.zero_()
-        for k in ("ts", "qxs", "qys", "temp", "qx", "qy"):
-            getattr(s.mom, k).zero_()
-        s.ctx.flux_wall.zero_()
+        s.reset()
 
     def barrier():
-        if dist is not None:
-            dist.barrier()
+        rank_barrier(dist)
         torch.cuda.synchronize(dev)
 
     def timed(pool, k, check=None):
@@ -253,14 +249,13 @@ def main():
         for k in range(args.steps):
             ms, rec = timed(solvers, k)
             times.append(ms)
-            launches += 5 * (rec.diagnostics["fp64_sweeps"] + rec.diagnostics["fp32_sweeps"])
+            # per FP32 Arnoldi column: sources, sweep, moments (2), wall flux,
+            # CGS2 (3); per FP64 product: sources, sweep, moments (2),
+            # element integrals, wall flux
+            launches += 8 * rec.diagnostics["fp32_sweeps"] + 6 * rec.diagnostics["fp64_sweeps"]
     clocks = clk.summary()
-    total = float(sum(times))
-    if dist is not None:
-        t = torch.tensor([total], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total = float(t.item())
-    value = world * args.steps / (total * 1e-3)
+    total = max_over_ranks(float(sum(times)), dist)
+    value = replica_throughput(args.steps, total * 1e-3, world)
 
     # FP64 drop-in on the same steps (reported beside the headline)
     t64 = []
@@ -268,6 +263,25 @@ def main():
         ms, _ = timed(fp64, k)
         t64.append(ms)
     fp64_rate = len(t64) / (sum(t64) * 1e-3)
+
+    # batched: two copies of each Kn case solved concurrently (one stream and
+    # host thread per solve, pbte_gb300.batch); same results as alone
+    from pbte_gb300.batch import BatchSolver
+    batch = BatchSolver(list(solvers.values()) + [Solver(make_case(kn), device=str(dev)) for kn in KN])
+    batch.prepare()
+    bt = []
+    for k in range(2):
+        flush.fill_(float(k))
+        barrier()
+        recs = batch.run()
+        if not all(r.converged for r in recs):
+            raise RuntimeError("a batched solve did not converge")
+        bt.append(batch.wall_clock)
+    batched = {"value": round(len(batch.solvers) * len(bt) / sum(bt), 4), "unit": "solves/s",
+               "solves_per_batch": len(batch.solvers), "ms_per_batch": round(1e3 * sum(bt) / len(bt), 3)}
+    for s in solvers.values():
+        s.ctx.set_groups(0, 0)
+    del batch
 
     # e2e: public API from host arrays -- context creation (H2D of the
     # operators + schedule), solve, fields back to host
@@ -308,7 +322,9 @@ def main():
                 "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                                "p99": round(float(np.percentile(lat, 99)), 3)},
                 "fp64": {"value": round(fp64_rate, 4), "unit": "solves/s",
-                         "speedup_mixed_over_fp64": round(value / world / fp64_rate, 3)},
+                         "speedup_mixed_over_fp64": round(value / world / fp64_rate, 3),
+                         "speedup_batched_mixed_over_fp64": round(batched["value"] / fp64_rate, 3)},
+                "batched": batched,
                 "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches)}
