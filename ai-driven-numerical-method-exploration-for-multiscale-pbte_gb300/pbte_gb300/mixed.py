@@ -33,7 +33,7 @@ __all__ = ["run_mixed", "MixedOptions"]
 class MixedOptions:
     refine_tol = 1e-11      # stop on ||r|| / ||F64(u)||
     inner_rtol = 1e-6       # inner relative accuracy per outer step (FP32 limits it to ~1e-6)
-    max_outer = 12
+    max_outer = 200         # outer steps (one inner GMRES cycle each by default)
     max_inner = 200_000
     #: inner GMRES restart cycles per outer step before handing back to the
     #: FP64 defect correction.  One cycle per outer step measured fastest on
@@ -69,6 +69,8 @@ def run_mixed(solver, opts: MixedOptions | None = None):
         history.append(rn / fn)
         if rn <= opts.refine_tol * fn:
             converged = True
+            break
+        if op64.sweeps + inner_sweeps >= c.iteration.tmax:
             break
         if method == "source":
             d = r.clone()
