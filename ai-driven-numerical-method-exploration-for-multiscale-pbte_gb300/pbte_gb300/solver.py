@@ -70,11 +70,12 @@ class RunRecord:
 class Solver:
     """Set up a case on the GPU and run it to convergence."""
 
-    def __init__(self, case: Case, device: str = "cuda", graph_block: int = 32):
+    def __init__(self, case: Case, device: str = "cuda", graph_block: int = 32,
+                 discretisation: Discretisation | None = None):
         t0 = time.perf_counter()
         self.case = case
         self.device = torch.device(device)
-        self.disc = Discretisation.build(case)
+        self.disc = discretisation if discretisation is not None else Discretisation.build(case)
         self.mesh, self.integrals, self.vel = self.disc.mesh, self.disc.integrals, self.disc.vel
         self.bcdata = self.disc.bcdata
         self.ndir, self.n_tris, self.ndof = self.disc.ndir, self.disc.n_tris, self.disc.ndof
@@ -90,7 +91,7 @@ class Solver:
         if case.scheme.accflag == 1:
             from .gsis import GSIS
             self.acc = GSIS(self)
-        torch.cuda.synchronize(self.device)
+        sync(self.device)
         self.setup_seconds = time.perf_counter() - t0
 
     def reset(self) -> None:
