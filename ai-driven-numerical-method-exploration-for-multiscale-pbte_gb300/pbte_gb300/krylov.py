@@ -22,12 +22,20 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import sync
+from .device import bury, device_lock, empty_graveyard, sync
 
 __all__ = ["FixedPointOperator", "gmres", "run_krylov"]
 
 _ENOUGH = 1.0e-2
 _FLOOR = 1.0e-14
+
+
+def uses_graphs(solver) -> bool:
+    """Products and Arnoldi columns replay captured CUDA graphs unless the
+    solver's ``use_graphs`` is False (then the same launches are issued
+    directly: no capture cost, for short-lived solves such as served
+    requests)."""
+    return getattr(solver, "use_graphs", True)
 
 
 class FixedPointOperator:
@@ -89,18 +97,26 @@ class FixedPointOperator:
                 _lib.check(L.pbte_wall_flux_f32(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux_f32")
 
     def _capture(self):
-        torch.cuda.synchronize(self.s.device)
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
-            self._launch(torch.cuda.current_stream().cuda_stream)
+        with device_lock:
+            empty_graveyard()
+            torch.cuda.synchronize(self.s.device)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+                self._launch(torch.cuda.current_stream().cuda_stream)
         self.graph = g
+
+    def __del__(self):
+        bury(getattr(self, "graph", None))
 
     def apply(self, u: torch.Tensor) -> torch.Tensor:
         """F(u), stream-ordered on the current stream."""
-        if self.graph is None:
-            self._capture()
         self.uin[:self.n].copy_(u)
-        self.graph.replay()
+        if uses_graphs(self.s):
+            if self.graph is None:
+                self._capture()
+            self.graph.replay()
+        else:
+            self._launch(torch.cuda.current_stream().cuda_stream)
         self.sweeps += 1
         return self.uout[:self.n].clone()
 
@@ -172,11 +188,16 @@ class ArnoldiGraphs:
                       self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(),
                       torch.cuda.current_stream().cuda_stream), "pbte_arnoldi_column")
 
+    def __del__(self):
+        bury(*getattr(self, "graphs", {}).values())
+
     def _capture(self, j: int) -> None:
-        torch.cuda.synchronize(self.op.s.device)
-        gr = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(gr, stream=self.stream, capture_error_mode="thread_local"):
-            self._record(j)
+        with device_lock:
+            empty_graveyard()
+            torch.cuda.synchronize(self.op.s.device)
+            gr = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(gr, stream=self.stream, capture_error_mode="thread_local"):
+                self._record(j)
         self.graphs[j] = gr
 
     def capture_all(self) -> None:
@@ -187,9 +208,12 @@ class ArnoldiGraphs:
                 self._capture(j)
 
     def column(self, j: int) -> np.ndarray:
-        if j not in self.graphs:
-            self._capture(j)
-        self.graphs[j].replay()
+        if uses_graphs(self.op.s):
+            if j not in self.graphs:
+                self._capture(j)
+            self.graphs[j].replay()
+        else:
+            self._record(j)
         self.h_host[:j + 2].copy_(self.h[:j + 2], non_blocking=True)
         torch.cuda.current_stream().synchronize()
         self.op.sweeps += 1

@@ -83,11 +83,16 @@ class Server:
     to drain."""
 
     def __init__(self, device: str = "cuda", hbm_budget: float = 150e9, slots: int = 4,
-                 ring_shape: tuple[int, int] | None = (4, 64), runner=None, estimator=None):
+                 ring_shape: tuple[int, int] | None = (4, 64), runner=None, estimator=None,
+                 use_graphs: bool = False):
         self.device = torch.device(device)
         self.budget = int(hbm_budget)
         self.slots = int(slots)
         self.ring_shape = ring_shape
+        # a served solve lives for one run: capturing a graph per Arnoldi
+        # column costs more than it saves, and each capture holds the
+        # device lock that the other requests' captures wait on
+        self.use_graphs = use_graphs
         # runner(case, disc) -> RunRecord and estimator(disc, case) -> bytes;
         # replaceable so the admission logic can be exercised without a GPU
         self.runner = runner or self._run_on_device
@@ -168,11 +173,14 @@ class Server:
         stream = torch.cuda.Stream(device=self.device)
         with torch.cuda.stream(stream):
             s = Solver(case, device=str(self.device), discretisation=disc)
+            s.use_graphs = self.use_graphs
             if self.ring_shape is not None:
                 s.ctx.set_groups(*self.ring_shape)
-            rec = s.run()
-            stream.synchronize()
-            del s
+            try:
+                rec = s.run()
+                stream.synchronize()
+            finally:
+                s.release()
         return rec
 
     def _solve(self, t: Ticket, disc: Discretisation) -> None:
@@ -260,7 +268,10 @@ def main(argv=None) -> int:
         for c in draw_cases(a.requests, a.seed, ints(a.grids), ints(a.degs), ints(a.ndirs), (lo, hi),
                             precision="fp64"):
             t1 = time.perf_counter()
-            Solver(c).run()
+            s = Solver(c)
+            s.use_graphs = srv.use_graphs
+            s.run()
+            s.release()
             lat.append(time.perf_counter() - t1)
         span = time.perf_counter() - t0
         out["serial_fp64"] = {"solves_per_s": len(lat) / span, "p50_ms": float(np.percentile(lat, 50) * 1e3),

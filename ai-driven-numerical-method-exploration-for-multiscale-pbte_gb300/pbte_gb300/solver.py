@@ -26,7 +26,7 @@ import torch
 
 from . import _lib
 from .config import Case
-from .device import sync
+from .device import bury, device_lock, empty_graveyard, sync
 from .discretisation import Discretisation
 from .sweep import Moments, SweepContext
 
@@ -94,6 +94,18 @@ class Solver:
         sync(self.device)
         self.setup_seconds = time.perf_counter() - t0
 
+    def release(self) -> None:
+        """Free the solver's device state now -- Krylov operators and their
+        graphs, the acceleration, the context -- under the device lock, so
+        nothing is destroyed while another thread captures a graph.  The
+        solver is unusable afterwards."""
+        with device_lock:
+            self.__dict__.pop("_krylov_cache", None)
+            self.acc = None
+            ctx = self.__dict__.pop("ctx", None)
+            del ctx
+            empty_graveyard()
+
     def reset(self) -> None:
         """Back to the zero initial state of a fresh solve (on the current
         stream)."""
@@ -155,19 +167,22 @@ class Solver:
         stream = torch.cuda.Stream(device=dev)
         sync(dev)
         t0 = time.perf_counter()
+        g = None
         try:
             g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, stream=stream):
-                s = torch.cuda.current_stream().cuda_stream
-                for _ in range(K):
-                    self._iteration(s, tol, tmax, done, count, hist, cap)
+            with device_lock:
+                empty_graveyard()
+                with torch.cuda.graph(g, stream=stream, capture_error_mode="thread_local"):
+                    s = torch.cuda.current_stream().cuda_stream
+                    for _ in range(K):
+                        self._iteration(s, tol, tmax, done, count, hist, cap)
             while True:
                 g.replay()
-                stream.synchronize()
                 if int(done.item()) != 0:
                     break
         finally:
             _lib.check(L.pbte_set_done_flag(self.ctx.handle, None), "set_done_flag")
+            bury(g)
         sync(dev)
         wall = time.perf_counter() - t0
         n = int(count.item())

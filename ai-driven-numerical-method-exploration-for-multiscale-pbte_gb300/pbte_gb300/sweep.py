@@ -20,9 +20,24 @@ import numpy as np
 import torch
 
 from . import _lib
+from .device import device_lock, empty_graveyard
 from .discretisation import Discretisation
 
 __all__ = ["SweepContext", "Moments", "device_ptr"]
+
+# contexts whose destruction waits for a moment outside graph captures
+_deferred: list = []
+
+
+def _destroy_deferred() -> None:
+    """Destroy the contexts queued by SweepContext.__del__ (caller holds
+    device_lock)."""
+    while _deferred:
+        h = _deferred.pop()
+        try:
+            _lib.lib().pbte_ctx_destroy(h)
+        except Exception:
+            pass
 
 
 def device_ptr(t) -> int:
@@ -120,7 +135,9 @@ class SweepContext:
                                  "tri_faces", "upwind_tri", "edge_map", "face_bc", "face_tri",
                                  "face_lfc", "bc_type", "bc_temp", "int_tri")))
         handle = ctypes.c_void_p()
-        with torch.cuda.device(self.device):
+        with device_lock, torch.cuda.device(self.device):
+            empty_graveyard()
+            _destroy_deferred()
             _lib.check(_lib.lib().pbte_ctx_create(ctypes.byref(desc), int(precompute),
                                                   ctypes.byref(handle)), "pbte_ctx_create")
         self._ctx = handle
@@ -139,11 +156,20 @@ class SweepContext:
     def __del__(self):
         h = getattr(self, "_ctx", None)
         if h is not None and h.value:
-            try:
-                _lib.lib().pbte_ctx_destroy(h)
-            except Exception:
-                pass
+            # destruction frees device memory (a device-wide synchronisation):
+            # not while this thread captures a graph or another thread holds
+            # the device lock; then it waits for the next context creation
+            _deferred.append(ctypes.c_void_p(h.value))
             self._ctx = ctypes.c_void_p()
+            try:
+                capturing = torch.cuda.is_current_stream_capturing()
+            except Exception:
+                capturing = True
+            if not capturing and device_lock.acquire(blocking=False):
+                try:
+                    _destroy_deferred()
+                finally:
+                    device_lock.release()
 
     @property
     def handle(self) -> ctypes.c_void_p:

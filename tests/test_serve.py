@@ -12,7 +12,8 @@ from pbte_gb300.serve import Server, draw_cases, estimate_device_bytes
 
 
 def _small(kn, deg=1, n=6, precision="mixed", dt=0.5):
-    return square_case(n, deg, 2, 4, tau_r=kn, tau_n=0.1 * kn, method="krylov", precision=precision,
+    # 4 x 8 ordinates: with 2 x 4 GMRES stalls on these walls in FP64 as well
+    return square_case(n, deg, 4, 8, tau_r=kn, tau_n=0.1 * kn, method="krylov", precision=precision,
                        krylov_restart=30, tol=1e-8, tmax=4000, t_west=dt, t_east=-dt)
 
 
@@ -87,6 +88,7 @@ def test_results_in_the_mix_equal_results_alone(cuda):
     for c in cases:
         s = Solver(c)
         alone.append(s.run())
+        s.release()
     srv = Server(hbm_budget=8e9, slots=3)
     tickets = [srv.submit(c) for c in cases]
     srv.close()
