@@ -24,7 +24,7 @@ one scaling away; the GPU sweep is built on that compact form.
 """
 from __future__ import annotations
 
-from dataclasses import dataclass
+from dataclasses import dataclass, field
 from math import factorial, sqrt
 
 import numpy as np
@@ -65,10 +65,8 @@ class Integrals:
     int_tri_tri_x: np.ndarray
     int_tri_tri_y: np.ndarray
     int_tri_fc: np.ndarray
-    int_tri_fc_fc: np.ndarray
     int_fc_fc: np.ndarray
     int_fc: np.ndarray
-    int_tri_tri_fc: np.ndarray
     # compact form -------------------------------------------------------
     ref_mass: np.ndarray      # (nd, nd)
     ref_dx: np.ndarray        # (nd, nd)  int d_xi(phi_M) phi_L
@@ -78,6 +76,33 @@ class Integrals:
     dxi: np.ndarray           # (n_tris, 2)  d(xi)/dx, d(eta)/dx
     deta: np.ndarray          # (n_tris, 2)  d(xi)/dy, d(eta)/dy
     edge_scale: np.ndarray    # (n_tris, 3)  len12, len23/sqrt2, len31
+    # the two quadrature-built cross-space tensors, computed on first use: the
+    # GPU sweep needs only the compact form, and these take ~90 % of the setup
+    _face_fn: object = field(default=None, repr=False)
+    _face: dict = field(default_factory=dict, repr=False)
+
+    def _faces(self, k: int) -> np.ndarray:
+        if k not in self._face:
+            ff, tt = self._face_fn()
+            self._face.setdefault(0, ff)
+            self._face.setdefault(1, tt)
+        return self._face[k]
+
+    @property
+    def int_tri_fc_fc(self) -> np.ndarray:
+        return self._faces(0)
+
+    @int_tri_fc_fc.setter
+    def int_tri_fc_fc(self, v: np.ndarray) -> None:
+        self._face[0] = v
+
+    @property
+    def int_tri_tri_fc(self) -> np.ndarray:
+        return self._faces(1)
+
+    @int_tri_tri_fc.setter
+    def int_tri_tri_fc(self, v: np.ndarray) -> None:
+        self._face[1] = v
 
 
 def _eval_points(basis: Basis, nodes, tri_nodes_rows, xp, yp):
@@ -153,7 +178,21 @@ def build_integrals(mesh: Mesh, basis: Basis, np_fc: int = 15, bc_codes=None,
     int_fc_fc = ref_fc_fc[:, :, None] * half[None, None, :]
     int_fc = ref_fc[:, None] * half[None, :]
 
-    # numerical face tensors ---------------------------------------------
+    def faces():
+        return _face_tensors(mesh, basis, np_fc, bc_codes, bc_xoff, bc_yoff, chunk)
+
+    return Integrals(int_tri=int_tri, int_tri_tri=int_tri_tri, int_tri_tri_x=int_tri_tri_x,
+                     int_tri_tri_y=int_tri_tri_y, int_tri_fc=int_tri_fc,
+                     int_fc_fc=int_fc_fc, int_fc=int_fc, ref_mass=ref_mass, ref_dx=ref_dx,
+                     ref_dy=ref_dy, ref_edge=ref_edge, area2=area2, dxi=dxi, deta=deta,
+                     edge_scale=edge_scale, _face_fn=faces)
+
+
+def _face_tensors(mesh: Mesh, basis: Basis, np_fc, bc_codes, bc_xoff, bc_yoff, chunk):
+    """``int_tri_fc_fc`` and ``int_tri_tri_fc`` by the 15-point face rule."""
+    nd, nf = basis.ndof_tri, basis.ndof_fc
+    nodes = mesh.nodes
+    n_tris = mesh.n_tris
     bc_codes = np.asarray(bc_codes if bc_codes is not None else [], dtype=np.int64)
     bc_xoff = np.asarray(bc_xoff if bc_xoff is not None else np.zeros(bc_codes.size), dtype=float)
     bc_yoff = np.asarray(bc_yoff if bc_yoff is not None else np.zeros(bc_codes.size), dtype=float)
@@ -203,9 +242,4 @@ def build_integrals(mesh: Mesh, basis: Basis, np_fc: int = 15, bc_codes=None,
                 v = np.einsum("kqm,kq->km", pm[wall], w[wall])
                 int_tri_tri_fc[ids[wall], j2] = v[:, :, None]
 
-    return Integrals(int_tri=int_tri, int_tri_tri=int_tri_tri, int_tri_tri_x=int_tri_tri_x,
-                     int_tri_tri_y=int_tri_tri_y, int_tri_fc=int_tri_fc,
-                     int_tri_fc_fc=int_tri_fc_fc, int_fc_fc=int_fc_fc, int_fc=int_fc,
-                     int_tri_tri_fc=int_tri_tri_fc, ref_mass=ref_mass, ref_dx=ref_dx,
-                     ref_dy=ref_dy, ref_edge=ref_edge, area2=area2, dxi=dxi, deta=deta,
-                     edge_scale=edge_scale)
+    return int_tri_fc_fc, int_tri_tri_fc
