@@ -185,9 +185,12 @@ __global__ void __launch_bounds__(kT) cgs2_pass_kernel(const V *__restrict__ Q, 
                                                        double *scratch, double *out, const double *add,
                                                        double *out_plus, const V *__restrict__ qj,
                                                        const double *__restrict__ uout,
-                                                       const double *__restrict__ g) {
+                                                       const double *__restrict__ g, const int32_t *done) {
     __shared__ double wsum[kWarps][kMaxRows];
     __shared__ V csh[kMaxRows];
+    // a device-side stop flag set by an earlier launch: every block returns
+    // before touching the ticket, which therefore stays at zero
+    if (done != nullptr && *(volatile const int32_t *)done != 0) return;
     const Scratch S = scratch_of(scratch);
     const int nrow = MODE == 2 ? 1 : rows;
     for (int i = threadIdx.x; i < kWarps * kMaxRows; i += kT) (&wsum[0][0])[i] = 0.0;
@@ -247,9 +250,10 @@ __global__ void __launch_bounds__(kT) cgs2_pass_kernel(const V *__restrict__ Q, 
 
 // uout == nullptr: CGS2 of w in place.  Otherwise pass 1 first forms
 // w = Q[rows-1] - (uout - g) (the Arnoldi product of the newest basis vector).
+// done (optional): every launch returns at once while *done != 0.
 template <typename V>
 int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
-         const double *uout, const double *g, void *stream) {
+         const double *uout, const double *g, const int32_t *done, void *stream) {
     if (!Q || !w || !h || !scratch || rows < 1 || rows > kMaxRows || n < 1 || ldq < n) return PBTE_ERR_ARG;
     if (scratch_len < PBTE_CGS2_SCRATCH) return PBTE_ERR_ARG;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -258,11 +262,73 @@ int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, doub
     const long long nchunk = (n + (long long)kT * kE - 1) / ((long long)kT * kE);
     const int nb = (int)std::min<long long>(nchunk, kMaxBlocks);
     cgs2_pass_kernel<V, 0><<<nb, kT, 0, s>>>(Q, ldq, rows, w, nullptr, n, scratch, S.c1, nullptr, nullptr, qj,
-                                             uout, g);
+                                             uout, g, done);
     cgs2_pass_kernel<V, 1><<<nb, kT, 0, s>>>(Q, ldq, rows, w, S.c1, n, scratch, S.c2, S.c1, h,   // h = c1 + c2
-                                             nullptr, nullptr, nullptr);
+                                             nullptr, nullptr, nullptr, done);
     cgs2_pass_kernel<V, 2><<<nb, kT, 0, s>>>(Q, ldq, rows, w, S.c2, n, scratch, h + rows, nullptr, nullptr,
-                                             nullptr, nullptr, nullptr);
+                                             nullptr, nullptr, nullptr, done);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+// Column j of a restart cycle on the device (gmres_full's host loop,
+// pybte/krylov.py:211-235): the earlier rotations applied to the Hessenberg
+// column h[0..j+1], the new rotation from hypot(h_j, h_j+1), the column of
+// R, the residual estimates gam, and the stop state: state[0] = 1 when
+// |gam[j+1]| <= *tol_abs, 2 when h[j+1] == 0 (breakdown), state[1] = columns
+// done, hist[j] = |gam[j+1]|.  One thread; nothing runs once state[0] != 0.
+__global__ void gmres_givens_kernel(int j, const double *h, double *R, int ldr, double *cs, double *sn,
+                                    double *gam, const double *tol_abs, int32_t *state, double *hist) {
+    if (threadIdx.x != 0 || state[0] != 0) return;
+    double col[kMaxRows + 1];
+    for (int i = 0; i <= j + 1; ++i) col[i] = h[i];
+    const double hn = col[j + 1];
+    for (int i = 0; i < j; ++i) {
+        const double t = cs[i] * col[i] + sn[i] * col[i + 1];
+        col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
+        col[i] = t;
+    }
+    const double d = hypot(col[j], col[j + 1]);
+    double c = 1.0, s = 0.0;
+    if (d != 0.0) {
+        c = col[j] / d;
+        s = col[j + 1] / d;
+    }
+    cs[j] = c;
+    sn[j] = s;
+    col[j] = d;
+    for (int i = 0; i <= j; ++i) R[(size_t)j * ldr + i] = col[i];
+    gam[j + 1] = -s * gam[j];
+    gam[j] = c * gam[j];
+    const double res = fabs(gam[j + 1]);
+    hist[j] = res;
+    state[1] = j + 1;
+    if (res <= *tol_abs) state[0] = 1;
+    else if (hn == 0.0) state[0] = 2;
+}
+
+// q_{j+1} = w / h[j+1] into row j+1 of the basis, and widened into the
+// operator's FP64 input for the next product; nothing once state[0] != 0.
+template <typename V>
+__global__ void gmres_next_basis_kernel(int j, const V *__restrict__ w, const double *__restrict__ h,
+                                        V *__restrict__ Q, long long ldq, double *__restrict__ uin, long long n,
+                                        const int32_t *state) {
+    if (*(volatile const int32_t *)state != 0) return;
+    const V hn = (V)h[j + 1];
+    V *q = Q + (size_t)(j + 1) * ldq;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const V v = w[t] / hn;
+        q[t] = v;
+        uin[t] = (double)v;
+    }
+}
+
+template <typename V>
+int next_basis(int32_t j, const V *w, const double *h, V *Q, int64_t ldq, double *uin, int64_t n,
+               const int32_t *state, void *stream) {
+    if (j < 0 || j + 1 >= kMaxRows || !w || !h || !Q || !uin || !state || n < 1 || ldq < n) return PBTE_ERR_ARG;
+    const int th = 256;
+    const int bl = (int)std::min<long long>((n + th - 1) / th, 152 * 8);
+    gmres_next_basis_kernel<V><<<bl, th, 0, reinterpret_cast<cudaStream_t>(stream)>>>(j, w, h, Q, ldq, uin, n, state);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
@@ -273,26 +339,46 @@ int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, doub
 // rows <= 64.
 extern "C" int pbte_cgs2(const double *Q, int64_t ldq, int32_t rows, double *w, int64_t n, double *h,
                          double *scratch, int64_t scratch_len, void *stream) {
-    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, scratch_len, nullptr, nullptr, stream);
+    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, scratch_len, nullptr, nullptr, nullptr, stream);
 }
 
 extern "C" int pbte_cgs2_f32(const float *Q, int64_t ldq, int32_t rows, float *w, int64_t n, double *h,
                              double *scratch, int64_t scratch_len, void *stream) {
-    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, nullptr, nullptr, stream);
+    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, nullptr, nullptr, nullptr, stream);
 }
 
 extern "C" int pbte_arnoldi_column(const double *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
                                    double *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
-                                   void *stream) {
+                                   const int32_t *done, void *stream) {
     if (!uout) return PBTE_ERR_ARG;
-    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, stream);
+    return cgs2<double>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, done, stream);
 }
 
 extern "C" int pbte_arnoldi_column_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout,
                                        const double *g, float *w, int64_t n, double *h, double *scratch,
-                                       int64_t scratch_len, void *stream) {
+                                       int64_t scratch_len, const int32_t *done, void *stream) {
     if (!uout) return PBTE_ERR_ARG;
-    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, stream);
+    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, done, stream);
+}
+
+extern "C" int pbte_gmres_givens(int32_t j, const double *h, double *R, int32_t ldr, double *cs, double *sn,
+                                 double *gam, const double *tol_abs, int32_t *state, double *hist, void *stream) {
+    if (j < 0 || j + 1 >= kMaxRows + 1 || ldr < j + 1 || !h || !R || !cs || !sn || !gam || !tol_abs || !state ||
+        !hist)
+        return PBTE_ERR_ARG;
+    gmres_givens_kernel<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>(j, h, R, ldr, cs, sn, gam, tol_abs,
+                                                                              state, hist);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+extern "C" int pbte_gmres_next_basis(int32_t j, const double *w, const double *h, double *Q, int64_t ldq,
+                                     double *uin, int64_t n, const int32_t *state, void *stream) {
+    return next_basis<double>(j, w, h, Q, ldq, uin, n, state, stream);
+}
+
+extern "C" int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float *Q, int64_t ldq,
+                                         double *uin, int64_t n, const int32_t *state, void *stream) {
+    return next_basis<float>(j, w, h, Q, ldq, uin, n, state, stream);
 }
 
 static_assert((size_t)kMaxBlocks * kMaxRows + 3 * kMaxRows <= PBTE_CGS2_SCRATCH, "scratch size");

@@ -115,9 +115,15 @@ _SIGS = {
     "pbte_cgs2_f32": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, ctypes.c_int64, _vp, _vp, ctypes.c_int64, _vp],
                       ctypes.c_int),
     "pbte_arnoldi_column": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, _vp,
-                             ctypes.c_int64, _vp], ctypes.c_int),
+                             ctypes.c_int64, _vp, _vp], ctypes.c_int),
     "pbte_arnoldi_column_f32": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, _vp,
-                                 ctypes.c_int64, _vp], ctypes.c_int),
+                                 ctypes.c_int64, _vp, _vp], ctypes.c_int),
+    "pbte_gmres_givens": ([ctypes.c_int32, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+                          ctypes.c_int),
+    "pbte_gmres_next_basis": ([ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp, _vp],
+                              ctypes.c_int),
+    "pbte_gmres_next_basis_f32": ([ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp, _vp],
+                                  ctypes.c_int),
     "pbte_hot_source": ([_vp, _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],

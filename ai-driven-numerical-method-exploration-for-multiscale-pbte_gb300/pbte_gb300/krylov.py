@@ -168,28 +168,125 @@ class ArnoldiGraphs:
         self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
         self.g = None if g is None else g.detach().clone()
         self.graphs = {}
+        self.cycle_graphs = None
         self.stream = torch.cuda.Stream(device=dev)
         self.on_product = None   # called after every product (sweep bookkeeping)
+        #: whole restart cycles on the device when no per-column host
+        #: callback is needed (the mixed path's inner solve)
+        self.device_cycles = True
 
     def set_g(self, g: torch.Tensor) -> None:
         self.g.copy_(g)
 
-    def _record(self, j: int) -> None:
+    def _record(self, j: int, done=None, fill_input: bool = True) -> None:
         op = self.op
         n = self.n
-        qj = self.Q[j]
         Qj = self.Q[:j + 1]
-        op.uin[:n].copy_(qj)
+        if fill_input:
+            op.uin[:n].copy_(self.Q[j])
         op._launch(torch.cuda.current_stream().cuda_stream)
         L = _lib.lib()
         fn = L.pbte_arnoldi_column_f32 if self.dtype == torch.float32 else L.pbte_arnoldi_column
         g = self.g.data_ptr() if self.g is not None else None
         _lib.check(fn(Qj.data_ptr(), self.Q.stride(0), j + 1, op.uout.data_ptr(), g, self.w.data_ptr(), n,
                       self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(),
+                      None if done is None else done.data_ptr(),
                       torch.cuda.current_stream().cuda_stream), "pbte_arnoldi_column")
 
     def __del__(self):
-        bury(*getattr(self, "graphs", {}).values())
+        bury(*getattr(self, "graphs", {}).values(), *(getattr(self, "cycle_graphs", None) or {}).values())
+
+    # -- whole restart cycles on the device ----------------------------------
+    #: columns per captured chunk of a cycle (the host checks the stop state
+    #: after each chunk)
+    CHUNK = 10
+
+    def _cycle_buffers(self) -> None:
+        if getattr(self, "cycle_graphs", None) is not None:
+            return
+        dev = self.op.s.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        m = self.m_cap
+        self.R = torch.zeros((m, m), **f64)          # row j: column j of the triangular factor
+        self.cs = torch.zeros(m, **f64)
+        self.sn = torch.zeros(m, **f64)
+        self.gam = torch.zeros(m + 1, **f64)
+        self.hist = torch.zeros(m, **f64)
+        self.tol = torch.zeros(1, **f64)
+        self.state = torch.zeros(4, dtype=torch.int32, device=dev)
+        self.state_host = torch.zeros(4, dtype=torch.int32, pin_memory=True)
+        self.cycle_graphs = {}
+
+    def _record_cycle(self, j0: int, j1: int) -> None:
+        """Columns j0..j1-1: product, CGS2, rotation, next basis vector; all
+        of it skipped once the stop state is set."""
+        L = _lib.lib()
+        s = torch.cuda.current_stream().cuda_stream
+        n, ctx = self.n, self.op.s.ctx.handle
+        _lib.check(L.pbte_set_done_flag(ctx, self.state.data_ptr()), "set_done_flag")
+        try:
+            for j in range(j0, j1):
+                self._record(j, done=self.state, fill_input=False)
+                _lib.check(L.pbte_gmres_givens(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap,
+                                               self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(),
+                                               self.tol.data_ptr(), self.state.data_ptr(), self.hist.data_ptr(),
+                                               s), "gmres_givens")
+                nb = L.pbte_gmres_next_basis_f32 if self.dtype == torch.float32 else L.pbte_gmres_next_basis
+                _lib.check(nb(j, self.w.data_ptr(), self.h.data_ptr(), self.Q.data_ptr(), self.Q.stride(0),
+                              self.op.uin.data_ptr(), n, self.state.data_ptr(), s), "gmres_next_basis")
+        finally:
+            _lib.check(L.pbte_set_done_flag(ctx, None), "set_done_flag")
+
+    def _chunk(self, j0: int, j1: int):
+        key = (j0, j1)
+        if key not in self.cycle_graphs:
+            if uses_graphs(self.op.s):
+                with device_lock:
+                    empty_graveyard()
+                    torch.cuda.synchronize(self.op.s.device)
+                    gr = torch.cuda.CUDAGraph()
+                    with torch.cuda.graph(gr, stream=self.stream, capture_error_mode="thread_local"):
+                        self._record_cycle(j0, j1)
+                self.cycle_graphs[key] = gr
+            else:
+                return None
+        return self.cycle_graphs[key]
+
+    def cycle(self, r: torch.Tensor, beta: float, m: int, tol_abs: float):
+        """One restart cycle of at most ``m`` columns from the residual ``r``
+        (norm ``beta``), stopping on the device when the residual estimate
+        reaches ``tol_abs`` or on breakdown.  Returns ``(k, state, R, gam,
+        hist)`` on the host: columns done, stop state (0 none, 1 converged,
+        2 breakdown), the k x k triangular factor, the k + 1 residual
+        estimates and the k residual norms."""
+        self._cycle_buffers()
+        n = self.n
+        torch.div(r, beta, out=self.Q[0])
+        self.op.uin[:n].copy_(self.Q[0])
+        self.gam.zero_()
+        self.gam[0] = beta
+        self.tol.fill_(tol_abs)
+        self.state.zero_()
+        for j0 in range(0, m, self.CHUNK):
+            j1 = min(m, j0 + self.CHUNK)
+            g = self._chunk(j0, j1)
+            if g is not None:
+                g.replay()
+            else:
+                self._record_cycle(j0, j1)
+            self.state_host.copy_(self.state, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            if int(self.state_host[0]) != 0:
+                break
+        k = int(self.state_host[1])
+        R = self.R[:k, :k].cpu().numpy().T.copy()
+        gam = self.gam[:k + 1].cpu().numpy()
+        hist = self.hist[:k].cpu().numpy()
+        self.op.sweeps += k
+        if self.on_product is not None:
+            for _ in range(k):
+                self.on_product()
+        return k, int(self.state_host[0]), R, gam, hist
 
     def _capture(self, j: int) -> None:
         with device_lock:
@@ -202,10 +299,15 @@ class ArnoldiGraphs:
 
     def capture_all(self) -> None:
         """Capture every column's graph now (capturing synchronises the
-        device, which concurrent solves should not meet mid-run)."""
+        device, which concurrent solves should not meet mid-run): the
+        per-column graphs and the chunks of a full device cycle."""
         for j in range(self.m_cap):
             if j not in self.graphs:
                 self._capture(j)
+        if self.device_cycles:
+            self._cycle_buffers()
+            for j0 in range(0, self.m_cap, self.CHUNK):
+                self._chunk(j0, min(self.m_cap, j0 + self.CHUNK))
 
     def column(self, j: int) -> np.ndarray:
         if uses_graphs(self.op.s):
@@ -312,9 +414,40 @@ def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, 
     return x, converged, nmv
 
 
+def _gmres_cycles(matvec, b, x, tol_abs, maxiter, m_cap, ar: ArnoldiGraphs):
+    """The loop of :func:`gmres` with whole restart cycles on the device
+    (:meth:`ArnoldiGraphs.cycle`): the rotations and the stopping test run
+    after each column on the device, the host sees the cycle's end.  Same
+    Krylov arithmetic; the rotations use the device's hypot."""
+    nmv = 0
+    converged = False
+    while nmv < maxiter and not converged:
+        if bool(torch.any(x != 0).item()):
+            r = b - matvec(x)
+            nmv += 1
+        else:
+            r = b.clone()
+        beta = float(torch.linalg.vector_norm(r).item())
+        if beta <= tol_abs:
+            converged = True
+            break
+        m = min(m_cap, maxiter - nmv)
+        if m <= 0:
+            break
+        k, state, rmat, gam, _ = ar.cycle(r, beta, m, tol_abs)
+        nmv += k
+        converged = state == 1
+        if k:
+            y = torch.from_numpy(_back_substitute(rmat, gam[:k])).to(device=b.device, dtype=ar.Q.dtype)
+            x += ar.Q[:k].T @ y
+    return x, converged, nmv
+
+
 def _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, ar: ArnoldiGraphs):
     """The loop of :func:`gmres` with the basis in ``ar.Q`` and every Arnoldi
     column from one graph replay; same arithmetic, same stopping."""
+    if callback is None and ar.device_cycles:
+        return _gmres_cycles(matvec, b, x, tol_abs, maxiter, m_cap, ar)
     nmv = 0
     converged = halted = False
     Q = ar.Q

@@ -202,13 +202,32 @@ int pbte_cgs2_f32(const float *Q, int64_t ldq, int32_t rows, float *w, int64_t n
  * output, FP64, first n entries): w = q_j - (uout - g) with q_j = Q[rows-1]
  * (g may be NULL: w = q_j - uout), then the CGS2 of pbte_cgs2 /
  * pbte_cgs2_f32 -- gmres_full's product and orthogonalisation
- * (pybte/krylov.py:195-210) in three launches. */
+ * (pybte/krylov.py:195-210) in three launches.  `done` (may be NULL): a
+ * device flag; while it is nonzero every launch returns at once. */
 int pbte_arnoldi_column(const double *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
                         double *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
-                        void *stream);
+                        const int32_t *done, void *stream);
 int pbte_arnoldi_column_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout,
                             const double *g, float *w, int64_t n, double *h, double *scratch,
-                            int64_t scratch_len, void *stream);
+                            int64_t scratch_len, const int32_t *done, void *stream);
+
+/* The host part of a GMRES column on the device, so that a restart cycle
+ * runs as captured launches without a host round trip per column
+ * (gmres_full, pybte/krylov.py:211-235): pbte_gmres_givens applies the
+ * earlier rotations to the Hessenberg column h[0..j+1], forms rotation j
+ * (hypot), stores column j of R at R[j*ldr + 0..j], updates the residual
+ * estimates gam, writes hist[j] = |gam[j+1]| and the state: state[0] = 1
+ * when |gam[j+1]| <= *tol_abs (a device scalar, so a captured cycle serves
+ * any tolerance), 2 on breakdown (h[j+1] == 0); state[1] =
+ * columns done.  pbte_gmres_next_basis(_f32) stores q_{j+1} = w / h[j+1] in
+ * row j+1 of Q and widened into the operator input uin[0..n).  Both do
+ * nothing while state[0] != 0; j + 1 < 64. */
+int pbte_gmres_givens(int32_t j, const double *h, double *R, int32_t ldr, double *cs, double *sn,
+                      double *gam, const double *tol_abs, int32_t *state, double *hist, void *stream);
+int pbte_gmres_next_basis(int32_t j, const double *w, const double *h, double *Q, int64_t ldq,
+                          double *uin, int64_t n, const int32_t *state, void *stream);
+int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float *Q, int64_t ldq,
+                              double *uin, int64_t n, const int32_t *state, void *stream);
 
 /* GSIS per-iteration kernels (pybte/acceleration/):
  * third-order moment source, hot_source.py:29-58 -> work[n_tris][7*ndof];

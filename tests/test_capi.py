@@ -56,4 +56,4 @@ def test_cgs2_rejects_short_scratch_on_the_host():
     for fn in (L.pbte_cgs2, L.pbte_cgs2_f32):
         assert fn(p, 4, 1, p, 4, p, p, short, None) == -1
     for fn in (L.pbte_arnoldi_column, L.pbte_arnoldi_column_f32):
-        assert fn(p, 4, 1, p, None, p, 4, p, p, short, None) == -1
+        assert fn(p, 4, 1, p, None, p, 4, p, p, short, None, None) == -1

@@ -195,6 +195,39 @@ def test_mixed_precision_reaches_fp64_fixed_point(cuda, method):
     assert rec.diagnostics["fp32_sweeps"] > rec.diagnostics["fp64_sweeps"]
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+def test_device_gmres_cycles_match_host_rotations(cuda, graphs):
+    """The mixed path's inner GMRES with whole restart cycles on the device
+    (rotations and stopping test in pbte_gmres_givens, basis update in
+    pbte_gmres_next_basis_f32, captured in chunks or launched directly)
+    against the same solve with the rotations on the host after every
+    column: the same fixed point to 1e-10 and the same sweep counts (the
+    two differ only in hypot's last bit)."""
+    from pbte_gb300 import mixed
+    from pbte_gb300.krylov import ArnoldiGraphs
+    base = dict(deg=2, npole=4, nazim=8, tau_r=0.2, tau_n=0.02, method="krylov", precision="mixed")
+    out = {}
+    for cycles in (True, False):
+        s = Solver(small_case(**base))
+        s.use_graphs = graphs
+        orig = ArnoldiGraphs.__init__
+
+        def init(self, *a, _c=cycles, **k):
+            orig(self, *a, **k)
+            self.device_cycles = _c
+        ArnoldiGraphs.__init__ = init
+        try:
+            out[cycles] = mixed.run_mixed(s)
+        finally:
+            ArnoldiGraphs.__init__ = orig
+        s.release()
+    a, b = out[True], out[False]
+    assert a.converged and b.converged
+    assert abs(a.diagnostics["fp32_sweeps"] - b.diagnostics["fp32_sweeps"]) <= 1
+    assert a.diagnostics["outer_steps"] == b.diagnostics["outer_steps"]
+    assert _rel(a.temp_dofs, b.temp_dofs) < 1e-10 and _rel(a.qx_dofs, b.qx_dofs) < 1e-10
+
+
 def test_square_benchmark_mesh_levels(cuda):
     s = Solver(square_case(64, 2, 8, 32, tau_r=1.0, tmax=3))
     assert s.n_tris == 8192
@@ -265,6 +298,6 @@ def test_arnoldi_column_forms_product_then_cgs2(cuda, f32, with_g):
     h = torch.zeros(rows + 1, dtype=torch.float64, device="cuda")
     ac = L.pbte_arnoldi_column_f32 if f32 else L.pbte_arnoldi_column
     _lib.check(ac(Q.data_ptr(), n, rows, uout.data_ptr(), g.data_ptr() if with_g else None, w.data_ptr(), n,
-                  h.data_ptr(), scr.data_ptr(), scr.numel(), s), "arnoldi_column")
+                  h.data_ptr(), scr.data_ptr(), scr.numel(), None, s), "arnoldi_column")
     assert torch.equal(w, w_ref)
     assert torch.equal(h, h_ref)
