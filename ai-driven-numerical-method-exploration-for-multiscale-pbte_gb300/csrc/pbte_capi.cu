@@ -36,6 +36,18 @@ int pbte_sweep_f32(pbte_ctx *c, const double *ts, const double *qxs, const doubl
     return pbte::launch_sweep32(c, vdf32, flux_wall, wall_scale, S(stream));
 }
 
+int pbte_fixed_point_f32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                         const double *flux_wall_in, double wall_scale, float *vdf32, double *ts_out,
+                         double *qxs_out, double *qys_out, double *flux_wall_out, double *temp, double *qx,
+                         double *qy, void *stream) {
+    if (!c || !ts || !qxs || !qys || !vdf32 || !ts_out || !qxs_out || !qys_out) return PBTE_ERR_ARG;
+    if (c->n_wall_ad && (!flux_wall_in || !flux_wall_out)) return PBTE_ERR_ARG;
+    if ((temp == nullptr) != (qx == nullptr) || (temp == nullptr) != (qy == nullptr)) return PBTE_ERR_ARG;
+    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
+    return pbte::launch_fixed_point32(c, ts, qxs, qys, flux_wall_in, wall_scale, vdf32, ts_out, qxs_out, qys_out,
+                                      flux_wall_out, temp, qx, qy, S(stream));
+}
+
 int pbte_moments(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys, double *temp,
                  double *qx, double *qy, void *stream) {
     if (!c || !vdf || !ts || !qxs || !qys) return PBTE_ERR_ARG;

@@ -86,7 +86,8 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_lvl_cells, c->d_int_tri, c->d_wall_ad, c->d_S64, c->d_S32, c->d_lu,
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
                     c->d_udir_rep, c->d_udir_twin, c->d_rf64, c->d_rf32, c->d_ri, c->d_mom_part,
-                    c->d_cx32, c->d_cy32, c->d_w32, c->d_udir_of};
+                    c->d_cx32, c->d_cy32, c->d_w32, c->d_udir_of, c->d_uw32, c->d_ucx32, c->d_ucy32,
+                    c->d_uw64, c->d_ucx64, c->d_ucy64};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -360,6 +361,22 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         if (utwin[u] >= 0) udir_of[utwin[u]] = u;
     }
     TRY(upload(udir_of.data(), udir_of.size(), &c->d_udir_of, &c->device_bytes));
+    {
+        // folded weights: a twin pair contributes w_a f + w_b f = (w_a + w_b) f
+        std::vector<double> uw(c->n_udir), ucx(c->n_udir), ucy(c->n_udir);
+        for (int u = 0; u < c->n_udir; ++u) {
+            uw[u] = d->domega[urep[u]] + (utwin[u] >= 0 ? d->domega[utwin[u]] : 0.0);
+            ucx[u] = d->cxv[urep[u]];
+            ucy[u] = d->cyv[urep[u]];
+        }
+        std::vector<float> uw32(uw.begin(), uw.end()), ucx32(ucx.begin(), ucx.end()), ucy32(ucy.begin(), ucy.end());
+        TRY(upload(uw.data(), uw.size(), &c->d_uw64, &c->device_bytes));
+        TRY(upload(ucx.data(), ucx.size(), &c->d_ucx64, &c->device_bytes));
+        TRY(upload(ucy.data(), ucy.size(), &c->d_ucy64, &c->device_bytes));
+        TRY(upload(uw32.data(), uw32.size(), &c->d_uw32, &c->device_bytes));
+        TRY(upload(ucx32.data(), ucx32.size(), &c->d_ucx32, &c->device_bytes));
+        TRY(upload(ucy32.data(), ucy32.size(), &c->d_ucy32, &c->device_bytes));
+    }
     TRY(upload(dir_class.data(), dir_class.size(), &c->d_dir_class, &c->device_bytes));
     TRY(upload(class_off.data(), class_off.size(), &c->d_class_lvl_off, &c->device_bytes));
     TRY(upload(class_nlev.data(), class_nlev.size(), &c->d_class_nlev, &c->device_bytes));

@@ -40,6 +40,7 @@ struct SweepParams {
     const double *lu;       // stored factors, factor_base() layout
     const int8_t *piv;
     const int32_t *udir_of; // ordinate -> distinct in-plane velocity (factor owner)
+    int store_twin;         // ring sweep: also store the z-mirror twin's copy (0: folded consumers)
     int32_t *singular;
     const int32_t *done;
     int nt, n_faces;

@@ -105,6 +105,9 @@ struct pbte_ctx {
     int32_t *d_udir_rep = nullptr, *d_udir_twin = nullptr;
     int32_t *d_udir_of = nullptr;   // [ndir]: the distinct velocity an ordinate belongs to
     int n_udir = 0;
+    // per distinct velocity, FP32: summed weight of the ordinate and its twin, cx, cy
+    float *d_uw32 = nullptr, *d_ucx32 = nullptr, *d_ucy32 = nullptr;
+    double *d_uw64 = nullptr, *d_ucx64 = nullptr, *d_ucy64 = nullptr;
     int sweep_variant = 0;          // 0 automatic, 1 level-serial, 2 ring pipeline
     int ring_groups = 0;            // thread groups of the ring pipeline (0: default)
     int ring_width = 0;             // threads per group of the ring pipeline (0: 64)
@@ -125,7 +128,13 @@ int launch_sources(pbte_ctx *c, const double *ts, const double *qxs, const doubl
 int launch_sweep64(pbte_ctx *c, double *vdf, const double *flux_wall, const double *pbuf,
                    int use_pbuf, cudaStream_t s);
 int launch_sweep32(pbte_ctx *c, float *vdf32, const double *flux_wall, double wall_scale,
-                   cudaStream_t s);
+                   cudaStream_t s, bool store_twin = true);
+// the FP32 fixed-point product with z-mirror twins folded (one copy per
+// in-plane velocity written and read): sources, sweep, moments, emission
+int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                         const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
+                         double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
+                         double *qy, cudaStream_t s);
 int launch_factorise(pbte_ctx *c, cudaStream_t s);
 int launch_moments64(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys,
                      double *temp, double *qx, double *qy, cudaStream_t s);

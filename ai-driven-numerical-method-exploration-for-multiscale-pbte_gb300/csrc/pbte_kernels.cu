@@ -356,6 +356,84 @@ __global__ void wall_flux_np_kernel(const T *vdf, const WallFace *walls, const C
 }
 
 
+// ---------------------------------------------------------------------------
+// Folded FP32 forms for the fixed-point product of the mixed path: z-mirror
+// twins see the same transport, so one row per distinct in-plane velocity u
+// (ordinate rep[u]) is read with the pair's summed weight uw[u].
+// ---------------------------------------------------------------------------
+
+__global__ void moments_partial_fold_kernel(const float *vdf, const int32_t *rep, const float *ucx,
+                                            const float *ucy, const float *uw, int nu, int total, double *part,
+                                            const int32_t *done) {
+    if (stopped(done)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ch = blockIdx.y;
+    if (t >= total) return;
+    const int u0 = ch * kMomChunk, u1 = min(nu, u0 + kMomChunk);
+    float a = 0.f, bx = 0.f, by = 0.f;
+#pragma unroll 8
+    for (int u = u0; u < u1; ++u) {
+        const float fw = vdf[(size_t)rep[u] * total + t] * uw[u];
+        a += fw;
+        bx += ucx[u] * fw;
+        by += ucy[u] * fw;
+    }
+    double *p = part + (size_t)ch * 3 * total;
+    p[t] = a;
+    p[total + t] = bx;
+    p[2 * total + t] = by;
+}
+
+// Adiabatic-wall emission, folded: one warp per wall face, distinct
+// velocities over lanes, FP32 products, FP64 sums reduced by shuffles in a
+// fixed order.
+template <int NP>
+__global__ void wall_flux_fold_kernel(const float *vdf, const WallFace *walls, int nwall, const CellRec<double> *cells,
+                                      const float *ref_edge, const int32_t *rep, const double *ucx, const double *ucy,
+                                      const double *uw, int nu, int nt, double *fw_out, const int32_t *done) {
+    if (stopped(done)) return;
+    const int lane = threadIdx.x % 32;
+    const int f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
+    if (f >= nwall) return;
+    const WallFace wf = walls[f];
+    const float es = (float)cells[wf.tri].es[wf.lfc];
+    const float *R = ref_edge + (size_t)wf.lfc * NP * NP;
+    double acc[NP];
+#pragma unroll
+    for (int m = 0; m < NP; ++m) acc[m] = 0.0;
+    double s2 = 0.0;
+    for (int u = lane; u < nu; u += 32) {
+        const double un = ucx[u] * wf.nx + ucy[u] * wf.ny;
+        if (un < 0.0) {
+            const float *fr = vdf + ((size_t)rep[u] * nt + wf.tri) * NP;
+            float fl[NP];
+#pragma unroll
+            for (int l = 0; l < NP; ++l) fl[l] = fr[l];
+            const double uwv = un * uw[u];
+#pragma unroll
+            for (int m = 0; m < NP; ++m) {
+                float a = 0.f;
+#pragma unroll
+                for (int l = 0; l < NP; ++l) a += fl[l] * (es * R[m * NP + l]);
+                acc[m] += uwv * (double)a;
+            }
+        } else {
+            s2 -= un * uw[u];
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int m = 0; m < NP; ++m) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], o);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    }
+    if (lane == 0) {
+        double *out = fw_out + (size_t)wf.face * NP;
+#pragma unroll
+        for (int m = 0; m < NP; ++m) out[m] = -acc[m] / s2;
+    }
+}
+
 // Step residual and mass; out[0] = residual, out[1] = sum(temp); t_old <- temp.
 __global__ void residual_kernel(const double *temp, double *t_old, int n, double *out, const int32_t *done) {
     if (stopped(done)) return;
@@ -598,6 +676,7 @@ static SweepParams<T> make_params(pbte_ctx *c) {
     P.dir_class = c->d_dir_class; P.class_off = c->d_class_lvl_off; P.class_nlev = c->d_class_nlev;
     P.lvl_ptr = c->d_lvl_ptr; P.lvl_cells = c->d_lvl_cells;
     P.udir_of = c->d_udir_of;
+    P.store_twin = 1;
     P.singular = c->d_singular; P.done = c->done;
     P.nt = c->n_tris; P.n_faces = c->n_faces;
     P.inv_tau_c = (T)(1.0 / c->tau_c);
@@ -678,10 +757,12 @@ int launch_sweep64(pbte_ctx *c, double *vdf, const double *fw, const double *pbu
     return sweep_dispatch<double, false>(c, P, s);
 }
 
-int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale, cudaStream_t s) {
+int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale, cudaStream_t s,
+                   bool store_twin) {
     SweepParams<float> P = make_params<float>(c);
     P.cells = c->d_cells32; P.ref = c->d_ref32; P.S = c->d_S32; P.vdf = vdf32;
     P.flux_wall = fw; P.wall_scale = (float)wall_scale;
+    P.store_twin = store_twin ? 1 : 0;
     if (c->sweep_variant != 1) {
         const int rc = launch_ring<float, false>(c, P, s);
         if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant >= 2) return rc;
@@ -756,6 +837,48 @@ static int wall_flux_impl(pbte_ctx *c, const T *vdf, double *fw, cudaStream_t s)
             wall_flux_kernel<T><<<c->n_wall_ad, th, shm, s>>>(vdf, c->d_wall_ad, c->d_cells64,
                                                               c->d_ref64 + 3 * c->nd * c->nd, c->d_cx, c->d_cy,
                                                               c->d_w, c->ndir, c->n_tris, c->nd, fw, c->done);
+    }
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                         const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
+                         double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
+                         double *qy, cudaStream_t s) {
+    // folded kernels exist for N_p = 3, 6, 10; other orders store and read every ordinate
+    const bool fold = c->nd == 3 || c->nd == 6 || c->nd == 10;
+    int rc = launch_sources(c, ts, qxs, qys, true, s);
+    if (rc) return rc;
+    rc = launch_sweep32(c, vdf32, fw_in, wall_scale, s, !fold);
+    if (rc) return rc;
+    if (!fold) {
+        rc = moments_impl<float>(c, vdf32, ts_out, qxs_out, qys_out, temp, qx, qy, s);
+        if (rc == PBTE_OK && fw_out) rc = wall_flux_impl<float>(c, vdf32, fw_out, s);
+        return rc;
+    }
+    const int total = c->n_tris * c->nd, th = 256;
+    const int nch = (c->n_udir + kMomChunk - 1) / kMomChunk;
+    moments_partial_fold_kernel<<<dim3((total + th - 1) / th, nch), th, 0, s>>>(
+        vdf32, c->d_udir_rep, c->d_ucx32, c->d_ucy32, c->d_uw32, c->n_udir, total, c->d_mom_part, c->done);
+    moments_combine_kernel<<<(total + th - 1) / th, th, 0, s>>>(c->d_mom_part, nch, c->n_tris, c->nd, c->cv, ts_out,
+                                                               qxs_out, qys_out, c->done);
+    if (temp)
+        element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts_out, qxs_out, qys_out, c->d_int_tri,
+                                                                         c->n_tris, c->nd, c->cv, temp, qx, qy,
+                                                                         c->done);
+    if (c->n_wall_ad && fw_out) {
+        const int wpb = 4;   // wall faces (warps) per block
+        const int bl = (c->n_wall_ad + wpb - 1) / wpb;
+        const float *ref_edge = c->d_ref32 + 3 * c->nd * c->nd;
+        auto go = [&](auto kern) {
+            kern<<<bl, 32 * wpb, 0, s>>>(vdf32, c->d_wall_ad, c->n_wall_ad, c->d_cells64, ref_edge, c->d_udir_rep,
+                                         c->d_ucx64, c->d_ucy64, c->d_uw64, c->n_udir, c->n_tris, fw_out, c->done);
+        };
+        switch (c->nd) {
+            case 3: go(wall_flux_fold_kernel<3>); break;
+            case 6: go(wall_flux_fold_kernel<6>); break;
+            default: go(wall_flux_fold_kernel<10>); break;
+        }
     }
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }

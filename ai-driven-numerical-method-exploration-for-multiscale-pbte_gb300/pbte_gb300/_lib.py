@@ -95,6 +95,7 @@ _SIGS = {
                        ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_sweep": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp], ctypes.c_int),
     "pbte_sweep_f32": ([_vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_double, _vp], ctypes.c_int),
+    "pbte_fixed_point_f32": ([_vp, _vp, _vp, _vp, _vp, ctypes.c_double] + [_vp] * 8 + [_vp], ctypes.c_int),
     "pbte_moments": ([_vp] + [_vp] * 7 + [_vp], ctypes.c_int),
     "pbte_moments_f32": ([_vp] + [_vp] * 7 + [_vp], ctypes.c_int),
     "pbte_wall_flux": ([_vp, _vp, _vp, _vp], ctypes.c_int),

@@ -87,14 +87,15 @@ class FixedPointOperator:
             if self.wall:
                 _lib.check(L.pbte_wall_flux(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux")
         else:
-            _lib.check(L.pbte_sweep_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), self.vdf.data_ptr(),
-                                        fw.data_ptr(), 0.0 if self.homogeneous else 1.0, s), "sweep_f32")
+            # one call: sources, FP32 sweep, moments and emission with the
+            # z-mirror twins folded (self.vdf is scratch here)
             ints = (self.temp.data_ptr(), self.qx.data_ptr(), self.qy.data_ptr()) if self.integrals \
                 else (None, None, None)
-            _lib.check(L.pbte_moments_f32(ctx, self.vdf.data_ptr(), ots.data_ptr(), oqxs.data_ptr(),
-                                          oqys.data_ptr(), *ints, s), "moments_f32")
-            if self.wall:
-                _lib.check(L.pbte_wall_flux_f32(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux_f32")
+            _lib.check(L.pbte_fixed_point_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), fw.data_ptr(),
+                                              0.0 if self.homogeneous else 1.0, self.vdf.data_ptr(),
+                                              ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(),
+                                              ofw.data_ptr() if self.wall else None, *ints, s),
+                       "fixed_point_f32")
 
     def _capture(self):
         with device_lock:

@@ -121,6 +121,20 @@ int pbte_sweep(pbte_ctx *ctx, const double *ts, const double *qxs, const double 
 int pbte_sweep_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
                    float *vdf32, const double *flux_wall, double wall_scale, void *stream);
 
+/* The FP32 fixed-point product of the mixed path in one call: moment
+ * sources, FP32 sweep, moments (and, when temp/qx/qy are given, the element
+ * integrals) and the adiabatic-wall emission, from the state (ts, qxs, qys,
+ * flux_wall_in) to (ts_out, qxs_out, qys_out, flux_wall_out) -- the map of
+ * FixedPointOperator.apply (pybte/krylov.py:64-136) in FP32.  z-mirror
+ * twins are folded (P1-P3): the sweep stores one copy per in-plane velocity
+ * in vdf32 (scratch: the twins' rows are not written), and the moments and
+ * the emission read it with the pair's summed weight.  No reference
+ * counterpart: the reference is FP64 only. */
+int pbte_fixed_point_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
+                         const double *flux_wall_in, double wall_scale, float *vdf32, double *ts_out,
+                         double *qxs_out, double *qys_out, double *flux_wall_out, double *temp,
+                         double *qx, double *qy, void *stream);
+
 /* Angular moments and element integrals.  Replaces compute_moments
  * (pybte/moments.py:51-55 -> _kernels.moments_kernel, _kernels.py:312-338).
  * temp, qx, qy may all be NULL to skip the element integrals.  The partial

@@ -130,6 +130,39 @@ def test_fp32_sweep_close_to_fp64(cuda):
     assert _rel(v32.double().cpu().numpy(), o.vdf) < 2e-5
 
 
+@pytest.mark.parametrize("deg", [1, 2, 3])
+def test_fused_fp32_product_matches_separate_calls(cuda, deg):
+    """pbte_fixed_point_f32 (sources, sweep, moments and emission in one call,
+    z-mirror twins folded) against pbte_sweep_f32 + pbte_moments_f32 +
+    pbte_wall_flux_f32 on every ordinate: the same numbers up to the FP32
+    rounding of w_a f + w_b f against (w_a + w_b) f (tolerance 1e-6)."""
+    from pbte_gb300 import _lib
+    s = Solver(small_case(deg, 4, 8, 0.5, 0.05))
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 21)
+    s.ctx.wall_flux(s.vdf)
+    L, st = _lib.lib(), torch.cuda.current_stream().cuda_stream
+    h, m = s.ctx.handle, s.mom
+    f64 = dict(dtype=torch.float64, device="cuda")
+    v32 = torch.zeros(s.vdf.shape, dtype=torch.float32, device="cuda")
+    ref = [torch.zeros_like(m.ts) for _ in range(3)] + [torch.zeros_like(s.ctx.flux_wall)]
+    out = [torch.zeros_like(m.ts) for _ in range(3)] + [torch.zeros_like(s.ctx.flux_wall)]
+    ints = [torch.zeros(s.n_tris, **f64) for _ in range(6)]
+    _lib.check(L.pbte_sweep_f32(h, m.ts.data_ptr(), m.qxs.data_ptr(), m.qys.data_ptr(), v32.data_ptr(),
+                                s.ctx.flux_wall.data_ptr(), 1.0, st), "sweep_f32")
+    _lib.check(L.pbte_moments_f32(h, v32.data_ptr(), *(r.data_ptr() for r in ref[:3]),
+                                  *(i.data_ptr() for i in ints[:3]), st), "moments_f32")
+    _lib.check(L.pbte_wall_flux_f32(h, v32.data_ptr(), ref[3].data_ptr(), st), "wall_flux_f32")
+    v32.zero_()
+    _lib.check(L.pbte_fixed_point_f32(h, m.ts.data_ptr(), m.qxs.data_ptr(), m.qys.data_ptr(),
+                                      s.ctx.flux_wall.data_ptr(), 1.0, v32.data_ptr(),
+                                      *(x.data_ptr() for x in out), *(i.data_ptr() for i in ints[3:]), st),
+               "fixed_point_f32")
+    torch.cuda.synchronize()
+    for a, b in zip(out + ints[3:], ref + ints[:3]):
+        assert _rel(a.cpu().numpy(), b.cpu().numpy()) < 1e-6
+
+
 @pytest.mark.parametrize("name", ["cis_deg1_adiabatic", "cis_deg2_isothermal"])
 def test_cis_solve_matches_reference(cuda, name):
     z = golden(name)
