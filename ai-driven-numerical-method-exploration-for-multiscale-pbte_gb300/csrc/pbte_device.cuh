@@ -41,6 +41,7 @@ struct SweepParams {
     const int8_t *piv;
     const int32_t *udir_of; // ordinate -> distinct in-plane velocity (factor owner)
     int store_twin;         // ring sweep: also store the z-mirror twin's copy (0: folded consumers)
+    int by_udir;            // ring sweep: row of the distinct velocity u instead of the ordinate d
     int32_t *singular;
     const int32_t *done;
     int nt, n_faces;

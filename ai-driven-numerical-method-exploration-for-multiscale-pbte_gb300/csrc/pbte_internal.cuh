@@ -128,7 +128,7 @@ int launch_sources(pbte_ctx *c, const double *ts, const double *qxs, const doubl
 int launch_sweep64(pbte_ctx *c, double *vdf, const double *flux_wall, const double *pbuf,
                    int use_pbuf, cudaStream_t s);
 int launch_sweep32(pbte_ctx *c, float *vdf32, const double *flux_wall, double wall_scale,
-                   cudaStream_t s, bool store_twin = true);
+                   cudaStream_t s, bool store_twin = true, bool by_udir = false);
 // the FP32 fixed-point product with z-mirror twins folded (one copy per
 // in-plane velocity written and read): sources, sweep, moments, emission
 int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,

@@ -362,21 +362,29 @@ __global__ void wall_flux_np_kernel(const T *vdf, const WallFace *walls, const C
 // (ordinate rep[u]) is read with the pair's summed weight uw[u].
 // ---------------------------------------------------------------------------
 
-__global__ void moments_partial_fold_kernel(const float *vdf, const int32_t *rep, const float *ucx,
-                                            const float *ucy, const float *uw, int nu, int total, double *part,
-                                            const int32_t *done) {
+// vdf rows by distinct velocity: vdf[u][element dof]
+__global__ void moments_partial_fold_kernel(const float *vdf, const float *ucx, const float *ucy, const float *uw,
+                                            int nu, int total, double *part, const int32_t *done) {
     if (stopped(done)) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    __shared__ float sw[kMomChunk], sx[kMomChunk], sy[kMomChunk];
     const int ch = blockIdx.y;
-    if (t >= total) return;
     const int u0 = ch * kMomChunk, u1 = min(nu, u0 + kMomChunk);
+    if ((int)threadIdx.x < u1 - u0) {
+        sw[threadIdx.x] = uw[u0 + threadIdx.x];
+        sx[threadIdx.x] = ucx[u0 + threadIdx.x];
+        sy[threadIdx.x] = ucy[u0 + threadIdx.x];
+    }
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const float *f = vdf + (size_t)u0 * total + t;
     float a = 0.f, bx = 0.f, by = 0.f;
 #pragma unroll 8
-    for (int u = u0; u < u1; ++u) {
-        const float fw = vdf[(size_t)rep[u] * total + t] * uw[u];
+    for (int k = 0; k < u1 - u0; ++k) {
+        const float fw = f[(size_t)k * total] * sw[k];
         a += fw;
-        bx += ucx[u] * fw;
-        by += ucy[u] * fw;
+        bx += sx[k] * fw;
+        by += sy[k] * fw;
     }
     double *p = part + (size_t)ch * 3 * total;
     p[t] = a;
@@ -384,13 +392,13 @@ __global__ void moments_partial_fold_kernel(const float *vdf, const int32_t *rep
     p[2 * total + t] = by;
 }
 
-// Adiabatic-wall emission, folded: one warp per wall face, distinct
-// velocities over lanes, FP32 products, FP64 sums reduced by shuffles in a
-// fixed order.
+// Adiabatic-wall emission, folded (vdf rows by distinct velocity): one warp
+// per wall face, distinct velocities over lanes, FP32 products, FP64 sums
+// reduced by shuffles in a fixed order.
 template <int NP>
 __global__ void wall_flux_fold_kernel(const float *vdf, const WallFace *walls, int nwall, const CellRec<double> *cells,
-                                      const float *ref_edge, const int32_t *rep, const double *ucx, const double *ucy,
-                                      const double *uw, int nu, int nt, double *fw_out, const int32_t *done) {
+                                      const float *ref_edge, const double *ucx, const double *ucy, const double *uw,
+                                      int nu, int nt, double *fw_out, const int32_t *done) {
     if (stopped(done)) return;
     const int lane = threadIdx.x % 32;
     const int f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
@@ -405,7 +413,7 @@ __global__ void wall_flux_fold_kernel(const float *vdf, const WallFace *walls, i
     for (int u = lane; u < nu; u += 32) {
         const double un = ucx[u] * wf.nx + ucy[u] * wf.ny;
         if (un < 0.0) {
-            const float *fr = vdf + ((size_t)rep[u] * nt + wf.tri) * NP;
+            const float *fr = vdf + ((size_t)u * nt + wf.tri) * NP;
             float fl[NP];
 #pragma unroll
             for (int l = 0; l < NP; ++l) fl[l] = fr[l];
@@ -677,6 +685,7 @@ static SweepParams<T> make_params(pbte_ctx *c) {
     P.lvl_ptr = c->d_lvl_ptr; P.lvl_cells = c->d_lvl_cells;
     P.udir_of = c->d_udir_of;
     P.store_twin = 1;
+    P.by_udir = 0;
     P.singular = c->d_singular; P.done = c->done;
     P.nt = c->n_tris; P.n_faces = c->n_faces;
     P.inv_tau_c = (T)(1.0 / c->tau_c);
@@ -758,11 +767,17 @@ int launch_sweep64(pbte_ctx *c, double *vdf, const double *fw, const double *pbu
 }
 
 int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale, cudaStream_t s,
-                   bool store_twin) {
+                   bool store_twin, bool by_udir) {
     SweepParams<float> P = make_params<float>(c);
     P.cells = c->d_cells32; P.ref = c->d_ref32; P.S = c->d_S32; P.vdf = vdf32;
     P.flux_wall = fw; P.wall_scale = (float)wall_scale;
     P.store_twin = store_twin ? 1 : 0;
+    P.by_udir = by_udir ? 1 : 0;
+    if (by_udir) {
+        // rows by distinct velocity exist only in the ring sweep
+        if (c->sweep_variant == 1) return PBTE_ERR_UNSUPPORTED;
+        return launch_ring<float, false>(c, P, s);
+    }
     if (c->sweep_variant != 1) {
         const int rc = launch_ring<float, false>(c, P, s);
         if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant >= 2) return rc;
@@ -845,21 +860,27 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
                          const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
                          double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
                          double *qy, cudaStream_t s) {
-    // folded kernels exist for N_p = 3, 6, 10; other orders store and read every ordinate
-    const bool fold = c->nd == 3 || c->nd == 6 || c->nd == 10;
+    // folded kernels exist for N_p = 3, 6, 10 and the ring sweep (which
+    // writes rows by distinct velocity u); otherwise every ordinate is
+    // stored and read
+    bool fold = c->nd == 3 || c->nd == 6 || c->nd == 10;
     int rc = launch_sources(c, ts, qxs, qys, true, s);
     if (rc) return rc;
-    rc = launch_sweep32(c, vdf32, fw_in, wall_scale, s, !fold);
-    if (rc) return rc;
+    if (fold) {
+        rc = launch_sweep32(c, vdf32, fw_in, wall_scale, s, false, true);
+        if (rc == PBTE_ERR_UNSUPPORTED) fold = false;
+        else if (rc) return rc;
+    }
     if (!fold) {
-        rc = moments_impl<float>(c, vdf32, ts_out, qxs_out, qys_out, temp, qx, qy, s);
+        rc = launch_sweep32(c, vdf32, fw_in, wall_scale, s);
+        if (rc == PBTE_OK) rc = moments_impl<float>(c, vdf32, ts_out, qxs_out, qys_out, temp, qx, qy, s);
         if (rc == PBTE_OK && fw_out) rc = wall_flux_impl<float>(c, vdf32, fw_out, s);
         return rc;
     }
     const int total = c->n_tris * c->nd, th = 256;
     const int nch = (c->n_udir + kMomChunk - 1) / kMomChunk;
     moments_partial_fold_kernel<<<dim3((total + th - 1) / th, nch), th, 0, s>>>(
-        vdf32, c->d_udir_rep, c->d_ucx32, c->d_ucy32, c->d_uw32, c->n_udir, total, c->d_mom_part, c->done);
+        vdf32, c->d_ucx32, c->d_ucy32, c->d_uw32, c->n_udir, total, c->d_mom_part, c->done);
     moments_combine_kernel<<<(total + th - 1) / th, th, 0, s>>>(c->d_mom_part, nch, c->n_tris, c->nd, c->cv, ts_out,
                                                                qxs_out, qys_out, c->done);
     if (temp)
@@ -871,8 +892,8 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
         const int bl = (c->n_wall_ad + wpb - 1) / wpb;
         const float *ref_edge = c->d_ref32 + 3 * c->nd * c->nd;
         auto go = [&](auto kern) {
-            kern<<<bl, 32 * wpb, 0, s>>>(vdf32, c->d_wall_ad, c->n_wall_ad, c->d_cells64, ref_edge, c->d_udir_rep,
-                                         c->d_ucx64, c->d_ucy64, c->d_uw64, c->n_udir, c->n_tris, fw_out, c->done);
+            kern<<<bl, 32 * wpb, 0, s>>>(vdf32, c->d_wall_ad, c->n_wall_ad, c->d_cells64, ref_edge, c->d_ucx64,
+                                         c->d_ucy64, c->d_uw64, c->n_udir, c->n_tris, fw_out, c->done);
         };
         switch (c->nd) {
             case 3: go(wall_flux_fold_kernel<3>); break;

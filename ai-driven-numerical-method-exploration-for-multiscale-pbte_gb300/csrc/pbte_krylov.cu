@@ -278,32 +278,45 @@ int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, doub
 // done, hist[j] = |gam[j+1]|.  One thread; nothing runs once state[0] != 0.
 __global__ void gmres_givens_kernel(int j, const double *h, double *R, int ldr, double *cs, double *sn,
                                     double *gam, const double *tol_abs, int32_t *state, double *hist) {
-    if (threadIdx.x != 0 || state[0] != 0) return;
-    double col[kMaxRows + 1];
-    for (int i = 0; i <= j + 1; ++i) col[i] = h[i];
-    const double hn = col[j + 1];
-    for (int i = 0; i < j; ++i) {
-        const double t = cs[i] * col[i] + sn[i] * col[i + 1];
-        col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1];
-        col[i] = t;
+    // the column and the rotations are staged in shared memory by the warp
+    // (independent loads), then lane 0 runs the sequential rotations
+    __shared__ double col[kMaxRows + 1], c_s[kMaxRows], s_s[kMaxRows];
+    if (*(volatile const int32_t *)state != 0) return;
+    for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) col[i] = h[i];
+    for (int i = threadIdx.x; i < j; i += blockDim.x) {
+        c_s[i] = cs[i];
+        s_s[i] = sn[i];
     }
-    const double d = hypot(col[j], col[j + 1]);
-    double c = 1.0, s = 0.0;
-    if (d != 0.0) {
-        c = col[j] / d;
-        s = col[j + 1] / d;
+    __syncwarp();
+    if (threadIdx.x == 0) {
+        const double hn = col[j + 1];
+        double a = col[0];
+        for (int i = 0; i < j; ++i) {
+            const double b = col[i + 1];
+            col[i] = c_s[i] * a + s_s[i] * b;
+            a = -s_s[i] * a + c_s[i] * b;
+        }
+        col[j] = a;
+        const double d = hypot(col[j], col[j + 1]);
+        double c = 1.0, s = 0.0;
+        if (d != 0.0) {
+            c = col[j] / d;
+            s = col[j + 1] / d;
+        }
+        cs[j] = c;
+        sn[j] = s;
+        col[j] = d;
+        const double g = gam[j];
+        gam[j + 1] = -s * g;
+        gam[j] = c * g;
+        const double res = fabs(-s * g);
+        hist[j] = res;
+        state[1] = j + 1;
+        if (res <= *tol_abs) state[0] = 1;
+        else if (hn == 0.0) state[0] = 2;
     }
-    cs[j] = c;
-    sn[j] = s;
-    col[j] = d;
-    for (int i = 0; i <= j; ++i) R[(size_t)j * ldr + i] = col[i];
-    gam[j + 1] = -s * gam[j];
-    gam[j] = c * gam[j];
-    const double res = fabs(gam[j + 1]);
-    hist[j] = res;
-    state[1] = j + 1;
-    if (res <= *tol_abs) state[0] = 1;
-    else if (hn == 0.0) state[0] = 2;
+    __syncwarp();
+    for (int i = threadIdx.x; i <= j; i += blockDim.x) R[(size_t)j * ldr + i] = col[i];
 }
 
 // q_{j+1} = w / h[j+1] into row j+1 of the basis, and widened into the

@@ -119,7 +119,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
     const int W = Q.class_W[cls], Rr = Q.class_R[cls];
     const int G = Q.groups;
     const int g = threadIdx.x / TPG, t = threadIdx.x % TPG;
-    T *f1 = P.vdf + (size_t)d * P.nt * NP;
+    T *f1 = P.vdf + (size_t)(P.by_udir ? u : d) * P.nt * NP;
     T *f2 = (d2 >= 0 && P.store_twin) ? P.vdf + (size_t)d2 * P.nt * NP : nullptr;
     int sing = 0;
     int beg = g < nlev ? P.lvl_ptr[off + g] : 0;

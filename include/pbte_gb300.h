@@ -126,9 +126,9 @@ int pbte_sweep_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const dou
  * integrals) and the adiabatic-wall emission, from the state (ts, qxs, qys,
  * flux_wall_in) to (ts_out, qxs_out, qys_out, flux_wall_out) -- the map of
  * FixedPointOperator.apply (pybte/krylov.py:64-136) in FP32.  z-mirror
- * twins are folded (P1-P3): the sweep stores one copy per in-plane velocity
- * in vdf32 (scratch: the twins' rows are not written), and the moments and
- * the emission read it with the pair's summed weight.  No reference
+ * twins are folded (P1-P3, ring sweep): vdf32 is scratch whose first rows
+ * hold one copy per distinct in-plane velocity, and the moments and the
+ * emission read them with the pair's summed weight.  No reference
  * counterpart: the reference is FP64 only. */
 int pbte_fixed_point_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
                          const double *flux_wall_in, double wall_scale, float *vdf32, double *ts_out,
