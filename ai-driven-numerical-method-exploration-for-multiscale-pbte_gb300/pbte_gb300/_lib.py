@@ -17,7 +17,7 @@ CSRC = PKG_ROOT / "csrc"
 INCLUDE = REPO_ROOT / "include"
 LIB_PATH = PKG_ROOT / "_build" / "libpbte_gb300.so"
 SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_krylov.cu", "pbte_capi.cu",
-           "pbte_noalloc.cu"]
+           "pbte_noalloc.cu", "pbte_output.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0
@@ -130,6 +130,13 @@ _SIGS = {
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],
                      ctypes.c_int),
     "pbte_batched_inverse": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+    "pbte_field_moments": ([_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32] + [_vp] * 6 + [_vp],
+                           ctypes.c_int),
+    "pbte_locate_points": ([_vp, _vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+                            ctypes.c_double, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int32,
+                            _vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+    "pbte_sample_fields": ([_vp, _vp, _vp, _vp, ctypes.c_int32, _vp, ctypes.c_int32, _vp, _vp, ctypes.c_int32,
+                            _vp, _vp, _vp, ctypes.c_int32, ctypes.c_double, _vp, _vp, _vp], ctypes.c_int),
     "pbte_version": ([], ctypes.c_char_p),
 }
 

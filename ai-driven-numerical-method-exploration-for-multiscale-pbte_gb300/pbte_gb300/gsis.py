@@ -238,6 +238,15 @@ class GSIS:
         self.uq = torch.zeros((7 * nd, n), **f64)
         self.solve_count = 0
 
+    def diagnostics(self) -> dict:
+        """The run-record entries of ``Acceleration.diagnostics``
+        (``pybte/acceleration/__init__.py:175-187``); the defect-repair
+        experiment is not implemented, so its entries are its off values."""
+        return {"acc_variant": self.variant, "global_matrix_n": int(self.K.shape[0]),
+                "global_matrix_nnz": int(self.K.nnz), "global_solve_count": int(self.solve_count),
+                "stabilisation": [float(v) for v in self.st], "defect_omega": 0.0, "defect_every": 1,
+                "defect_anderson": 0, "defect_outer": 0, "defect_norm": 0.0}
+
     def rhs(self, aa_src: torch.Tensor, vdf: torch.Tensor, stream=None) -> torch.Tensor:
         """``GlobalSolver.rhs`` (``global_solve.py:131-187``)."""
         nf = self.nf

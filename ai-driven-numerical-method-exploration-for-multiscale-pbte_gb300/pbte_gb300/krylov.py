@@ -121,6 +121,26 @@ class FixedPointOperator:
         self.sweeps += 1
         return self.uout[:self.n].clone()
 
+    def state(self) -> torch.Tensor:
+        """The state of the solver's current ``vdf`` without sweeping: its
+        moments and wall emission, also left in the solver's moments and
+        flux buffers (``pybte/krylov.py:128-136``; the restart start)."""
+        s = self.s
+        L = _lib.lib()
+        st = torch.cuda.current_stream().cuda_stream
+        u = torch.zeros_like(self.uin)
+        ts, qxs, qys, fw = self._views(u)
+        m = s.mom
+        _lib.check(L.pbte_moments(s.ctx.handle, s.vdf.data_ptr(), ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(),
+                                  m.temp.data_ptr(), m.qx.data_ptr(), m.qy.data_ptr(), st), "moments")
+        m.ts.copy_(ts)
+        m.qxs.copy_(qxs)
+        m.qys.copy_(qys)
+        if self.wall:
+            _lib.check(L.pbte_wall_flux(s.ctx.handle, s.vdf.data_ptr(), fw.data_ptr(), st), "wall_flux")
+            s.ctx.flux_wall.copy_(fw)
+        return u[:self.n].clone()
+
     def publish(self) -> None:
         """Copy the last product's moments into the solver's state."""
         s = self.s
@@ -527,27 +547,46 @@ def basis_cap(case, n: int) -> int:
     return int(max(32, min(int(case.iteration.tmax), int(case.scheme.krylov_max_bytes / per))))
 
 
-def run_krylov(solver):
-    """``pybte/krylov.py:257-363`` on the device."""
+def run_krylov(solver, callback=None, progress_every: int = 0):
+    """``pybte/krylov.py:257-363`` on the device.  ``callback(step,
+    residual, solver)`` and progress lines follow every residual the host
+    sees (each product's GMRES residual, the closing true residual); a
+    restarted solver starts GMRES from its loaded state."""
     c = solver.case
     tol, tmax = c.iteration.tol, c.iteration.tmax
+    want_true = c.iteration.true_residual
     op = cached(solver, "fp64", lambda: FixedPointOperator(solver))
     op.sweeps = 0
-    residuals, masses = [], []
+    residuals, masses, true_res = [], [], []
 
     def sweep(u):
         out = op.apply(u)
+        product()
+        return out
+
+    def product():
         masses.append(np.nan)
         residuals.append(np.nan)
-        return out
+        if want_true:
+            true_res.append(np.nan)
+
+    def close(res):
+        residuals[-1] = res
+        step = len(residuals)
+        if progress_every and step % progress_every == 0:
+            print(f"  step {step:8d}  residual {res:.6e}", flush=True)
+        if callback is not None:
+            callback(step, res, solver)
 
     sync(solver.device)
     t0 = time.perf_counter()
+    restarted = bool(solver.restart_info.get("enabled")) if hasattr(solver, "restart_info") else False
+    x = op.state() if restarted else torch.zeros(op.n, dtype=torch.float64, device=solver.device)
     zero = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
     g = sweep(zero)
     gnorm = float(torch.linalg.vector_norm(g).item())
     scale = gnorm or 1.0
-    residuals[-1] = 1.0
+    close(1.0)
 
     def matvec(v):
         return v - (sweep(v) - g)
@@ -559,19 +598,15 @@ def run_krylov(solver):
 
     def on_residual(res):
         nonlocal reached
-        residuals[-1] = res / scale
+        close(res / scale)
         n = len(residuals)
         if reached < 0 and res <= enough:
             reached = n
         return reached >= 0 and n - reached > max(64, reached // 4)
 
-    x = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
     ar = cached(solver, ("arnoldi64", cap), lambda: ArnoldiGraphs(op, g, cap)) if cap <= 63 else None
     if ar is not None:
         ar.set_g(g)
-        def product():
-            masses.append(np.nan)
-            residuals.append(np.nan)
         ar.on_product = product
     converged = False
     final = float("nan")
@@ -585,7 +620,9 @@ def run_krylov(solver):
         sweep(x)
         op.publish()
         final = solver.ctx.true_residual(solver.mom, solver.vdf)
-        residuals[-1] = final
+        if want_true:
+            true_res[-1] = final
+        close(final)
         converged = bool(final < tol) if np.isfinite(final) else gnorm == 0.0
         if converged or len(residuals) >= tmax:
             break
@@ -595,5 +632,6 @@ def run_krylov(solver):
     solver.ctx.sweep_count += op.sweeps
     masses = [solver.mom.mass] * len(residuals)
     return solver._record(len(residuals), converged, residuals, masses, wall, "KRYLOV",
-                          extra={"krylov_size": op.n, "krylov_basis_cap": cap,
-                                 "transport_residual": final})
+                          extra={"krylov_size": op.n, "krylov_periodic_state": 0, "krylov_basis_cap": cap,
+                                 "krylov_precond": False, "transport_residual": final},
+                          true_res=true_res if want_true else None)

@@ -54,7 +54,8 @@ def run_mixed(solver, opts: MixedOptions | None = None):
     op64.sweeps = op32.sweeps = 0
     n = op64.n
     dev = solver.device
-    u = torch.zeros(n, dtype=torch.float64, device=dev)
+    restarted = bool(getattr(solver, "restart_info", {}).get("enabled"))
+    u = op64.state() if restarted else torch.zeros(n, dtype=torch.float64, device=dev)
     ar32 = None
     history = []
     inner_sweeps = 0

@@ -14,12 +14,23 @@
 
 ``performance.precision = "mixed"`` runs the same scheme with FP32 sweeps
 inside an FP64 defect-correction loop (:mod:`pbte_gb300.mixed`).
+
+Restart files (``VDFP{deg}T{n_tris}NP{npole}NA{nazim}.out``, the Fortran's
+``VDF(NDOF, N_TRIS, NPOLE, NAZIM)`` as raw little-endian doubles) are read
+at construction and written by :meth:`Solver.save_restart`
+(``pybte/driver.py:99-141``); :meth:`Solver.write_outputs` writes the run
+record, ``RunTime.txt`` and the sampled fields (``driver.py:256-291``).
 """
 from __future__ import annotations
 
-import ctypes
+import hashlib
+import json
+import platform
+import sys
 import time
-from dataclasses import dataclass, field
+import warnings
+from dataclasses import dataclass, field, fields
+from pathlib import Path
 
 import numpy as np
 import torch
@@ -33,38 +44,131 @@ from .sweep import Moments, SweepContext
 __all__ = ["Solver", "RunRecord"]
 
 
+def _empty(*shape):
+    return field(default_factory=lambda: np.zeros(shape))
+
+
 @dataclass
 class RunRecord:
-    """The fields of pybte's ``RunRecord`` (``pybte/io_output.py:30-164``)
-    that describe a solve; arrays are host numpy."""
-    iterations: int
-    converged: bool
-    residual_history: np.ndarray
-    mass_history: np.ndarray
-    temp: np.ndarray
-    qx: np.ndarray
-    qy: np.ndarray
-    temp_dofs: np.ndarray
-    qx_dofs: np.ndarray
-    qy_dofs: np.ndarray
-    sweep_count: int
-    wall_clock: float
-    setup_wall_clock: float
-    scheme: str
-    tol: float
-    tau_r: float
-    tau_n: float
-    deg: int
-    npole: int
-    nazim: int
-    n_tris: int
-    precision: str = "fp64"
+    """pybte's machine-readable run record (``pybte/io_output.py:30-164``):
+    the same fields, helpers and JSON / npz writers, plus ``precision``;
+    arrays are host numpy."""
+    iterations: int = 0
+    converged: bool = False
+    residual_history: np.ndarray = _empty(0)
     residual_true: np.ndarray | None = None
+    mass_history: np.ndarray = _empty(0)
+    temp: np.ndarray = _empty(0)
+    qx: np.ndarray = _empty(0)
+    qy: np.ndarray = _empty(0)
+    temp_dofs: np.ndarray = _empty(0, 0)
+    qx_dofs: np.ndarray = _empty(0, 0)
+    qy_dofs: np.ndarray = _empty(0, 0)
+    sweep_count: int = 0
+    factorisation_count: int = 0
+    wall_clock: float = 0.0
+    setup_wall_clock: float = 0.0
+    config_hash: str = ""
+    scheme: str = "CIS"
+    acc_variant: str | None = None
+    tol: float = 0.0
+    tmax: int = 0
+    tau_r: float = 0.0
+    tau_n: float = 0.0
+    tau_c: float = 0.0
+    deg: int = 0
+    npole: int = 0
+    nazim: int = 0
+    n_tris: int = 0
+    n_faces: int = 0
+    mesh_file: str = ""
+    restart: dict = field(default_factory=dict)
+    environment: dict = field(default_factory=dict)
     diagnostics: dict = field(default_factory=dict)
+    precision: str = "fp64"
+
+    @property
+    def final_residual(self) -> float:
+        h = np.asarray(self.residual_history)
+        return float(h[-1]) if h.size else float("nan")
 
     @property
     def mass(self) -> float:
-        return float(np.sum(self.temp))
+        t = np.asarray(self.temp)
+        return float(np.sum(t)) if t.size else float("nan")
+
+    @property
+    def contraction(self) -> float:
+        """Geometric decay rate of the second half of the residual history
+        (``io_output.py:76-94``): ``(r_last / r_first) ** (1 / (n - 1))`` over
+        its finite positive entries, or ``nan`` if there are fewer than 8
+        residuals, fewer than 4 usable ones, no decay, or a rate outside
+        (0, 1)."""
+        h = np.asarray(self.residual_history, dtype=float)
+        if h.size < 8:
+            return float("nan")
+        tail = h[max(1, h.size // 2):]
+        tail = tail[np.isfinite(tail) & (tail > 0)]
+        if tail.size < 4 or not tail[-1] < tail[0]:
+            return float("nan")
+        rho = (tail[-1] / tail[0]) ** (1.0 / (tail.size - 1))
+        return float(rho) if 0.0 < rho < 1.0 else float("nan")
+
+    @property
+    def error_estimate(self) -> float:
+        """Remaining distance to the fixed point of a linearly converging
+        iteration, ``r rho / (1 - rho)`` (``io_output.py:96-112``)."""
+        rho = self.contraction
+        return float(self.final_residual * rho / (1.0 - rho)) if np.isfinite(rho) else float("nan")
+
+    def to_dict(self, include_fields: bool = True) -> dict:
+        """JSON-ready dict; ``include_fields=False`` drops the 2-D arrays
+        (``io_output.py:114-126``)."""
+        d = {}
+        for f in fields(self):
+            v = getattr(self, f.name)
+            if isinstance(v, np.ndarray):
+                v = None if (not include_fields and v.ndim > 1) else v.tolist()
+            elif isinstance(v, (dict, list)):
+                v = json.loads(json.dumps(v, default=_jsonable))
+            d[f.name] = v
+        d.update(final_residual=self.final_residual, mass=self.mass, contraction=self.contraction,
+                 error_estimate=self.error_estimate)
+        return d
+
+    def to_json(self, path, include_fields: bool = True) -> Path:
+        path = Path(path)
+        path.parent.mkdir(parents=True, exist_ok=True)
+        path.write_text(json.dumps(self.to_dict(include_fields), indent=2))
+        return path
+
+    def to_npz(self, path) -> Path:
+        """Every array field plus ``meta``, the field-less dict as JSON
+        (``io_output.py:134-141``)."""
+        path = Path(path)
+        path.parent.mkdir(parents=True, exist_ok=True)
+        payload = {f.name: getattr(self, f.name) for f in fields(self)
+                   if isinstance(getattr(self, f.name), np.ndarray)}
+        payload["meta"] = np.array(json.dumps(self.to_dict(include_fields=False)))
+        np.savez_compressed(path, **payload)
+        return path
+
+    @staticmethod
+    def environment_fingerprint() -> dict:
+        import scipy
+
+        return {"python": sys.version.split()[0], "numpy": np.__version__, "scipy": scipy.__version__,
+                "numba": None, "torch": torch.__version__, "cuda": torch.version.cuda,
+                "platform": platform.platform(), "machine": platform.machine(),
+                "device": torch.cuda.get_device_name() if torch.cuda.is_available() else None}
+
+
+def _jsonable(v):
+    if isinstance(v, np.generic):
+        return v.item()
+    if isinstance(v, np.ndarray):
+        return v.tolist()
+    return str(v)
 
 
 class Solver:
@@ -86,6 +190,7 @@ class Solver:
         self.mom = Moments.zeros(self.ndof, self.n_tris, device=self.device)
         self.t_old = torch.zeros(self.n_tris, **f64)
         self._res = torch.zeros(2, **f64)
+        self.restart_info = self._apply_restart()
         self.graph_block = int(graph_block)
         self.acc = None
         if case.scheme.accflag == 1:
@@ -93,6 +198,91 @@ class Solver:
             self.acc = GSIS(self)
         sync(self.device)
         self.setup_seconds = time.perf_counter() - t0
+
+    # -- restart (pybte/driver.py:99-141) ------------------------------------
+    def _restart_stem(self) -> str:
+        c = self.case
+        return (f"VDFP{c.dg.deg}T{self.n_tris:3d}NP{c.velmesh.npole:2d}NA{c.velmesh.nazim:2d}"
+                .replace(" ", ""))
+
+    def _apply_restart(self) -> dict:
+        """Load the restart file into ``vdf`` when ``restart.enabled``.  A
+        default-named file left in ``basedir`` while restart is off is an
+        error unless ``restart.error_on_stale`` is False (the Fortran would
+        read it silently)."""
+        r = self.case.restart
+        default = Path(self.case.basedir) / f"{self._restart_stem()}.out"
+        if not r.enabled:
+            if r.error_on_stale and default.exists():
+                raise FileExistsError(
+                    f"a restart file {default} is present but restart is disabled; delete it, or set "
+                    "restart.enabled or restart.error_on_stale explicitly")
+            return {"enabled": False, "path": None, "sha256": None}
+        path = Path(r.path) if r.path else default
+        if not path.is_absolute():
+            path = Path(self.case.basedir) / path
+        if not path.exists():
+            raise FileNotFoundError(f"restart enabled but {path} does not exist")
+        raw = path.read_bytes()
+        want = self.vdf.numel() * 8
+        if len(raw) != want:
+            raise ValueError(f"{path}: {len(raw)} bytes, expected {want} (wrong DEG / mesh / angular resolution?)")
+        # Fortran VDF(l, i, j1, j2) with l fastest is the C-order (ndir, n_tris,
+        # ndof) array with direction d = j2 * npole + j1: the same bytes.
+        host = np.frombuffer(raw, dtype="<f8").astype(np.float64).reshape(tuple(self.vdf.shape))
+        self.vdf.copy_(torch.from_numpy(host))
+        return {"enabled": True, "path": str(path), "sha256": hashlib.sha256(raw).hexdigest()}
+
+    def save_restart(self, path=None) -> Path:
+        """Write ``vdf`` in the restart format; default name in ``basedir``."""
+        path = Path(path) if path else Path(self.case.basedir) / f"{self._restart_stem()}.out"
+        path.parent.mkdir(parents=True, exist_ok=True)
+        path.write_bytes(self.vdf.detach().cpu().numpy().astype("<f8").tobytes())
+        return path
+
+    def vdf_fortran(self) -> np.ndarray:
+        """Host view ``VDF(NDOF, N_TRIS, NPOLE, NAZIM)`` of the distribution."""
+        npole, nazim = self.case.velmesh.npole, self.case.velmesh.nazim
+        v = self.vdf.detach().cpu().numpy()
+        return np.transpose(v.reshape(nazim, npole, self.n_tris, self.ndof), (3, 2, 1, 0))
+
+    # -- output (pybte/driver.py:256-291) ------------------------------------
+    def write_outputs(self, rec: "RunRecord") -> dict:
+        """Write what ``case.output`` asks for under its ``dir``: the run
+        record JSON, a ``RunTime.txt`` line, and the fields on the sampling
+        grid as ``field.npz`` and/or Tecplot ``field.dat``.  Returns
+        ``{artefact: path}``."""
+        from .output import append_runtime_log, locate_points, sample_fields, sampling_grid, write_tecplot
+
+        c = self.case
+        o = c.output
+        out = c.output_path()
+        out.mkdir(parents=True, exist_ok=True)
+        written = {}
+        if o.run_record:
+            written["run_record"] = str(rec.to_json(out / "run_record.json"))
+        if o.runtime_log:
+            written["runtime_log"] = str(append_runtime_log(
+                out / "RunTime.txt", rec.scheme, c.flow.tau_r, c.flow.tau_n, self.n_tris, c.velmesh.npole,
+                c.velmesh.nazim, rec.iterations, rec.wall_clock))
+        if o.field:
+            px, py = sampling_grid(o.field_nx, o.field_ny)
+            triid = locate_points(self.mesh, px, py, device=self.device)
+            missing = int(np.count_nonzero(triid < 0))
+            if missing:
+                warnings.warn(f"{missing} sampling points fell outside the mesh")
+            uq = self.acc.uq if self.acc is not None else None
+            cx, cy, dw = self.vel.flat()
+            pT, pqx, pqy, pxx, pxy, pyy = sample_fields(self.mesh, self.disc.basis, self.vdf, cx, cy, dw,
+                                                        c.flow.cv, px, py, triid, uq=uq, ndof_tri=self.ndof)
+            if o.npz:
+                np.savez_compressed(out / "field.npz", px=px, py=py, triid=triid, T=pT, qx=pqx, qy=pqy,
+                                    Nxx=pxx, Nxy=pxy, Nyy=pyy)
+                written["field_npz"] = str(out / "field.npz")
+            if o.tecplot:
+                written["field_dat"] = str(write_tecplot(out / "field.dat", px, py, [pT, pqx, pqy, pxx, pxy, pyy],
+                                                         ["T", "qx", "qy", "Nxx", "Nxy", "Nyy"]))
+        return written
 
     def release(self) -> None:
         """Free the solver's device state now -- Krylov operators and their
@@ -126,15 +316,20 @@ class Solver:
             self.acc.apply(stream=stream)
 
     def run(self, callback=None, progress_every: int = 0) -> RunRecord:
+        """Solve to ``iteration.tol``.  ``callback(step, residual, solver)``
+        after every outer step and ``progress_every`` progress lines, as
+        pybte's (``driver.py:164-215``); either one, or
+        ``iteration.true_residual``, moves CIS from the graph-captured loop
+        to the host-driven one (same iterates, one host read per step)."""
         c = self.case
         if self.precision == "mixed":
             from .mixed import run_mixed
             return run_mixed(self)
         if c.scheme.method == "krylov":
             from .krylov import run_krylov
-            return run_krylov(self)
-        if self.acc is not None:
-            return self._run_stepwise("GSIS")
+            return run_krylov(self, callback, progress_every)
+        if self.acc is not None or callback is not None or progress_every or c.iteration.true_residual:
+            return self._run_stepwise("GSIS" if self.acc is not None else "CIS", callback, progress_every)
         return self._run_source()
 
     # -- CIS, graph-captured ------------------------------------------------
@@ -192,11 +387,13 @@ class Solver:
         return self._record(n, flag == 1, h[:, 0], h[:, 1], wall, "CIS")
 
     # -- host-driven loop (GSIS and debugging) -------------------------------
-    def _run_stepwise(self, scheme: str) -> RunRecord:
+    def _run_stepwise(self, scheme: str, callback=None, progress_every: int = 0) -> RunRecord:
         c = self.case
         tol, tmax = c.iteration.tol, c.iteration.tmax
+        want_true = c.iteration.true_residual
+        every = max(1, int(c.iteration.true_residual_every))
         L = _lib.lib()
-        residuals, masses = [], []
+        residuals, masses, true_res = [], [], []
         sync(self.device)
         t0 = time.perf_counter()
         step, converged = 0, False
@@ -207,32 +404,53 @@ class Solver:
             _lib.check(L.pbte_residual_iterate(self.ctx.handle, self.mom.temp.data_ptr(), self.t_old.data_ptr(),
                                                self._res.data_ptr(), s), "residual")
             r = self._res.cpu().numpy()
-            residuals.append(float(r[0]))
+            res = float(r[0])
+            residuals.append(res)
             masses.append(float(r[1]))
-            if r[0] < tol:
+            if want_true:
+                true_res.append(self.true_residual() if step % every == 0 else np.nan)
+            if progress_every and step % progress_every == 0:
+                print(f"  step {step:8d}  residual {res:.6e}  mass {masses[-1]:.10f}", flush=True)
+            if callback is not None:
+                callback(step, res, self)
+            if res < tol:
                 converged = True
                 break
             if step >= tmax:
                 break
         sync(self.device)
         wall = time.perf_counter() - t0
-        return self._record(step, converged, np.array(residuals), np.array(masses), wall, scheme)
+        return self._record(step, converged, np.array(residuals), np.array(masses), wall, scheme,
+                            true_res=true_res if want_true else None)
 
-    def _record(self, iterations, converged, residuals, masses, wall, scheme, extra=None) -> RunRecord:
+    def _record(self, iterations, converged, residuals, masses, wall, scheme, extra=None,
+                true_res=None) -> RunRecord:
         c = self.case
         h = self.mom.host()
+        nfact = self.ndir * self.n_tris
+        if self.ctx.mode != "precomputed":
+            # pybte counts on-the-fly factorisations in its Krylov products only
+            nfact = nfact * self.ctx.sweep_count if scheme == "KRYLOV" else 0
         rec = RunRecord(iterations=int(iterations), converged=bool(converged),
-                        residual_history=np.asarray(residuals), mass_history=np.asarray(masses),
+                        residual_history=np.asarray(residuals),
+                        residual_true=np.asarray(true_res) if true_res is not None else None,
+                        mass_history=np.asarray(masses),
                         temp=h["temp"], qx=h["qx"], qy=h["qy"], temp_dofs=h["ts"], qx_dofs=h["qxs"],
-                        qy_dofs=h["qys"], sweep_count=self.ctx.sweep_count, wall_clock=wall,
-                        setup_wall_clock=self.setup_seconds, scheme=scheme, tol=c.iteration.tol,
-                        tau_r=c.flow.tau_r, tau_n=c.flow.tau_n, deg=c.dg.deg,
-                        npole=c.velmesh.npole, nazim=c.velmesh.nazim, n_tris=self.n_tris,
+                        qy_dofs=h["qys"], sweep_count=self.ctx.sweep_count, factorisation_count=int(nfact),
+                        wall_clock=wall, setup_wall_clock=self.setup_seconds, config_hash=c.config_hash,
+                        scheme=scheme, acc_variant=c.scheme.acc_variant if c.scheme.accflag == 1 else None,
+                        tol=c.iteration.tol, tmax=c.iteration.tmax, tau_r=c.flow.tau_r, tau_n=c.flow.tau_n,
+                        tau_c=c.tau_c, deg=c.dg.deg, npole=c.velmesh.npole, nazim=c.velmesh.nazim,
+                        n_tris=self.n_tris, n_faces=self.mesh.n_faces, mesh_file=str(c.mesh_path()),
+                        restart=dict(self.restart_info), environment=RunRecord.environment_fingerprint(),
                         precision=self.precision,
-                        diagnostics={"sweep_mode": self.ctx.mode, "n_classes": self.ctx.n_classes,
-                                     "n_levels_max": self.ctx.n_levels_max,
-                                     "device_bytes": self.ctx.device_bytes,
-                                     "boundary_types": [b.type for b in c.boundaries]})
+                        diagnostics={"sweep_mode": self.ctx.mode, "cycles_broken": 0,
+                                     "hmin": float(self.mesh.hmin), "n_faces_b": int(self.mesh.n_faces_b),
+                                     "boundary_types": [b.type for b in c.boundaries],
+                                     "n_classes": self.ctx.n_classes, "n_levels_max": self.ctx.n_levels_max,
+                                     "device_bytes": self.ctx.device_bytes})
+        if self.acc is not None and hasattr(self.acc, "diagnostics"):
+            rec.diagnostics.update(self.acc.diagnostics())
         if extra:
             rec.diagnostics.update(extra)
         return rec

@@ -261,6 +261,42 @@ int pbte_correct(pbte_ctx *ctx, double *vdf, const double *uq, const double *tri
 int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int32_t *singular,
                          void *stream);
 
+/* ---- field output (pybte/io_output.py:187-276) ---------------------------
+ * No context: these take the mesh, basis and state as plain device arrays,
+ * so they serve any solver's vdf.
+ *
+ * Angular moments per element DOF, the einsums of sample_fields
+ * (io_output.py:235-237): m[l*n_tris + i] = sum_d w[d] * vdf[d][i][l] for the
+ * weights w0 = domega, wx = cx*domega, wy = cy*domega. */
+int pbte_field_moments(const double *vdf, int32_t ndir, int32_t n_tris, int32_t ndof, const double *w0,
+                       const double *wx, const double *wy, double *m0, double *mx, double *my,
+                       void *stream);
+
+/* locate_points (io_output.py:187-217): out[i*ny + j] = the first element
+ * (lowest index) whose three sub-areas at (px[i], py[j]) are all >= -1e-12,
+ * or -1.  tri_x/tri_y: [n_tris][3] vertex coordinates.  The candidates come
+ * from an nbx x nby bin grid (origin x0, y0; bin sizes hx, hy): bin
+ * b = bx*nby + by lists bin_items[bin_start[b] .. bin_start[b+1]) in
+ * increasing element index; the bin of a coordinate v is
+ * clamp(floor((v - v0) / h), 0, nb - 1) and every element must be listed in
+ * each bin its box, widened past the -1e-12 slack, touches.  One bin holding
+ * every element is a plain scan. */
+int pbte_locate_points(const double *tri_x, const double *tri_y, int32_t n_tris, double x0, double y0,
+                       double hx, double hy, int32_t nbx, int32_t nby, const int32_t *bin_start,
+                       const int32_t *bin_items, const double *px, int32_t nx, const double *py,
+                       int32_t ny, int32_t *out, void *stream);
+
+/* sample_fields (io_output.py:220-276): T = (phi . m0) / cv, qx = phi . mx,
+ * qy = phi . my at every located point, and with uq (the GSIS macroscopic
+ * unknowns [7*ndof][n_tris], or NULL for zeros) the stress trio
+ * Nxx, Nxy, Nyy.  nodfun [ndof][ndof] and mono [ndof][2] are the basis's
+ * monomial coefficients and exponents.  out: [6][nx*ny] in the order
+ * T, qx, qy, Nxx, Nxy, Nyy; points with triid < 0 get zeros. */
+int pbte_sample_fields(const double *tri_x, const double *tri_y, const int32_t *triid, const double *px,
+                       int32_t nx, const double *py, int32_t ny, const double *nodfun, const int32_t *mono,
+                       int32_t ndof, const double *m0, const double *mx, const double *my, int32_t n_tris,
+                       double cv, const double *uq, double *out, void *stream);
+
 /* Version string of the built library. */
 const char *pbte_version(void);
 

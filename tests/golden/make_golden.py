@@ -12,7 +12,9 @@ The fixtures are plain arrays; nothing at test time reads the reference.
 """
 from __future__ import annotations
 
+import atexit
 import json
+import shutil
 import sys
 import tempfile
 from pathlib import Path
@@ -20,6 +22,13 @@ from pathlib import Path
 import numpy as np
 
 OUT = Path(__file__).resolve().parent
+
+
+def _scratch() -> Path:
+    """A temporary folder removed when the script exits."""
+    d = tempfile.mkdtemp()
+    atexit.register(shutil.rmtree, d, True)
+    return Path(d)
 
 
 def main(ref_root: str) -> None:
@@ -30,7 +39,7 @@ def main(ref_root: str) -> None:
     from pybte import krylov as rkrylov
     from pybte.acceleration import Acceleration  # noqa: F401  (import check)
 
-    tmp = Path(tempfile.mkdtemp())
+    tmp = _scratch()
     mesh5 = tmp / "A1_Nx6_Ny6.msh"
     mesh5.write_text(build(5, "cavity", "smootherstep"))
 
@@ -125,8 +134,105 @@ def main(ref_root: str) -> None:
                                "mass": index[key]["mass"]}
     np.savez_compressed(OUT / "task_solutions.npz",
                         **{f"{k}__{f}": v for k, d in keep.items() for f, v in d.items()})
+    meta.update(field_output(ref, case))
     (OUT / "golden_meta.json").write_text(json.dumps(meta, indent=1, sort_keys=True))
 
 
+def field_output(ref: Path, case) -> dict:
+    """4. Field output, restart file and writers (``pybte/io_output.py``,
+    ``pybte/driver.py:99-141``) on a converged GSIS solve, so the stress
+    trio is non-zero; plus the shipped 200-triangle mesh's nodes and
+    triangles, which the structured generator has to reproduce."""
+    from pybte import Solver
+    from pybte.io_output import (append_runtime_log, locate_points, sample_fields, sampling_grid,
+                                 write_tecplot)
+    from pybte.mesh.gmsh_reader import read_gmsh22
+
+    tmp = _scratch()
+    c = case(deg=2, npole=4, nazim=8, tau_r=0.1, tau_n=0.01, accflag=1)
+    c.basedir = str(tmp)
+    s = Solver(c)
+    rec = s.run()
+    px, py = sampling_grid()
+    tri = locate_points(s.mesh, px, py)
+    out = {"vdf": s.vdf, "uq": s.acc.uq, "px": px, "py": py, "triid": tri}
+    for k, v in zip(("T", "qx", "qy", "Nxx", "Nxy", "Nyy"),
+                    sample_fields(s.mesh, s.basis, s.vdf, s.ctx.cxv, s.ctx.cyv, s.ctx.domega,
+                                  c.flow.cv, px, py, tri, uq=s.acc.uq, ndof_tri=s.ndof)):
+        out[k] = v
+    # a coarse grid that reaches outside the square, without the stress trio, cv = 2
+    pxo, pyo = np.linspace(-0.05, 1.05, 23), np.linspace(-0.02, 1.02, 17)
+    trio = locate_points(s.mesh, pxo, pyo)
+    To, qxo, qyo, *_ = sample_fields(s.mesh, s.basis, s.vdf, s.ctx.cxv, s.ctx.cyv, s.ctx.domega,
+                                     2.0, pxo, pyo, trio)
+    out.update(pxo=pxo, pyo=pyo, triido=trio, To=To, qxo=qxo, qyo=qyo)
+    # writers: Tecplot text of the coarse grid, RunTime.txt lines, restart bytes
+    dat = write_tecplot(tmp / "field.dat", pxo, pyo, [To, qxo, qyo], ["T", "qx", "qy"])
+    out["tecplot"] = np.frombuffer(dat.read_bytes(), dtype=np.uint8)
+    log = tmp / "RunTime.txt"
+    for args in (("CIS", 1e-3, 1e5, 200, 20, 40, 183211, 48123.46),
+                 ("GSIS", 0.1, 0.01, 50, 4, 8, 17, 0.05),
+                 ("KRYLOV", 2.5e-7, 3e12, 20000, 10, 20, 9, 123456789.0)):
+        append_runtime_log(log, *args)
+    out["runtime_log"] = np.frombuffer(log.read_bytes(), dtype=np.uint8)
+    path = s.save_restart()
+    out["restart"] = np.frombuffer(path.read_bytes(), dtype=np.uint8)
+    # CIS restarted from that file (moments start at zero, the wall emission
+    # from the loaded distribution)
+    cr = case(deg=2, npole=4, nazim=8, tau_r=0.1, tau_n=0.01)
+    cr.basedir = str(tmp)
+    cr.restart.enabled = True
+    cr.restart.path = str(path)
+    sr = Solver(cr)
+    # pybte leaves the loaded distribution as a read-only view of the file's
+    # bytes, which its numpy sweep cannot write: run on a writable copy
+    sr.vdf = sr.vdf.copy()
+    rr = sr.run()
+    out["restart_cis_temp"] = rr.temp
+    out["restart_cis_residuals"] = rr.residual_history
+    d = rec.to_dict(include_fields=False)
+    out["record_keys"] = np.array(sorted(d))
+    out["residuals"] = rec.residual_history
+    shipped = read_gmsh22(ref / "solver-python" / "meshes" / "A1_Nx11_Ny11.msh")
+    tri_ids = np.flatnonzero(shipped.elem_type == 2)
+    line_ids = np.flatnonzero(shipped.elem_type == 1)
+    out["shipped_nodes"] = shipped.nodes[:, :2]
+    out["shipped_tri_nodes"] = np.array([shipped.elem_nodes[k] for k in tri_ids], dtype=np.int64)
+    out["shipped_line_nodes"] = np.array([shipped.elem_nodes[k] for k in line_ids], dtype=np.int64)
+    out["shipped_line_phyid"] = shipped.elem_phyid[line_ids]
+    np.savez_compressed(OUT / "field_output.npz", **out)
+    print("field output: restart", path.name, "iterations", rec.iterations, flush=True)
+    return {"field_output": {"deg": 2, "npole": 4, "nazim": 8, "tau_r": 0.1, "tau_n": 0.01,
+                             "accflag": 1, "iterations": int(rec.iterations),
+                             "restart_name": path.name, "restart_cis_iterations": int(rr.iterations),
+                             "contraction": rec.contraction, "error_estimate": rec.error_estimate,
+                             "final_residual": rec.final_residual}}
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if "--field-only" in sys.argv[2:]:
+        sys.path[:0] = [str(Path(ref_root) / "solver-python"), str(Path(ref_root) / "solver-python" / "tools")]
+        from make_meshes import build as _build
+        from pybte import Case as _Case
+
+        _tmp = _scratch()
+        (_tmp / "A1_Nx6_Ny6.msh").write_text(_build(5, "cavity", "smootherstep"))
+
+        def _case(deg, npole, nazim, tau_r, tau_n, accflag=0):
+            return _Case.from_dict({
+                "iteration": {"tol": 1e-8, "tmax": 20000}, "scheme": {"accflag": accflag},
+                "velmesh": {"npole": npole, "nazim": nazim}, "dg": {"deg": deg},
+                "flow": {"cv": 1.0, "vg": 1.0, "tau_r": tau_r, "tau_n": tau_n, "tau_thr": 1.0},
+                "mesh": {"file": str(_tmp / "A1_Nx6_Ny6.msh")},
+                "boundaries": [{"name": "SWall", "phyid": 11, "type": "nonthermalising", "temp": 0.0},
+                               {"name": "NWall", "phyid": 12, "type": "thermalising", "temp": 1.0},
+                               {"name": "EWall", "phyid": 13, "type": "thermalising", "temp": -0.5},
+                               {"name": "WWall", "phyid": 14, "type": "thermalising", "temp": 0.5}],
+                "output": {"field": False, "runtime_log": False, "run_record": False}}, basedir=str(_tmp))
+
+        m = json.loads((OUT / "golden_meta.json").read_text())
+        m.update(field_output(Path(ref_root), _case))
+        (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
+    else:
+        main(ref_root)
