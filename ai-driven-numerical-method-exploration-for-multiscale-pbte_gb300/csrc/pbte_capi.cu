@@ -17,10 +17,6 @@ int pbte_sweep(pbte_ctx *c, const double *ts, const double *qxs, const double *q
     if (!c || !ts || !qxs || !qys || !vdf) return PBTE_ERR_ARG;
     if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
     if (use_pbuf && !pbuf) return PBTE_ERR_ARG;
-    // Source iteration over periodic faces reads the partner "as of its place
-    // in the reference element order"; only the explicit-state form (pbuf) is
-    // implemented here.
-    if (c->has_periodic && !use_pbuf) return PBTE_ERR_UNSUPPORTED;
     int rc = pbte::launch_sources(c, ts, qxs, qys, false, S(stream));
     if (rc) return rc;
     return pbte::launch_sweep64(c, vdf, flux_wall, pbuf, use_pbuf, S(stream));
@@ -120,8 +116,23 @@ int pbte_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, co
                             double *den, void *stream) {
     if (!c || !ts || !qxs || !qys || !vdf || !num || !den) return PBTE_ERR_ARG;
     if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
-    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
     return pbte::launch_transport_residual(c, ts, qxs, qys, vdf, flux_wall, pbuf, num, den, S(stream));
+}
+
+int pbte_periodic_count(const pbte_ctx *c, int64_t *n_pfaces) {
+    if (!c || !n_pfaces) return PBTE_ERR_ARG;
+    *n_pfaces = c->n_pfaces;
+    return PBTE_OK;
+}
+
+int pbte_periodic_gather(pbte_ctx *c, const double *vdf, double *out, void *stream) {
+    if (!c || !vdf || (c->n_pfaces && !out)) return PBTE_ERR_ARG;
+    return pbte::launch_periodic_copy(c, vdf, out, 0, S(stream));
+}
+
+int pbte_periodic_scatter(pbte_ctx *c, const double *in, double *pbuf, void *stream) {
+    if (!c || (c->n_pfaces && (!in || !pbuf))) return PBTE_ERR_ARG;
+    return pbte::launch_periodic_copy(c, in, pbuf, 1, S(stream));
 }
 
 int pbte_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, void *stream) {

@@ -43,38 +43,92 @@ int alloc(size_t n, T **d, size_t *bytes) {
 
 int8_t sgn(double v) { return v > 0.0 ? 1 : (v < 0.0 ? -1 : 0); }
 
-// Kahn levels of one direction's dependency graph.  Returns false on a cycle.
-bool levels_for(const pbte_case_desc *d, double cx, double cy, std::vector<int32_t> &level,
-                std::vector<int32_t> &indeg, std::vector<int32_t> &queue) {
+// Does face il of element i make it wait for the element behind the face in
+// this sweep?  Interior faces with inflow (c.n < 0 on i's side, as pybte's
+// ioflag) do; periodic faces do when marked fresh for the class.
+inline bool in_sweep_inflow(const pbte_case_desc *d, double cx, double cy, const uint8_t *fresh, int i, int il) {
+    const int nb = d->upwind_tri[i * 3 + il];
+    const int fc = d->tri_faces[i * 3 + il];
+    if (nb < 0) return false;
+    if (d->face_bc[fc] >= 0 && !(fresh && ((fresh[i] >> il) & 1))) return false;
+    return cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0;
+}
+
+// Kahn levels of one direction's dependency graph (level = 1 + the deepest
+// element it waits for).  Returns false on a cycle.
+bool levels_for(const pbte_case_desc *d, double cx, double cy, const uint8_t *fresh,
+                std::vector<int32_t> &level, std::vector<int32_t> &indeg, std::vector<int32_t> &queue,
+                std::vector<int32_t> &succ_ptr, std::vector<int32_t> &succ) {
     const int nt = d->n_tris;
     level.assign(nt, 0);
     indeg.assign(nt, 0);
+    succ_ptr.assign(nt + 1, 0);
     for (int i = 0; i < nt; ++i)
-        for (int il = 0; il < 3; ++il) {
-            int nb = d->upwind_tri[i * 3 + il];
-            int fc = d->tri_faces[i * 3 + il];
-            if (nb < 0 || d->face_bc[fc] >= 0) continue;  // walls and periodic faces: no in-sweep dependency
-            double s = cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il];
-            if (s < 0.0) indeg[i]++;
-        }
+        for (int il = 0; il < 3; ++il)
+            if (in_sweep_inflow(d, cx, cy, fresh, i, il)) {
+                indeg[i]++;
+                succ_ptr[d->upwind_tri[i * 3 + il] + 1]++;
+            }
+    for (int i = 0; i < nt; ++i) succ_ptr[i + 1] += succ_ptr[i];
+    succ.assign(succ_ptr[nt], 0);
+    std::vector<int32_t> fill(succ_ptr.begin(), succ_ptr.end() - 1);
+    for (int i = 0; i < nt; ++i)
+        for (int il = 0; il < 3; ++il)
+            if (in_sweep_inflow(d, cx, cy, fresh, i, il)) succ[fill[d->upwind_tri[i * 3 + il]]++] = i;
     queue.clear();
     for (int i = 0; i < nt; ++i)
         if (indeg[i] == 0) queue.push_back(i);
     size_t head = 0;
     while (head < queue.size()) {
-        int i = queue[head++];
-        for (int il = 0; il < 3; ++il) {
-            int nb = d->upwind_tri[i * 3 + il];
-            int fc = d->tri_faces[i * 3 + il];
-            if (nb < 0 || d->face_bc[fc] >= 0) continue;
-            double s = cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il];
-            if (s > 0.0) {  // i is upwind of nb across this face
-                level[nb] = std::max(level[nb], level[i] + 1);
-                if (--indeg[nb] == 0) queue.push_back(nb);
-            }
+        const int i = queue[head++];
+        for (int e = succ_ptr[i]; e < succ_ptr[i + 1]; ++e) {
+            const int j = succ[e];
+            level[j] = std::max(level[j], level[i] + 1);
+            if (--indeg[j] == 0) queue.push_back(j);
         }
     }
     return (int)queue.size() == nt;
+}
+
+// pybte's TRI_ORDER position of every element for one direction
+// (pybte/ordering.py:61-140, without cycle breaking): rescan the elements in
+// ascending index, emit each one with no incoming interior face left, and
+// clear the matching flag of its neighbours at once, so a later element of
+// the same scan can follow it.  Returns false on a cycle.
+bool reference_order(const pbte_case_desc *d, double cx, double cy, std::vector<int32_t> &pos) {
+    const int nt = d->n_tris;
+    std::vector<int8_t> io((size_t)nt * 3, 0);
+    for (int i = 0; i < nt; ++i)
+        for (int il = 0; il < 3; ++il) {
+            const int fc = d->tri_faces[i * 3 + il];
+            if (d->upwind_tri[i * 3 + il] < 0 || d->face_bc[fc] >= 0) continue;
+            const double flux = cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il];
+            io[i * 3 + il] = flux > 0.0 ? 1 : (flux < 0.0 ? -1 : 0);
+        }
+    std::vector<char> queued(nt, 1);
+    pos.assign(nt, -1);
+    int num = 0;
+    while (num < nt) {
+        bool progressed = false;
+        for (int i = 0; i < nt; ++i) {
+            if (!queued[i] || io[i * 3] == -1 || io[i * 3 + 1] == -1 || io[i * 3 + 2] == -1) continue;
+            pos[i] = num++;
+            queued[i] = 0;
+            progressed = true;
+            for (int il = 0; il < 3; ++il) {
+                const int fc = d->tri_faces[i * 3 + il];
+                const int t2 = d->upwind_tri[i * 3 + il];
+                if (t2 < 0 || d->face_bc[fc] >= 0) continue;
+                for (int k = 0; k < 3; ++k)
+                    if (d->face_bc[d->tri_faces[t2 * 3 + k]] < 0 && d->upwind_tri[t2 * 3 + k] == i) {
+                        io[t2 * 3 + k] = 0;
+                        break;
+                    }
+            }
+        }
+        if (!progressed) return false;
+    }
+    return true;
 }
 
 }  // namespace
@@ -87,7 +141,8 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_piv, c->d_red, c->d_singular, c->d_up_slot, c->d_class_W, c->d_class_R,
                     c->d_udir_rep, c->d_udir_twin, c->d_rf64, c->d_rf32, c->d_ri, c->d_mom_part,
                     c->d_cx32, c->d_cy32, c->d_w32, c->d_udir_of, c->d_uw32, c->d_ucx32, c->d_ucy32,
-                    c->d_uw64, c->d_ucx64, c->d_ucy64};
+                    c->d_uw64, c->d_ucx64, c->d_ucy64, c->d_fresh, c->d_pface, c->d_ptri, c->d_pslot,
+                    c->d_psnap};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -199,12 +254,33 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     c->n_wall_ad = (int)walls.size();
     TRY(upload(walls.data(), walls.size(), &c->d_wall_ad, &c->device_bytes));
 
+    // ---- periodic faces ---------------------------------------------------
+    std::vector<int32_t> pface, ptri, pslot(d->n_faces, -1);
+    for (int f = 0; f < d->n_faces; ++f) {
+        const int bc = d->face_bc[f];
+        if (bc < 0 || d->bc_type[bc] != 3) continue;
+        const int side = d->face_tri[f * 2 + 0] >= 0 ? 0 : 1;
+        const int t = d->face_tri[f * 2 + side], l = d->face_lfc[f * 2 + side];
+        const int partner = d->upwind_tri[t * 3 + l];
+        if (partner < 0 || partner >= nt) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+        pslot[f] = (int32_t)pface.size();
+        pface.push_back(f);
+        ptri.push_back(partner);
+    }
+    c->n_pfaces = (int)pface.size();
+    if (c->n_pfaces) {
+        TRY(upload(pface.data(), pface.size(), &c->d_pface, &c->device_bytes));
+        TRY(upload(ptri.data(), ptri.size(), &c->d_ptri, &c->device_bytes));
+        TRY(upload(pslot.data(), pslot.size(), &c->d_pslot, &c->device_bytes));
+        TRY(alloc((size_t)ndir * c->n_pfaces * nd, &c->d_psnap, &c->device_bytes));
+    }
+
     // ---- direction classes and wavefront levels -------------------------
-    // sign pattern of c.n over the interior faces, hashed (FNV-1a) and then
-    // compared in full against the class representative
+    // sign pattern of c.n over the interior and periodic faces, hashed
+    // (FNV-1a) and then compared in full against the class representative
     std::vector<int32_t> iface_tri, iface_lfc;
     for (int f = 0; f < d->n_faces; ++f)
-        if (d->face_bc[f] < 0) {
+        if (d->face_bc[f] < 0 || pslot[f] >= 0) {
             int t = d->face_tri[f * 2 + 0] >= 0 ? d->face_tri[f * 2 + 0] : d->face_tri[f * 2 + 1];
             int l = d->face_tri[f * 2 + 0] >= 0 ? d->face_lfc[f * 2 + 0] : d->face_lfc[f * 2 + 1];
             iface_tri.push_back(t);
@@ -250,9 +326,28 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     // ring of upwind values in shared memory: slot (level % R) * W + position,
     // R = 1 + the largest level gap of an in-sweep dependency, W = widest level
     std::vector<int32_t> up_slot((size_t)c->nclass * nt * 3, -1), class_W(c->nclass), class_R(c->nclass);
+    std::vector<uint8_t> fresh(c->n_pfaces ? (size_t)c->nclass * nt : 0, 0);
+    std::vector<int32_t> succ_ptr, succ, rpos;
     for (int k = 0; k < c->nclass; ++k) {
         int dir = class_rep[k];
-        if (!levels_for(d, d->cxv[dir], d->cyv[dir], level, indeg, queue)) {
+        uint8_t *fr = c->n_pfaces ? fresh.data() + (size_t)k * nt : nullptr;
+        if (fr) {
+            // a periodic inflow reads this sweep's partner value when the
+            // partner comes first in pybte's order for these directions
+            if (!reference_order(d, d->cxv[dir], d->cyv[dir], rpos)) {
+                pbte_ctx_destroy(c);
+                return PBTE_ERR_CYCLE;
+            }
+            for (int i = 0; i < nt; ++i)
+                for (int il = 0; il < 3; ++il) {
+                    const int fc = d->tri_faces[i * 3 + il];
+                    if (pslot[fc] < 0) continue;
+                    const int p = d->upwind_tri[i * 3 + il];
+                    const double s = d->cxv[dir] * d->nx[i * 3 + il] + d->cyv[dir] * d->ny[i * 3 + il];
+                    if (s < 0.0 && rpos[p] < rpos[i]) fr[i] |= (uint8_t)(1u << il);
+                }
+        }
+        if (!levels_for(d, d->cxv[dir], d->cyv[dir], fr, level, indeg, queue, succ_ptr, succ)) {
             pbte_ctx_destroy(c);
             return PBTE_ERR_CYCLE;
         }
@@ -277,11 +372,9 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         int R = 1;
         const double cx = d->cxv[dir], cy = d->cyv[dir];
         for (int i = 0; i < nt; ++i)
-            for (int il = 0; il < 3; ++il) {
-                int nb = d->upwind_tri[i * 3 + il], fc = d->tri_faces[i * 3 + il];
-                if (nb < 0 || d->face_bc[fc] >= 0) continue;
-                if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0) R = std::max(R, level[i] - level[nb] + 1);
-            }
+            for (int il = 0; il < 3; ++il)
+                if (in_sweep_inflow(d, cx, cy, fr, i, il))
+                    R = std::max(R, level[i] - level[d->upwind_tri[i * 3 + il]] + 1);
         R = std::min(R, kNearDepth);
         class_W[k] = W;
         class_R[k] = R;
@@ -290,15 +383,13 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         for (int i = 0; i < nt; ++i) {
             size_t p = (size_t)k * nt + count[level[i]] + pos[i];
             for (int il = 0; il < 3; ++il) {
-                int nb = d->upwind_tri[i * 3 + il], fc = d->tri_faces[i * 3 + il];
-                if (nb < 0 || d->face_bc[fc] >= 0) continue;
-                if (cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il] < 0.0) {
-                    if (level[i] - level[nb] < R) {
-                        up_slot[p * 3 + il] = (level[nb] % R) * W + pos[nb];
-                    } else {
-                        if (far_idx[nb] < 0) far_idx[nb] = nfar++;
-                        up_slot[p * 3 + il] = -2 - far_idx[nb];
-                    }
+                if (!in_sweep_inflow(d, cx, cy, fr, i, il)) continue;
+                const int nb = d->upwind_tri[i * 3 + il];
+                if (level[i] - level[nb] < R) {
+                    up_slot[p * 3 + il] = (level[nb] % R) * W + pos[nb];
+                } else {
+                    if (far_idx[nb] < 0) far_idx[nb] = nfar++;
+                    up_slot[p * 3 + il] = -2 - far_idx[nb];
                 }
             }
         }
@@ -328,7 +419,8 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
                 for (int b = 0; b < nf; ++b) packed |= (uint32_t)(a.emap[il][b] & 15) << (4 * b);
                 ri[(pbte::kIEmp + il) * M + kp] = (int32_t)packed;
                 ri[(pbte::kIFace + il) * M + kp] = a.face[il];
-                kinds |= (uint32_t)(uint8_t)a.kind[il] << (8 * il);
+                const int kind = (a.kind[il] == 3 && fr && ((fr[i] >> il) & 1)) ? 4 : a.kind[il];
+                kinds |= (uint32_t)(uint8_t)kind << (8 * il);
             }
             ri[pbte::kICell * M + kp] = i;
             ri[pbte::kIFarOut * M + kp] = far_idx[i];
@@ -390,6 +482,7 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     TRY(upload(class_R.data(), class_R.size(), &c->d_class_R, &c->device_bytes));
     TRY(upload(urep.data(), urep.size(), &c->d_udir_rep, &c->device_bytes));
     TRY(upload(utwin.data(), utwin.size(), &c->d_udir_twin, &c->device_bytes));
+    if (!fresh.empty()) TRY(upload(fresh.data(), fresh.size(), &c->d_fresh, &c->device_bytes));
 
     // ---- scratch ----------------------------------------------------------
     TRY(alloc((size_t)3 * nd * nt, &c->d_S64, &c->device_bytes));

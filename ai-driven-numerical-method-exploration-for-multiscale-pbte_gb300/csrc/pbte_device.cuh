@@ -33,8 +33,13 @@ struct SweepParams {
     const T *S;    // [n_tris][3][NP]
     T *vdf;        // [ndir][n_tris][NP]
     const double *flux_wall;
+    // periodic inflow not read from vdf: row pslot[face] (or face, when pslot
+    // is null) of pbuf, which has pb_rows rows of NP values per ordinate
     const double *pbuf;
-    int use_pbuf;
+    const int32_t *pslot;
+    int pb_rows;
+    int use_pbuf;             // 1: every periodic face reads pbuf (explicit state)
+    const uint8_t *fresh;     // [nclass][nt] periodic faces read from vdf when use_pbuf == 0
     const double *cx, *cy;
     const int32_t *dir_class, *class_off, *class_nlev, *lvl_ptr, *lvl_cells;
     const double *lu;       // stored factors, factor_base() layout
@@ -76,11 +81,13 @@ __device__ __forceinline__ void assemble(const T *sref, const Rec &r, T cx, T cy
     }
 }
 
-// Right-hand side: Callaway source from the moment sources plus the upwind inflow.
+// Right-hand side: Callaway source from the moment sources plus the upwind
+// inflow.  fresh: bit il set when a periodic face il reads the partner's row
+// of f (unless P.use_pbuf), else it reads pbuf.
 template <typename T, int DEG>
 __device__ __forceinline__ void rhs(const SweepParams<T> &P, const T *sref, const CellRec<T> &r, int i,
                                     int d, T cx, T cy, const T (&s)[3], const T *f,
-                                    T (&b)[Shape<DEG>::NP]) {
+                                    T (&b)[Shape<DEG>::NP], unsigned fresh) {
     constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
     const T *S = P.S + (size_t)i * 3 * NP;
 #pragma unroll
@@ -93,8 +100,9 @@ __device__ __forceinline__ void rhs(const SweepParams<T> &P, const T *sref, cons
         const int kind = r.kind[il];
         if (kind == 0 || kind == 3) {
             T g[NF];
-            if (kind == 3 && P.use_pbuf) {
-                const double *pb = P.pbuf + ((size_t)d * P.n_faces + r.face[il]) * NP;
+            if (kind == 3 && (P.use_pbuf || !((fresh >> il) & 1u))) {
+                const int row = P.pslot ? P.pslot[r.face[il]] : r.face[il];
+                const double *pb = P.pbuf + ((size_t)d * P.pb_rows + row) * NP;
 #pragma unroll
                 for (int bb = 0; bb < NF; ++bb) g[bb] = (T)pb[r.emap[il][bb]];
             } else {

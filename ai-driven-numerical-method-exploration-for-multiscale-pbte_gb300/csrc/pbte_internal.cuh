@@ -40,7 +40,10 @@ struct alignas(16) CellRec {
 // ((level % R) * W + position); <= -2 far slot -(up + 2).
 // far_out: far slot this element's values must also be kept in, or -1.
 // emp[il]: emap[il][0..nf-1] packed four bits each (nd <= 15).
-// kind: kind[il] in byte il.
+// kind: kind[il] in byte il; the records add kind 4, a periodic face whose
+// partner precedes the element in the reference's sweep order (its inflow is
+// this sweep's value, read like an interior neighbour's), while kind 3 there
+// is a periodic face read from the previous sweep's values.
 enum RecReal { kRA2 = 0, kRGxa, kRGxb, kRGya, kRGyb, kREs, kRNx = kREs + 3, kRNy = kRNx + 3,
                kRBval = kRNy + 3, kNumRecReal = kRBval + 3 };
 enum RecInt { kICell = 0, kIFarOut, kIUp, kIEmp = kIUp + 3, kIFace = kIEmp + 3, kIKind = kIFace + 3,
@@ -119,6 +122,17 @@ struct pbte_ctx {
     int far_max = 0;
     double *d_mom_part = nullptr;   // [ceil(ndir/32)][3][n_tris*ndof] moment partial sums
     float *d_cx32 = nullptr, *d_cy32 = nullptr, *d_w32 = nullptr;   // ordinates in FP32
+    // Periodic faces.  pybte's source-iteration sweep reads the partner's
+    // current values, i.e. this sweep's when the partner comes earlier in the
+    // direction's TRI_ORDER ("fresh": a dependency of the schedule) and the
+    // previous sweep's otherwise ("lagged": read from a snapshot taken before
+    // the sweep).  Sweeps over periodic faces are not z-twin folded: twins
+    // may see different partner values.
+    uint8_t *d_fresh = nullptr;     // [nclass][n_tris]: bit il set when face il reads a fresh partner
+    int n_pfaces = 0;               // periodic faces, in increasing face index
+    int32_t *d_pface = nullptr, *d_ptri = nullptr;  // [n_pfaces]: face, partner element behind it
+    int32_t *d_pslot = nullptr;     // [n_faces]: row of a periodic face in the compact buffers, else -1
+    double *d_psnap = nullptr;      // [ndir][n_pfaces][nd]: partner values before a source-iteration sweep
 };
 
 // launchers (pbte_kernels.cu)
@@ -160,6 +174,9 @@ int launch_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri
                    double *temp, double *qx, double *qy, cudaStream_t s);
 int launch_batched_inverse(const double *a, double *inv, int n, int m, int32_t *singular,
                            cudaStream_t s);
+// partner values of the periodic faces: mode 0 vdf -> compact [ndir][n_pfaces][nd]
+// (gather), mode 1 compact -> full pbuf [ndir][n_faces][nd] rows (scatter)
+int launch_periodic_copy(pbte_ctx *c, const double *src, double *dst, int mode, cudaStream_t s);
 }  // namespace pbte
 
 #define PBTE_CUDA_TRY(expr)                                  \

@@ -41,7 +41,7 @@ __global__ void __launch_bounds__(kSweepThreads) sweep_kernel(SweepParams<T> P) 
 #pragma unroll
             for (int il = 0; il < 3; ++il) s[il] = cx * r.nx[il] + cy * r.ny[il];
             T b[NP];
-            rhs<T, DEG>(P, sref, r, i, d, cx, cy, s, f, b);
+            rhs<T, DEG>(P, sref, r, i, d, cx, cy, s, f, b, P.fresh ? P.fresh[(size_t)cls * P.nt + i] : 0u);
             if constexpr (PRECOMP) {
                 const int u = P.udir_of[d], p = k - cls * P.nt;
                 const double *lu = P.lu + factor_base(u, p, P.nt, NP * NP);
@@ -496,7 +496,8 @@ __global__ void transport_residual_kernel(SweepParams<double> P, double *num, do
         double s[3];
         for (int il = 0; il < 3; ++il) s[il] = cx * r.nx[il] + cy * r.ny[il];
         double b[NP];
-        rhs<double, DEG>(P, sref, r, i, d, cx, cy, s, f, b);
+        // no sweep here: every periodic partner's current row is final
+        rhs<double, DEG>(P, sref, r, i, d, cx, cy, s, f, b, 7u);
         double A[NP][NP];
         assemble<double, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A);
         const double *fi = f + (size_t)i * NP;
@@ -686,6 +687,9 @@ static SweepParams<T> make_params(pbte_ctx *c) {
     P.udir_of = c->d_udir_of;
     P.store_twin = 1;
     P.by_udir = 0;
+    P.fresh = c->d_fresh;
+    P.pslot = nullptr;
+    P.pb_rows = c->n_faces;
     P.singular = c->d_singular; P.done = c->done;
     P.nt = c->n_tris; P.n_faces = c->n_faces;
     P.inv_tau_c = (T)(1.0 / c->tau_c);
@@ -752,13 +756,46 @@ static int sweep_dispatch(pbte_ctx *c, SweepParams<T> P, cudaStream_t s) {
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
+// One thread per (ordinate, periodic face, DOF).  mode 0: the partner rows of
+// vdf [ndir][nt][nd] into the compact [ndir][n_pfaces][nd]; mode 1: compact
+// into the periodic-face rows of a full pbuf [ndir][n_faces][nd].
+__global__ void periodic_copy_kernel(const double *src, double *dst, const int32_t *pface, const int32_t *ptri,
+                                     int ndir, int npf, int nt, int nfaces, int nd, int mode, const int32_t *done) {
+    if (stopped(done)) return;
+    const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)ndir * npf * nd;
+    if (t >= total) return;
+    const int l = (int)(t % nd);
+    const int q = (int)((t / nd) % npf);
+    const int d = (int)(t / ((size_t)nd * npf));
+    if (mode == 0) dst[t] = src[((size_t)d * nt + ptri[q]) * nd + l];
+    else dst[((size_t)d * nfaces + pface[q]) * nd + l] = src[t];
+}
+
+int launch_periodic_copy(pbte_ctx *c, const double *src, double *dst, int mode, cudaStream_t s) {
+    if (c->n_pfaces == 0) return PBTE_OK;
+    const size_t total = (size_t)c->ndir * c->n_pfaces * c->nd;
+    const int th = 256;
+    periodic_copy_kernel<<<(unsigned)((total + th - 1) / th), th, 0, s>>>(
+        src, dst, c->d_pface, c->d_ptri, c->ndir, c->n_pfaces, c->n_tris, c->n_faces, c->nd, mode, c->done);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
 int launch_sweep64(pbte_ctx *c, double *vdf, const double *fw, const double *pbuf, int use_pbuf,
                    cudaStream_t s) {
     SweepParams<double> P = make_params<double>(c);
     P.cells = c->d_cells64; P.ref = c->d_ref64; P.S = c->d_S64; P.vdf = vdf;
     P.flux_wall = fw; P.pbuf = pbuf; P.use_pbuf = use_pbuf;
     P.lu = c->d_lu; P.piv = c->d_piv;
-    if (c->sweep_variant != 1 && !use_pbuf) {
+    if (c->has_periodic && !use_pbuf) {
+        // source iteration: lagged partners read the values before this sweep
+        const int rc = launch_periodic_copy(c, vdf, c->d_psnap, 0, s);
+        if (rc) return rc;
+        P.pbuf = c->d_psnap;
+        P.pslot = c->d_pslot;
+        P.pb_rows = c->n_pfaces;
+    }
+    if (c->sweep_variant != 1) {
         const int rc = c->d_lu ? launch_ring<double, true>(c, P, s) : launch_ring<double, false>(c, P, s);
         if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant >= 2) return rc;
     }
@@ -992,10 +1029,13 @@ int launch_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri
 
 int launch_batched_inverse(const double *a, double *inv, int n, int m, int32_t *singular, cudaStream_t s) {
     if (n <= 0) return PBTE_OK;
-    if (m <= 0 || m > 64) return PBTE_ERR_ARG;
-    const int warps = 4;
-    const size_t shm = (size_t)warps * m * 2 * m * sizeof(double);
-    if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
+    if (m <= 0) return PBTE_ERR_ARG;
+    // one warp per matrix, its [m][2m] augmented copy in shared memory: up to
+    // four warps a block while they fit (m = 7 N_p: 70 at P3, 105 at P4)
+    const size_t per_warp = (size_t)m * 2 * m * sizeof(double);
+    if (per_warp > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
+    const int warps = (int)std::max<size_t>(1, std::min<size_t>(4, (200 * 1024) / per_warp));
+    const size_t shm = (size_t)warps * per_warp;
     if (shm > 48 * 1024 &&
         cudaFuncSetAttribute(batched_inverse_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
         return PBTE_ERR_CUDA;

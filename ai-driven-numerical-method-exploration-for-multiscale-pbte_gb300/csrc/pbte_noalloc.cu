@@ -58,7 +58,6 @@ extern "C" int pbte_transport_residual_noalloc(pbte_ctx *c, const double *ts, co
                                                double *num, double *den, void *stream) {
     if (!c || !ts || !qxs || !qys || !vdf || !num || !den) return PBTE_ERR_ARG;
     if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
-    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
     if (3LL * c->nd * c->n_tris > kScratchDoubles) return PBTE_ERR_ARG;
     double *S = scratch_address();
     if (!S) return PBTE_ERR_CUDA;

@@ -46,6 +46,7 @@ struct RingParams {
     const int32_t *udir_rep, *udir_twin;
     int groups;
     int far_offset;             // start of the far slots, in values of T past the ring
+    int unfold;                 // one block per ordinate (no twin store): periodic faces
 };
 
 __device__ __forceinline__ void bar_sync(int id, int n) { asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(n) : "memory"); }
@@ -109,8 +110,9 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
     const T *__restrict__ rf = reinterpret_cast<const T *>(Q.rf);
     const int32_t *__restrict__ ri = Q.ri;
     const int64_t M = Q.stride;
-    const int u = blockIdx.x;
-    const int d = Q.udir_rep[u], d2 = Q.udir_twin[u];
+    const int u = Q.unfold ? P.udir_of[blockIdx.x] : (int)blockIdx.x;
+    const int d = Q.unfold ? (int)blockIdx.x : Q.udir_rep[u];
+    const int d2 = Q.unfold ? -1 : Q.udir_twin[u];
     for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
     __syncthreads();
     const T cx = (T)P.cx[d], cy = (T)P.cy[d];
@@ -183,9 +185,14 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
                 const T *R = sref + (3 + il) * NP * NP;
                 const int kind = (kinds >> (8 * il)) & 255u;
                 if (kind == 0) continue;
+                // a fresh periodic partner comes from the ring like an
+                // interior neighbour, unless the inflow is explicit state
+                if (kind == 4 && !P.use_pbuf) continue;
+                if (kind == 4) code[c][il] = -1;
                 const int face = __ldg(ri + (kIFace + il) * M + k);
-                if (kind == 3) {
-                    const double *pb = P.pbuf + ((size_t)d * P.n_faces + face) * NP;
+                if (kind == 3 || kind == 4) {
+                    const int row = P.pslot ? P.pslot[face] : face;
+                    const double *pb = P.pbuf + ((size_t)d * P.pb_rows + row) * NP;
 #pragma unroll
                     for (int a = 0; a < NF; ++a) {
                         const int ma = Shape<DEG>::edof(il, a);
@@ -367,7 +374,7 @@ static int ring_launch_cpt(pbte_ctx *c, const SweepParams<T> &P, const RingParam
         if (shm > 48 * 1024 &&
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
             return PBTE_ERR_CUDA;
-        kern<<<c->n_udir, threads, shm, s>>>(P, Q);
+        kern<<<Q.unfold ? c->ndir : c->n_udir, threads, shm, s>>>(P, Q);
         return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
     };
     switch (cpt) {
@@ -417,7 +424,8 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
     const void *rf = sizeof(T) == 4 ? (const void *)c->d_rf32 : (const void *)c->d_rf64;
     RingParams Q{rf, c->d_ri, (int64_t)c->nclass * c->n_tris, c->d_class_W, c->d_class_R,
-                 c->d_udir_rep, c->d_udir_twin, groups, (int)ring_vals};
+                 c->d_udir_rep, c->d_udir_twin, groups, (int)ring_vals, c->has_periodic ? 1 : 0};
+    if (Q.unfold && P.by_udir) return PBTE_ERR_UNSUPPORTED;
     if (width == 128) {
         switch (c->deg) {
             case 1: return ring_launch_cpt<T, 1, PRE, 128, 4>(c, P, Q, cpt, shm, s);

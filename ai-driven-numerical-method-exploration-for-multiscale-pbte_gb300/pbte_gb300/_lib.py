@@ -52,7 +52,9 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     for s in srcs:
         o = LIB_PATH.parent / (s.stem + ".o")
         objs.append(o)
-        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c",
+        # host code without FMA contraction: the schedule's inflow signs and
+        # pybte's element order are computed as numpy computes them
+        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off", "-c",
                f"-I{INCLUDE}", f"-I{CSRC}", str(s), "-o", str(o)]
         procs.append((cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)))
     for cmd, p in procs:
@@ -130,6 +132,9 @@ _SIGS = {
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],
                      ctypes.c_int),
     "pbte_batched_inverse": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+    "pbte_periodic_count": ([_vp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "pbte_periodic_gather": ([_vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_periodic_scatter": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_field_moments": ([_vp, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32] + [_vp] * 6 + [_vp],
                            ctypes.c_int),
     "pbte_locate_points": ([_vp, _vp, ctypes.c_int32, ctypes.c_double, ctypes.c_double, ctypes.c_double,

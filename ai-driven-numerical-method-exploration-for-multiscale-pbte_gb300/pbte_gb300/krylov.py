@@ -40,24 +40,30 @@ def uses_graphs(solver) -> bool:
 
 class FixedPointOperator:
     """``u -> F(u)``: scatter into the sweep's inputs, sweep, moments, wall
-    emission, gather (``pybte/krylov.py:64-136``).  Periodic faces are not
-    supported by the GPU sweep's source-iteration form and are refused."""
+    emission, gather (``pybte/krylov.py:64-136``).  The state is
+    ``[ts, qxs, qys]``, then the adiabatic-wall emission ``flux_wall`` when
+    there are adiabatic walls, then, with periodic faces, the partner
+    element's DOFs of every periodic face and ordinate (the sweep reads them
+    from ``ctx.pbuf``, so one sweep is a function of the state)."""
 
     def __init__(self, solver, precision: str = "fp64", homogeneous: bool = False, integrals: bool = True):
         s = solver
         self.integrals = integrals
-        if s.bcdata.has_periodic:
-            raise NotImplementedError("periodic faces: the Krylov state needs the partner DOFs")
         self.s = s
         self.nd, self.nt = s.ndof, s.n_tris
         self.k = self.nd * self.nt
         self.nmom = 3 * self.k
         self.wall = bool(s.bcdata.has_nonthermalising)
         self.nwall = s.mesh.n_faces * self.nd if self.wall else 0
-        self.n = self.nmom + self.nwall
+        self.per = bool(s.bcdata.has_periodic)
+        self.npf = int(np.count_nonzero(s.bcdata.periodic_tri >= 0)) if self.per else 0
+        if self.per and precision != "fp64":
+            raise NotImplementedError("periodic faces: the FP32 product has no periodic state")
+        self.nper = s.ndir * self.npf * self.nd
+        self.n = self.nmom + self.nwall + self.nper
         dev = s.device
         f64 = dict(dtype=torch.float64, device=dev)
-        self.uin = torch.zeros(self.n + (0 if self.wall else s.mesh.n_faces * self.nd), **f64)
+        self.uin = torch.zeros(self.n, **f64)
         self.uout = torch.zeros_like(self.uin)
         self.precision = precision
         self.homogeneous = homogeneous
@@ -70,31 +76,44 @@ class FixedPointOperator:
         self.stream = torch.cuda.Stream(device=dev)
 
     def _views(self, u):
-        k = self.k
+        """``(ts, qxs, qys, flux_wall or None, periodic block or None)``
+        views of a state-sized buffer."""
+        k, m, w = self.k, self.nmom, self.nwall
+        fw = u[m:m + w].view(-1, self.nd) if self.wall else None
+        per = u[m + w:].view(self.s.ndir, self.npf, self.nd) if self.per else None
         return (u[:k].view(self.nd, self.nt), u[k:2 * k].view(self.nd, self.nt),
-                u[2 * k:3 * k].view(self.nd, self.nt), u[3 * k:].view(-1, self.nd))
+                u[2 * k:3 * k].view(self.nd, self.nt), fw, per)
+
+    @staticmethod
+    def _ptr(t):
+        return t.data_ptr() if t is not None else None
 
     def _launch(self, s: int) -> None:
         L = _lib.lib()
         ctx = self.s.ctx.handle
-        ts, qxs, qys, fw = self._views(self.uin)
-        ots, oqxs, oqys, ofw = self._views(self.uout)
+        p = self._ptr
+        ts, qxs, qys, fw, per = self._views(self.uin)
+        ots, oqxs, oqys, ofw, oper = self._views(self.uout)
         if self.precision == "fp64":
+            pbuf = self.s.ctx.pbuf
+            if self.per:
+                _lib.check(L.pbte_periodic_scatter(ctx, per.data_ptr(), pbuf.data_ptr(), s), "periodic_scatter")
             _lib.check(L.pbte_sweep(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), self.vdf.data_ptr(),
-                                    fw.data_ptr(), self.s.ctx.pbuf.data_ptr(), 0, s), "sweep")
+                                    p(fw), pbuf.data_ptr(), int(self.per), s), "sweep")
             _lib.check(L.pbte_moments(ctx, self.vdf.data_ptr(), ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(),
                                       self.temp.data_ptr(), self.qx.data_ptr(), self.qy.data_ptr(), s), "moments")
             if self.wall:
                 _lib.check(L.pbte_wall_flux(ctx, self.vdf.data_ptr(), ofw.data_ptr(), s), "wall_flux")
+            if self.per:
+                _lib.check(L.pbte_periodic_gather(ctx, self.vdf.data_ptr(), oper.data_ptr(), s), "periodic_gather")
         else:
             # one call: sources, FP32 sweep, moments and emission with the
             # z-mirror twins folded (self.vdf is scratch here)
             ints = (self.temp.data_ptr(), self.qx.data_ptr(), self.qy.data_ptr()) if self.integrals \
                 else (None, None, None)
-            _lib.check(L.pbte_fixed_point_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), fw.data_ptr(),
+            _lib.check(L.pbte_fixed_point_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), p(fw),
                                               0.0 if self.homogeneous else 1.0, self.vdf.data_ptr(),
-                                              ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(),
-                                              ofw.data_ptr() if self.wall else None, *ints, s),
+                                              ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(), p(ofw), *ints, s),
                        "fixed_point_f32")
 
     def _capture(self):
@@ -111,7 +130,7 @@ class FixedPointOperator:
 
     def apply(self, u: torch.Tensor) -> torch.Tensor:
         """F(u), stream-ordered on the current stream."""
-        self.uin[:self.n].copy_(u)
+        self.uin.copy_(u)
         if uses_graphs(self.s):
             if self.graph is None:
                 self._capture()
@@ -119,7 +138,7 @@ class FixedPointOperator:
         else:
             self._launch(torch.cuda.current_stream().cuda_stream)
         self.sweeps += 1
-        return self.uout[:self.n].clone()
+        return self.uout.clone()
 
     def state(self) -> torch.Tensor:
         """The state of the solver's current ``vdf`` without sweeping: its
@@ -129,7 +148,7 @@ class FixedPointOperator:
         L = _lib.lib()
         st = torch.cuda.current_stream().cuda_stream
         u = torch.zeros_like(self.uin)
-        ts, qxs, qys, fw = self._views(u)
+        ts, qxs, qys, fw, per = self._views(u)
         m = s.mom
         _lib.check(L.pbte_moments(s.ctx.handle, s.vdf.data_ptr(), ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(),
                                   m.temp.data_ptr(), m.qx.data_ptr(), m.qy.data_ptr(), st), "moments")
@@ -139,12 +158,14 @@ class FixedPointOperator:
         if self.wall:
             _lib.check(L.pbte_wall_flux(s.ctx.handle, s.vdf.data_ptr(), fw.data_ptr(), st), "wall_flux")
             s.ctx.flux_wall.copy_(fw)
-        return u[:self.n].clone()
+        if self.per:
+            _lib.check(L.pbte_periodic_gather(s.ctx.handle, s.vdf.data_ptr(), per.data_ptr(), st), "periodic_gather")
+        return u
 
     def publish(self) -> None:
         """Copy the last product's moments into the solver's state."""
         s = self.s
-        ts, qxs, qys, fw = self._views(self.uout)
+        ts, qxs, qys, fw, _ = self._views(self.uout)
         s.mom.ts.copy_(ts)
         s.mom.qxs.copy_(qxs)
         s.mom.qys.copy_(qys)

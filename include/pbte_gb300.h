@@ -109,10 +109,25 @@ int pbte_ctx_info(const pbte_ctx *ctx, int64_t *n_levels_max, int64_t *n_classes
 /* One FP64 transport sweep, in place on vdf.  Replaces SweepContext.sweep
  * (pybte/sweep.py:132-158 -> _kernels.sweep_precomputed/_onthefly,
  * pybte/_kernels.py:218-269).  `pbuf`/`use_pbuf` as in the reference
- * (the Krylov path's periodic state); pbuf may be NULL when use_pbuf == 0. */
+ * (_kernels.py:170-215): with use_pbuf every periodic face reads its
+ * partner's row pbuf[d][face] (the Krylov path's explicit state); without,
+ * a periodic face reads the partner's current vdf as the reference's
+ * sequential sweep does -- this sweep's value when the partner comes first
+ * in the direction's TRI_ORDER, else the previous sweep's.  pbuf may be
+ * NULL when use_pbuf == 0. */
 int pbte_sweep(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
                double *vdf, const double *flux_wall, const double *pbuf, int use_pbuf,
                void *stream);
+
+/* Periodic faces of the context (faces with a periodic boundary, in
+ * increasing face index) and their partner elements' DOFs, the periodic
+ * block of the Krylov state (pybte/krylov.py:74-110):
+ * pbte_periodic_gather: out[d][q][l] = vdf[d][partner(q)][l];
+ * pbte_periodic_scatter: pbuf[d][face(q)][l] = in[d][q][l] (other rows of
+ * pbuf untouched).  q < *n_pfaces. */
+int pbte_periodic_count(const pbte_ctx *ctx, int64_t *n_pfaces);
+int pbte_periodic_gather(pbte_ctx *ctx, const double *vdf, double *out, void *stream);
+int pbte_periodic_scatter(pbte_ctx *ctx, const double *in, double *pbuf, void *stream);
 
 /* FP32 sweep (mixed precision): moments and wall emission read in FP64,
  * element solves and vdf32 in FP32.  With `wall_scale` = 0 the thermalising

@@ -209,9 +209,107 @@ def field_output(ref: Path, case) -> dict:
                              "final_residual": rec.final_residual}}
 
 
+def periodic(ref: Path) -> dict:
+    """5. Periodic faces on the 5 x 5 channel (north T = 1, south T = 0,
+    east/west a periodic pair): one seeded sweep in each of the reference's
+    two periodic forms (partner read from the current vdf, or from pbuf),
+    complete CIS / GSIS / GMRES(30) solves, the F3 task family's certified
+    solutions, and the shipped channel mesh."""
+    sys.path[:0] = [str(ref / "solver-python"), str(ref / "solver-python" / "tools")]
+    from make_meshes import build
+    from pybte import Case, Solver
+    from pybte import krylov as rkrylov
+    from pybte.mesh.gmsh_reader import read_gmsh22
+    from pybte.moments import compute_moments
+
+    tmp = _scratch()
+    msh = tmp / "C1_Nx6_Ny6.msh"
+    msh.write_text(build(5, "channel", "smootherstep", "uniform"))
+
+    def case(deg, npole, nazim, tau_r, tau_n, accflag=0, method="source"):
+        return Case.from_dict({
+            "iteration": {"tol": 1e-8, "tmax": 20000}, "scheme": {"accflag": accflag, "method": method},
+            "velmesh": {"npole": npole, "nazim": nazim}, "dg": {"deg": deg},
+            "flow": {"cv": 1.0, "vg": 1.0, "tau_r": tau_r, "tau_n": tau_n, "tau_thr": 1.0},
+            "mesh": {"file": str(msh)},
+            "boundaries": [{"name": "SWall", "phyid": 11, "type": "thermalising", "temp": 0.0},
+                           {"name": "NWall", "phyid": 12, "type": "thermalising", "temp": 1.0},
+                           {"name": "Master", "phyid": 13, "type": "periodic", "temp": 0.0, "xoff": -1.0},
+                           {"name": "Slave", "phyid": 14, "type": "periodic", "temp": 0.0, "xoff": 1.0}],
+            "output": {"field": False, "runtime_log": False, "run_record": False}}, basedir=str(tmp))
+
+    meta = {}
+    out = {}
+    for deg in (1, 2):
+        s = Solver(case(deg, 4, 8, 0.5, 0.05))
+        ctx = s.ctx
+        rng = np.random.default_rng(200 + deg)
+        nd, nt = s.ndof, s.n_tris
+        s.mom.ts[:] = rng.standard_normal((nd, nt))
+        s.mom.qxs[:] = 0.3 * rng.standard_normal((nd, nt))
+        s.mom.qys[:] = 0.3 * rng.standard_normal((nd, nt))
+        vdf0 = rng.standard_normal(s.vdf.shape)
+        pbuf = rng.standard_normal(ctx.pbuf.shape)
+        s.vdf[:] = vdf0
+        ctx.sweep(s.mom, s.vdf)
+        out[f"deg{deg}_vdf_in"] = vdf0
+        out[f"deg{deg}_vdf_cis"] = s.vdf.copy()
+        out[f"deg{deg}_true_residual"] = np.array(ctx.true_residual(s.mom, s.vdf))
+        s.vdf[:] = vdf0
+        ctx.pbuf[:] = pbuf
+        ctx.use_pbuf = True
+        ctx.sweep(s.mom, s.vdf)
+        ctx.use_pbuf = False
+        out[f"deg{deg}_pbuf"] = pbuf
+        out[f"deg{deg}_vdf_pbuf"] = s.vdf.copy()
+        out[f"deg{deg}_ts"], out[f"deg{deg}_qxs"], out[f"deg{deg}_qys"] = s.mom.ts, s.mom.qxs, s.mom.qys
+        out[f"deg{deg}_periodic_tri"] = s.bcdata.periodic_tri
+        meta[f"periodic_sweep_deg{deg}"] = {"deg": deg, "npole": 4, "nazim": 8, "tau_r": 0.5, "tau_n": 0.05,
+                                            "seed": 200 + deg}
+        print("periodic sweep deg", deg, flush=True)
+    runs = {"cis_deg1": dict(deg=1, npole=4, nazim=8, tau_r=1.0, tau_n=0.1),
+            "gsis_deg2": dict(deg=2, npole=4, nazim=8, tau_r=0.1, tau_n=0.01, accflag=1),
+            "krylov_deg2": dict(deg=2, npole=4, nazim=8, tau_r=0.1, tau_n=0.01, method="krylov")}
+    orig_cap = rkrylov.krylov_basis_cap
+    for name, kw in runs.items():
+        if kw.get("method") == "krylov":
+            rkrylov.krylov_basis_cap = lambda *a: 30
+        s = Solver(case(**kw))
+        rec = s.run()
+        rkrylov.krylov_basis_cap = orig_cap
+        for k, v in (("temp", rec.temp), ("qx", rec.qx), ("qy", rec.qy), ("ts", rec.temp_dofs),
+                     ("residuals", rec.residual_history)):
+            out[f"{name}_{k}"] = v
+        meta[f"periodic_{name}"] = {**kw, "iterations": int(rec.iterations), "mass": float(rec.mass),
+                                    "converged": bool(rec.converged)}
+        print("periodic", name, rec.iterations, rec.converged, rec.mass, flush=True)
+    task = ref / "tasks" / "t01-square"
+    index = json.loads((task / "reference" / "index.json").read_text())
+    for key in ("F3_1_1", "F3_1e-1"):
+        z = np.load(task / "reference" / f"{key}.npz")
+        for f in ("temp", "qx", "qy", "temp_dofs"):
+            out[f"task_{key}__{f}"] = z[f]
+        meta[f"task_{key}"] = {"iterations": index[key]["iterations"],
+                               "cis_iterations": index[key]["cis_iterations"], "mass": index[key]["mass"]}
+    shipped = read_gmsh22(ref / "solver-python" / "meshes" / "C1_Nx11_Ny11.msh")
+    tri_ids = np.flatnonzero(shipped.elem_type == 2)
+    line_ids = np.flatnonzero(shipped.elem_type == 1)
+    out["shipped_nodes"] = shipped.nodes[:, :2]
+    out["shipped_tri_nodes"] = np.array([shipped.elem_nodes[k] for k in tri_ids], dtype=np.int64)
+    out["shipped_line_nodes"] = np.array([shipped.elem_nodes[k] for k in line_ids], dtype=np.int64)
+    out["shipped_line_phyid"] = shipped.elem_phyid[line_ids]
+    np.savez_compressed(OUT / "periodic.npz", **out)
+    _ = compute_moments
+    return meta
+
+
 if __name__ == "__main__":
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if "--field-only" in sys.argv[2:]:
+    if "--periodic-only" in sys.argv[2:]:
+        m = json.loads((OUT / "golden_meta.json").read_text())
+        m.update(periodic(Path(ref_root)))
+        (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
+    elif "--field-only" in sys.argv[2:]:
         sys.path[:0] = [str(Path(ref_root) / "solver-python"), str(Path(ref_root) / "solver-python" / "tools")]
         from make_meshes import build as _build
         from pybte import Case as _Case

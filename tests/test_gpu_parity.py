@@ -261,6 +261,21 @@ def test_device_gmres_cycles_match_host_rotations(cuda, graphs):
     assert _rel(a.temp_dofs, b.temp_dofs) < 1e-10 and _rel(a.qx_dofs, b.qx_dofs) < 1e-10
 
 
+@pytest.mark.parametrize("m", [21, 42, 70, 105])
+def test_batched_inverse_sizes(cuda, m):
+    """The HDG element inverses (7 N_p: P1 21 ... P4 105) against LAPACK."""
+    from pbte_gb300 import _lib
+    rng = np.random.default_rng(m)
+    a = rng.standard_normal((9, m, m)) + m * np.eye(m)
+    ad = torch.from_numpy(a).to(cuda)
+    inv = torch.empty_like(ad)
+    bad = torch.zeros(1, dtype=torch.int32, device=cuda)
+    _lib.check(_lib.lib().pbte_batched_inverse(ad.data_ptr(), inv.data_ptr(), 9, m, bad.data_ptr(), None),
+               "batched_inverse")
+    assert int(bad.item()) == 0
+    assert _rel(inv.cpu().numpy(), np.linalg.inv(a)) < 1e-12
+
+
 def test_square_benchmark_mesh_levels(cuda):
     s = Solver(square_case(64, 2, 8, 32, tau_r=1.0, tmax=3))
     assert s.n_tris == 8192

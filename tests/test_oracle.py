@@ -5,9 +5,10 @@ tests/golden/make_golden.py from pybte), plus the certified task solutions."""
 import numpy as np
 import pytest
 
-from cases import case_from_meta, golden, meta, small_case, task_case
+from cases import case_from_meta, golden, meta, periodic_case, small_case, task_case
 from oracle.oracle import Oracle
 from pbte_gb300.discretisation import Discretisation
+from pbte_gb300.mesh import structured_square
 
 
 def _oracle_on_reference_arrays(deg):
@@ -65,17 +66,90 @@ def test_complete_solves_match_reference(name):
     assert abs(o.mass - float(z["masses"][-1])) < 1e-12
 
 
-@pytest.mark.parametrize("key", ["F1_1_1", "F1_1e-1", "F2_1_1", "F2_1e-1"])
+def _periodic_oracle(deg):
+    """The oracle on the periodic channel with the fixture's seeded state
+    (same draws, same order as make_golden.py)."""
+    z = golden("periodic")
+    o = Oracle(Discretisation.build(periodic_case(deg, 4, 8, 0.5, 0.05)), nthreads=2)
+    rng = np.random.default_rng(200 + deg)
+    o.ts[:] = rng.standard_normal(o.ts.shape)
+    o.qxs[:] = 0.3 * rng.standard_normal(o.ts.shape)
+    o.qys[:] = 0.3 * rng.standard_normal(o.ts.shape)
+    o.vdf[:] = rng.standard_normal(o.vdf.shape)
+    pbuf = rng.standard_normal(o.pbuf.shape)
+    return o, z, pbuf
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_periodic_sweeps_against_reference(deg):
+    """Both periodic forms of the reference sweep: the partner read from the
+    current distribution (fresh or lagged by its place in TRI_ORDER), and
+    from pbuf."""
+    o, z, pbuf = _periodic_oracle(deg)
+    assert np.array_equal(o.vdf, z[f"deg{deg}_vdf_in"]) and np.array_equal(pbuf, z[f"deg{deg}_pbuf"])
+    assert np.array_equal(o.arr["periodic_tri"], z[f"deg{deg}_periodic_tri"])
+    vdf0 = o.vdf.copy()
+    o.sweep()
+    ref = z[f"deg{deg}_vdf_cis"]
+    assert np.abs(o.vdf - ref).max() <= 1e-14 * np.abs(ref).max()
+    assert o.true_residual() == pytest.approx(float(z[f"deg{deg}_true_residual"]), rel=0.3, abs=1e-15)
+    o.vdf[:] = vdf0
+    o.pbuf[:] = pbuf
+    o.use_pbuf = True
+    o.sweep()
+    ref = z[f"deg{deg}_vdf_pbuf"]
+    assert np.abs(o.vdf - ref).max() <= 1e-14 * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("name", ["cis_deg1", "gsis_deg2", "krylov_deg2"])
+def test_periodic_solves_match_reference(name):
+    z = golden("periodic")
+    m = meta()[f"periodic_{name}"]
+    kw = {k: m[k] for k in ("deg", "npole", "nazim", "tau_r", "tau_n")}
+    o = Oracle(Discretisation.build(periodic_case(**kw, accflag=m.get("accflag", 0),
+                                                  method=m.get("method", "source"))), nthreads=2)
+    if m.get("method") == "krylov":
+        r = o.run_krylov(max_basis=30)
+        assert abs(r["iterations"] - m["iterations"]) <= 1
+    else:
+        r = o.run_source(gsis=bool(m.get("accflag")))
+        assert r["iterations"] == m["iterations"]
+    assert r["converged"]
+    tol = 1e-9 if m.get("method") == "krylov" else 1e-12
+    assert np.abs(o.temp - z[f"{name}_temp"]).max() <= tol * np.abs(z[f"{name}_temp"]).max()
+    assert abs(o.mass - m["mass"]) < 1e-10
+
+
+def test_shipped_channel_mesh_is_the_structured_generator():
+    """pybte's meshes/C1_Nx11_Ny11.msh (the F3 family's periodic channel) is
+    the 10 x 10 channel, uniform in x and smootherstep in y."""
+    z = golden("periodic")
+    raw = structured_square(10, "channel", "smootherstep", "uniform")
+    assert np.array_equal(raw.nodes, z["shipped_nodes"])
+    assert np.array_equal(raw.tri_nodes, z["shipped_tri_nodes"])
+    assert np.array_equal(raw.line_nodes, z["shipped_line_nodes"])
+    assert np.array_equal(raw.line_phyid, z["shipped_line_phyid"])
+
+
+def task_solution(key: str) -> np.ndarray:
+    """Certified temperatures of a task cell (F3 lives with the periodic
+    fixtures)."""
+    if key.startswith("F3"):
+        return golden("periodic")[f"task_{key}__temp"]
+    return golden("task_solutions")[f"{key}__temp"]
+
+
+@pytest.mark.parametrize("key", ["F1_1_1", "F1_1e-1", "F2_1_1", "F2_1e-1", "F3_1_1"])
 def test_task_certified_solutions(key):
     """The reference task's solutions (GMRES to 1e-10): same sweep count,
     fields within the task's own field-gap bar (1e-5; observed ~1e-12)."""
     fam, tau = key.split("_", 1)
-    sol = golden("task_solutions")
+    temp = task_solution(key)
     o = Oracle(Discretisation.build(task_case(fam, tau)), nthreads=4)
     r = o.run_krylov()
     want = meta()[f"task_{key}"]
     assert r["converged"]
     assert abs(r["iterations"] - want["iterations"]) <= 1
-    gap = np.abs(o.temp - sol[f"{key}__temp"]).max() / np.abs(sol[f"{key}__temp"]).max()
+    gap = np.abs(o.temp - temp).max() / np.abs(temp).max()
     assert gap < 1e-9
     assert abs(o.mass - want["mass"]) < 1e-10
