@@ -17,7 +17,7 @@ CSRC = PKG_ROOT / "csrc"
 INCLUDE = REPO_ROOT / "include"
 LIB_PATH = PKG_ROOT / "_build" / "libpbte_gb300.so"
 SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_krylov.cu", "pbte_capi.cu",
-           "pbte_noalloc.cu", "pbte_output.cu"]
+           "pbte_noalloc.cu", "pbte_output.cu", "pbte_trace.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0
@@ -132,6 +132,9 @@ _SIGS = {
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],
                      ctypes.c_int),
     "pbte_batched_inverse": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+    "pbte_nd_forward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp],
+                        ctypes.c_int),
+    "pbte_nd_backward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp], ctypes.c_int),
     "pbte_periodic_count": ([_vp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_periodic_gather": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_periodic_scatter": ([_vp, _vp, _vp, _vp], ctypes.c_int),

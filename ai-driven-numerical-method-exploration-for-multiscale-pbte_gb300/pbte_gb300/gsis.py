@@ -7,7 +7,9 @@ Per outer iteration, after the sweep (``acceleration/__init__.py:95-115``):
    inverses ``inv_aa_sol`` (batched product);
 2. trace right-hand side: ``BA_SOL @ AA_SRC`` from the one or two elements of
    each face, wall rows imposed from the kinetic wall traces (device);
-3. trace solve with the once-factorised global matrix;
+3. trace solve with the once-factorised global matrix: on the device from
+   nested-dissection multifrontal factors (:mod:`pbte_gb300.trace_nd`,
+   default), or SuperLU on the host (``performance.trace_solver = "host"``);
 4. local recovery ``UQ = AA_SRC + sum AA_TRACE @ U_TRACE`` (batched product);
 5. damped correction of the distribution and the moments (device kernel).
 
@@ -26,6 +28,7 @@ import torch
 
 from . import _lib
 from .constants import BC_NONTHERMALISING, BC_PERIODIC, BC_THERMALISING
+from .trace_nd import NestedDissectionSolver
 from .trace_solver import TraceSolver
 
 __all__ = ["GSIS", "local_blocks"]
@@ -206,7 +209,11 @@ class GSIS:
         K.eliminate_zeros()
         K.sort_indices()
         self.K = K
-        self.solver = TraceSolver(K, dev)
+        if c.performance.trace_solver == "device":
+            xy = m.nodes[m.face_nodes].mean(axis=1)
+            self.solver = NestedDissectionSolver(K, xy, nf3, dev)
+        else:
+            self.solver = TraceSolver(K, dev)
 
         # per-iteration bookkeeping (global_solve.py:88-117)
         self.p1 = (torch.from_numpy(p1_tri).to(dev), torch.from_numpy(p1_lfc).to(dev))

@@ -1,0 +1,300 @@
+"""Device solve of the GSIS trace system ``K x = b``
+(``pybte/acceleration/global_solve.py:120-195``, where pybte factorises
+``K`` once with SuperLU and runs its two triangular solves every iteration).
+
+``K`` has one dense ``b x b`` block (``b = 3 (deg + 1)``) for every pair of
+faces that share an element, and depends only on the geometry and the
+relaxation times, so it is factorised once, by nested dissection:
+
+* Ordering (host).  The faces are split recursively along the longer side
+  of their midpoints' box at the median; the faces of the left half that
+  touch the right half form the separator.  Every face is eliminated before
+  the faces of the separators above it (a post-order of the dissection
+  tree).
+* Multifrontal factorisation (device, dense library calls at setup).  A
+  tree node's *front* holds its own faces (fully summed) and its boundary
+  faces (neighbours eliminated later).  The front is assembled from the
+  blocks of ``K`` whose earlier-eliminated face is one of the node's own
+  (each block exactly once) plus its children's update matrices
+  (extend-add), then partially factorised: ``P F11 = L11 U11`` (partial
+  pivoting within the own faces), ``U12 = L11^-1 P F12``,
+  ``L21 = F21 U11^-1``, and ``F22 - L21 U12`` goes to the parent.
+* Solve operators.  The triangular factors are inverted once, so each
+  node's forward and backward steps are dense matrix-vector products:
+  ``G = [L11^-1 P ; -L21 L11^-1 P]`` maps the node's own right-hand side to
+  its forward values and the update of its boundary, and
+  ``H = [U11^-1, -U11^-1 U12]`` maps ``[forward values, x of the boundary]``
+  to the node's unknowns.
+
+The solve (``pbte_nd_forward`` / ``pbte_nd_backward``) walks the tree by
+height, one launch per height and direction; a node's right-hand side adds
+its children's updates in a fixed order, so the result is deterministic.
+At setup the device solve of a random right-hand side is checked against
+``K`` (relative residual below ``check_tol``).
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+import torch
+
+from . import _lib
+
+__all__ = ["NestedDissectionSolver", "dissect"]
+
+#: output rows of G or H per work item (one thread block)
+ROWS_PER_ITEM = 64
+
+
+def _ranges(ptr: np.ndarray, rows: np.ndarray):
+    """CSR entries of ``rows``: (owning position in ``rows``, entry index)."""
+    starts = ptr[rows]
+    lens = ptr[rows + 1] - starts
+    total = int(lens.sum())
+    owner = np.repeat(np.arange(rows.size), lens)
+    first = np.repeat(np.cumsum(lens) - lens, lens)
+    return owner, np.repeat(starts, lens) + (np.arange(total) - first)
+
+
+class _Node:
+    __slots__ = ("own", "children", "parent", "height", "bnd")
+
+    def __init__(self, own, children):
+        self.own = own
+        self.children = children
+        self.parent = None
+        self.height = 0
+        self.bnd = None
+
+
+def dissect(adj_ptr: np.ndarray, adj: np.ndarray, xy: np.ndarray, leaf: int = 32) -> list:
+    """Nested-dissection tree of a graph with vertex coordinates ``xy``
+    (CSR adjacency ``adj_ptr``/``adj``, no self loops); the nodes in
+    post-order (children first)."""
+    side = np.zeros(xy.shape[0], dtype=np.int8)     # scratch: 1 left, 2 right
+    order = []
+
+    def build(S):
+        if S.size <= leaf:
+            node = _Node(S, [])
+            order.append(node)
+            return node
+        ext = xy[S].max(axis=0) - xy[S].min(axis=0)
+        srt = S[np.argsort(xy[S, int(np.argmax(ext))], kind="stable")]
+        left, right = srt[:srt.size // 2], srt[srt.size // 2:]
+        side[left] = 1
+        side[right] = 2
+        owner, ent = _ranges(adj_ptr, left)
+        touches = np.zeros(left.size, dtype=bool)
+        touches[owner[side[adj[ent]] == 2]] = True
+        side[left] = 0
+        side[right] = 0
+        kids = [build(np.sort(p)) for p in (left[~touches], right) if p.size]
+        node = _Node(np.sort(left[touches]), kids)
+        for k in kids:
+            k.parent = node
+        order.append(node)
+        return node
+
+    build(np.arange(xy.shape[0]))
+    return order
+
+
+class NestedDissectionSolver:
+    """``solve(b) -> x`` for the trace matrix ``K`` (scipy sparse, face-major
+    blocks of size ``block``: unknown ``f * block + c``), on ``device``."""
+
+    def __init__(self, K, face_xy: np.ndarray, block: int, device, leaf: int = 32,
+                 check_tol: float | None = 1e-10):
+        K = sp.csr_matrix(K)
+        n_faces = face_xy.shape[0]
+        b = int(block)
+        if K.shape != (n_faces * b, n_faces * b):
+            raise ValueError("K does not have one block per face")
+        self.device = torch.device(device)
+        self.n = K.shape[0]
+        self.block = b
+        Kb = sp.bsr_matrix(K, blocksize=(b, b))
+        Kb.sort_indices()
+        KT = sp.bsr_matrix(K.T.tocsr(), blocksize=(b, b))
+        KT.sort_indices()
+        rows = np.repeat(np.arange(n_faces), np.diff(Kb.indptr))
+        A = sp.coo_matrix((np.ones(rows.size), (rows, Kb.indices)), shape=(n_faces, n_faces)).tocsr()
+        A = (A + A.T).tocsr()
+        A.setdiag(0)
+        A.eliminate_zeros()
+        A.sort_indices()
+        nodes = dissect(A.indptr, A.indices, np.asarray(face_xy, dtype=np.float64), leaf)
+        pos = np.empty(n_faces, dtype=np.int64)
+        ends = []
+        k = 0
+        for nd in nodes:
+            pos[nd.own] = np.arange(k, k + nd.own.size)
+            k += nd.own.size
+            ends.append(k)
+        for nd, k in zip(nodes, ends):
+            # boundary: neighbours of the own faces and the children's
+            # boundaries eliminated after this subtree
+            _, ent = _ranges(A.indptr, nd.own)
+            cand = np.unique(np.concatenate([A.indices[ent]] + [c.bnd for c in nd.children]))
+            nd.bnd = cand[pos[cand] >= k] if cand.size else cand
+            nd.height = 1 + max((c.height for c in nd.children), default=-1)
+        self.n_nodes = len(nodes)
+        self.height = max(nd.height for nd in nodes) + 1
+        self._layout(nodes, b)
+        self._factor(nodes, Kb, KT, b)
+        self.check_residual = self._check(K, check_tol) if check_tol is not None else None
+
+    # -- device layout -------------------------------------------------------
+    def _layout(self, nodes, b):
+        dev = self.device
+        comp = np.arange(b)
+        n_faces = self.n // b
+        loc = np.full(n_faces, -1, dtype=np.int64)
+        idx, meta, cptr, csrc = [], [], [], []
+        g_off = h_off = d_off = i_off = c_off = n_src = 0
+        delta_off = {}
+        for nd in nodes:
+            faces = np.concatenate([nd.own, nd.bnd])
+            o, m = nd.own.size * b, faces.size * b
+            loc[faces] = np.arange(faces.size)
+            # the children's boundary updates, by front position, children in order
+            tgt = [(loc[ch.bnd][:, None] * b + comp).ravel() for ch in nd.children]
+            src = [delta_off[id(ch)] + np.arange(ch.bnd.size * b) for ch in nd.children]
+            loc[faces] = -1
+            tgt = np.concatenate(tgt) if tgt else np.zeros(0, dtype=np.int64)
+            src = np.concatenate(src) if src else np.zeros(0, dtype=np.int64)
+            srt = np.argsort(tgt, kind="stable")
+            ptr = np.zeros(m + 1, dtype=np.int64)
+            np.cumsum(np.bincount(tgt, minlength=m), out=ptr[1:])
+            meta.append([i_off, o, m, g_off, h_off, d_off, c_off, 0])
+            delta_off[id(nd)] = d_off
+            idx.append((faces[:, None] * b + comp).ravel())
+            cptr.append(ptr + n_src)
+            csrc.append(src[srt])
+            n_src += src.size
+            i_off += m
+            g_off += m * o
+            h_off += o * m
+            d_off += m - o
+            c_off += m + 1
+        fwd = [[] for _ in range(self.height)]
+        bwd = [[] for _ in range(self.height)]
+        for i, nd in enumerate(nodes):
+            o, m = meta[i][1], meta[i][2]
+            fwd[nd.height] += [(i, r0, min(m, r0 + ROWS_PER_ITEM), 0) for r0 in range(0, m, ROWS_PER_ITEM)]
+            bwd[nd.height] += [(i, r0, min(o, r0 + ROWS_PER_ITEM), 0) for r0 in range(0, o, ROWS_PER_ITEM)]
+        self.levels = []
+        for h in range(self.height):
+            fo = max((meta[it[0]][1] for it in fwd[h]), default=0)
+            bm = max((meta[it[0]][2] for it in bwd[h]), default=0)
+            self.levels.append((torch.tensor(fwd[h] or [(0, 0, 0, 0)], dtype=torch.int32, device=dev), len(fwd[h]),
+                                int(fo), torch.tensor(bwd[h] or [(0, 0, 0, 0)], dtype=torch.int32, device=dev),
+                                len(bwd[h]), int(bm)))
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.meta_host = np.asarray(meta, dtype=np.int64)
+        self.meta = torch.from_numpy(self.meta_host).to(dev)
+        self.idx = torch.from_numpy(np.concatenate(idx).astype(np.int32)).to(dev)
+        self.cptr = torch.from_numpy(np.concatenate(cptr)).to(dev)
+        self.csrc = torch.from_numpy(np.concatenate(csrc + [np.zeros(1, np.int64)])).to(dev)
+        self.Gd = torch.empty(max(g_off, 1), **f64)
+        self.Hd = torch.empty(max(h_off, 1), **f64)
+        self.factor_entries = int(g_off + h_off)
+        self.max_front = int(max(mt[2] for mt in meta))
+        self.z = torch.zeros(self.n, **f64)
+        self.delta = torch.zeros(max(d_off, 1), **f64)
+
+    # -- factorisation -----------------------------------------------------------
+    def _factor(self, nodes, Kb, KT, b):
+        """Fronts assembled and factorised on ``self.device``; G and H written
+        into their slices of ``Gd`` / ``Hd``."""
+        dev = self.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        n_faces = Kb.shape[0] // b
+        loc = np.full(n_faces, -1, dtype=np.int64)
+        kb_data = torch.from_numpy(np.ascontiguousarray(Kb.data)).to(dev)
+        kt_data = torch.from_numpy(np.ascontiguousarray(np.transpose(KT.data, (0, 2, 1)))).to(dev)
+        upd = {}
+        for i, nd in enumerate(nodes):
+            _, o, m, g_off, h_off, *_ = (int(v) for v in self.meta_host[i])
+            faces = np.concatenate([nd.own, nd.bnd])
+            nf, no = faces.size, nd.own.size
+            loc[faces] = np.arange(nf)
+            Fp = torch.zeros((nf, nf, b, b), **f64)          # block (front face, front face)
+            if no:
+                # blocks K[own, front] from the rows, K[bnd, own] from the columns
+                owner, ent = _ranges(Kb.indptr, nd.own)
+                c = loc[Kb.indices[ent]]
+                keep = np.flatnonzero(c >= 0)
+                Fp.index_put_((torch.from_numpy(owner[keep]).to(dev), torch.from_numpy(c[keep]).to(dev)),
+                              kb_data[torch.from_numpy(ent[keep]).to(dev)], accumulate=True)
+                owner, ent = _ranges(KT.indptr, nd.own)
+                c = loc[KT.indices[ent]]
+                keep = np.flatnonzero(c >= no)
+                Fp.index_put_((torch.from_numpy(c[keep]).to(dev), torch.from_numpy(owner[keep]).to(dev)),
+                              kt_data[torch.from_numpy(ent[keep]).to(dev)], accumulate=True)
+            for ch in nd.children:
+                S = upd.pop(id(ch))
+                kp = torch.from_numpy(loc[ch.bnd]).to(dev)
+                L = kp.numel()
+                Fp.index_put_((kp[:, None].expand(L, L), kp[None, :].expand(L, L)),
+                              S.view(L, b, L, b).permute(0, 2, 1, 3), accumulate=True)
+            loc[faces] = -1
+            F = Fp.permute(0, 2, 1, 3).reshape(nf * b, nf * b)
+            del Fp
+            F11, F12, F21, F22 = F[:o, :o], F[:o, o:], F[o:, :o], F[o:, o:]
+            G = self.Gd[g_off:g_off + m * o].view(m, o)
+            H = self.Hd[h_off:h_off + o * m].view(o, m)
+            if o:
+                LU, piv = torch.linalg.lu_factor(F11)
+                perm = np.arange(o)
+                for r, p in enumerate(piv.cpu().numpy() - 1):
+                    perm[r], perm[p] = perm[p], perm[r]
+                eye = torch.eye(o, **f64)
+                Linv = torch.linalg.solve_triangular(LU, eye, upper=False, unitriangular=True)
+                Uinv = torch.linalg.solve_triangular(LU, eye, upper=True)
+                G[:o][:, torch.from_numpy(perm).to(dev)] = Linv      # L11^-1 P
+                U12 = G[:o] @ F12
+                L21 = F21 @ Uinv
+                S = F22 - L21 @ U12
+                H[:, :o] = Uinv
+                if m > o:
+                    G[o:] = -(L21 @ G[:o])
+                    H[:, o:] = -(Uinv @ U12)
+            else:
+                S = F22.clone()
+            if nd.parent is not None:
+                upd[id(nd)] = S.contiguous()
+            del F
+
+    # -- solve -----------------------------------------------------------------
+    def solve(self, b: torch.Tensor, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+        """``K^-1 b`` on the device (``b``: float64, n entries); into ``out``
+        when given, else a new tensor."""
+        if self.device.type != "cuda":
+            raise RuntimeError("the trace solve runs on the GPU; there is no CPU fallback")
+        L = _lib.lib()
+        s = (stream or torch.cuda.current_stream(self.device)).cuda_stream
+        b = b.contiguous()
+        x = out if out is not None else torch.empty(self.n, dtype=torch.float64, device=self.device)
+        for items, n_items, fo, _, _, _ in self.levels:
+            if n_items:
+                _lib.check(L.pbte_nd_forward(items.data_ptr(), n_items, self.meta.data_ptr(), self.idx.data_ptr(),
+                                             self.cptr.data_ptr(), self.csrc.data_ptr(), self.Gd.data_ptr(),
+                                             b.data_ptr(), self.z.data_ptr(), self.delta.data_ptr(), fo, s),
+                           "nd_forward")
+        for _, _, _, items, n_items, bm in reversed(self.levels):
+            if n_items:
+                _lib.check(L.pbte_nd_backward(items.data_ptr(), n_items, self.meta.data_ptr(), self.idx.data_ptr(),
+                                              self.Hd.data_ptr(), self.z.data_ptr(), x.data_ptr(), bm, s),
+                           "nd_backward")
+        return x
+
+    def _check(self, K, tol) -> float:
+        rng = np.random.default_rng(0)
+        rhs = K @ rng.standard_normal(self.n)
+        x = self.solve(torch.from_numpy(rhs).to(self.device)).cpu().numpy()
+        res = float(np.linalg.norm(K @ x - rhs) / max(np.linalg.norm(rhs), 1e-300))
+        if not res < tol:
+            raise np.linalg.LinAlgError(f"nested-dissection trace solve: relative residual {res:.2e} > {tol:.0e}")
+        return res

@@ -276,6 +276,22 @@ int pbte_correct(pbte_ctx *ctx, double *vdf, const double *uq, const double *tri
 int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int32_t *singular,
                          void *stream);
 
+/* ---- GSIS trace solve (pybte/acceleration/global_solve.py:120-195) --------
+ * One height of the forward / backward sweep of a nested-dissection
+ * multifrontal solve of K x = b (factors made once on the host,
+ * pbte_gb300/trace_nd.py).  items: [n_items][4] int32 (node, first row,
+ * end row, 0); meta: [nodes][8] int64 (index offset, own count o, front size
+ * m, G offset, H offset, delta offset, contribution-pointer offset, 0); idx:
+ * the global unknowns of each front, own first; G: per node m x o,
+ * H: o x m, row-major; cptr/csrc: per front position, the delta slots of
+ * the children's updates to add.  max_own / max_front: the largest o / m of
+ * the items (shared memory, at most 25 600 doubles). */
+int pbte_nd_forward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
+                    const int64_t *cptr, const int64_t *csrc, const double *G, const double *b, double *z,
+                    double *delta, int32_t max_own, void *stream);
+int pbte_nd_backward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
+                     const double *H, const double *z, double *x, int32_t max_front, void *stream);
+
 /* ---- field output (pybte/io_output.py:187-276) ---------------------------
  * No context: these take the mesh, basis and state as plain device arrays,
  * so they serve any solver's vdf.
