@@ -12,9 +12,9 @@
 // and its own boundary update G_bot v plus the children's updates to those
 // unknowns goes to its delta slots.  The backward sweep (root first) forms
 // x_own = H [z_own ; x_bnd].  One thread block per work item (a node and a
-// run of at most 64 output rows); a warp per row, lanes striding the
-// columns (coalesced), the input vector in shared memory.  Sums are in a
-// fixed order, so the solve is deterministic.
+// run of output rows, laid out by the host); a warp per row, lanes striding
+// the columns (coalesced, four loads in flight per lane), the input vector in
+// shared memory.  Sums are in a fixed order, so the solve is deterministic.
 #include <cuda_runtime.h>
 
 #include "pbte_internal.cuh"
@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(kThreads) nd_forward_kernel(const int4 *items,
     for (int r = it.y + warp; r < it.z; r += kThreads / 32) {
         const double *row = G + mt.goff + (int64_t)r * o;
         double acc = 0.0;
+#pragma unroll 4
         for (int c = lane; c < o; c += 32) acc += row[c] * v[c];
         acc = warp_sum(acc);
         if (lane == 0) {
@@ -82,6 +83,7 @@ __global__ void __launch_bounds__(kThreads) nd_backward_kernel(const int4 *items
     for (int r = it.y + warp; r < it.z; r += kThreads / 32) {
         const double *row = H + mt.hoff + (int64_t)r * m;
         double acc = 0.0;
+#pragma unroll 4
         for (int c = lane; c < m; c += 32) acc += row[c] * w[c];
         acc = warp_sum(acc);
         if (lane == 0) x[idx[mt.ioff + r]] = acc;

@@ -223,6 +223,9 @@ class GSIS:
         self.ba1 = self.ba_sol[self.p1].contiguous()
         self.ba2 = self.ba_sol[self.p2].contiguous()
         self.flip2 = torch.from_numpy(mirror2[sel2]).to(dev)
+        # rows of the second side that are mirrored periodic faces, as indices
+        # (no data-dependent shapes per iteration, so the step can be captured)
+        self.flip2_rows = torch.from_numpy(np.flatnonzero(mirror2[sel2])).to(dev)
         self.perm = permt
         wall_th = np.flatnonzero((fbc >= 0) & (code == BC_THERMALISING))
         wall_ad = np.flatnonzero((fbc >= 0) & (code == BC_NONTHERMALISING))
@@ -261,8 +264,8 @@ class GSIS:
         ffa = torch.bmm(self.ba1, src_t[self.p1[0]].unsqueeze(-1)).squeeze(-1)   # (n_faces, nf3)
         if self.sel2.numel():
             c2 = torch.bmm(self.ba2, src_t[self.p2[0]].unsqueeze(-1)).squeeze(-1)
-            if bool(self.flip2.any()):
-                c2[self.flip2] = c2[self.flip2][:, self.perm]
+            if self.flip2_rows.numel():
+                c2[self.flip2_rows] = c2[self.flip2_rows][:, self.perm]
             ffa.index_add_(0, self.sel2, c2)
         if self.wall_all.size:
             s = (stream or torch.cuda.current_stream()).cuda_stream

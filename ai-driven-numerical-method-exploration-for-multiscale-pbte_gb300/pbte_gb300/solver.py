@@ -398,11 +398,36 @@ class Solver:
         t0 = time.perf_counter()
         step, converged = 0, False
         s = torch.cuda.current_stream().cuda_stream
+
+        def one_step(st):
+            self.step(stream=st)
+            _lib.check(L.pbte_residual_iterate(self.ctx.handle, self.mom.temp.data_ptr(), self.t_old.data_ptr(),
+                                               self._res.data_ptr(), st.cuda_stream), "residual")
+
+        # a GSIS step (dozens of launches: sweep, hot source, trace solve,
+        # recovery, correction) is captured once and replayed; the host reads
+        # the residual after each replay for pybte's stopping rule
+        graph = None
+        if (self.acc is not None and getattr(self, "use_graphs", True)
+                and c.performance.trace_solver == "device"):
+            graph = torch.cuda.CUDAGraph()
+            with device_lock:
+                empty_graveyard()
+                sync(self.device)
+                with torch.cuda.graph(graph, stream=torch.cuda.Stream(device=self.device),
+                                      capture_error_mode="thread_local"):
+                    one_step(torch.cuda.current_stream())
+            # counted at capture, where nothing ran
+            self.acc.solve_count -= 1
+            self.ctx.sweep_count -= 1
         while True:
             step += 1
-            self.step()
-            _lib.check(L.pbte_residual_iterate(self.ctx.handle, self.mom.temp.data_ptr(), self.t_old.data_ptr(),
-                                               self._res.data_ptr(), s), "residual")
+            if graph is not None:
+                graph.replay()
+                self.acc.solve_count += 1
+                self.ctx.sweep_count += 1
+            else:
+                one_step(torch.cuda.current_stream())
             r = self._res.cpu().numpy()
             res = float(r[0])
             residuals.append(res)
@@ -419,6 +444,7 @@ class Solver:
             if step >= tmax:
                 break
         sync(self.device)
+        bury(graph)
         wall = time.perf_counter() - t0
         return self._record(step, converged, np.array(residuals), np.array(masses), wall, scheme,
                             true_res=true_res if want_true else None)

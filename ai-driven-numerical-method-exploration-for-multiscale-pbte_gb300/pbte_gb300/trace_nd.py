@@ -42,8 +42,9 @@ from . import _lib
 
 __all__ = ["NestedDissectionSolver", "dissect"]
 
-#: output rows of G or H per work item (one thread block)
-ROWS_PER_ITEM = 64
+#: output rows of G or H per work item (one thread block of 8 warps): small
+#: enough that the few large fronts near the root still spread over many SMs
+ROWS_PER_ITEM = 16
 
 
 def _ranges(ptr: np.ndarray, rows: np.ndarray):
