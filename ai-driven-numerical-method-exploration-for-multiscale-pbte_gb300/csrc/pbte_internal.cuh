@@ -133,6 +133,7 @@ struct pbte_ctx {
     int32_t *d_pface = nullptr, *d_ptri = nullptr;  // [n_pfaces]: face, partner element behind it
     int32_t *d_pslot = nullptr;     // [n_faces]: row of a periodic face in the compact buffers, else -1
     double *d_psnap = nullptr;      // [ndir][n_pfaces][nd]: partner values before a source-iteration sweep
+    double *d_gsis = nullptr;       // [4][n_tris * nd]: GSIS moment rows / correction coefficients
 };
 
 // launchers (pbte_kernels.cu)
@@ -172,6 +173,8 @@ int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, i
 int launch_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_hmin,
                    double tau_thr, int use_hmin, double *ts, double *qxs, double *qys,
                    double *temp, double *qx, double *qy, cudaStream_t s);
+int launch_element_integrals(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                             double *temp, double *qx, double *qy, cudaStream_t s);
 int launch_batched_inverse(const double *a, double *inv, int n, int m, int32_t *singular,
                            cudaStream_t s);
 // partner values of the periodic faces: mode 0 vdf -> compact [ndir][n_pfaces][nd]

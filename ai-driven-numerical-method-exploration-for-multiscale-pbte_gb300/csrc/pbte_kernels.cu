@@ -8,8 +8,8 @@
 // through the edge gather map, and solves A x = b with partial pivoting in
 // registers (or with stored FP64 factors in the "precomputed" mode).
 // Other kernels: moment sources, moments, adiabatic-wall emission, residuals,
-// transport residual, GSIS hot source / wall trace / correction, batched
-// inverse.
+// transport residual, batched inverse (the GSIS kernels on the distribution
+// are in pbte_gsis.cu).
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -528,101 +528,6 @@ __global__ void scale_by_weight_kernel(double *num, double *den, const double *w
     if (d < ndir) { num[d] *= w[d]; den[d] *= w[d]; }
 }
 
-// GSIS third-order moment source (hot_source.py:29-58), regrouped: the four
-// angular moments a_k(c) w f are taken first, then contracted with gx, gy.
-__global__ void hot_source_kernel(const double *vdf, const CellRec<double> *cells, const double *ref,
-                                  const double *cx, const double *cy, const double *w, int ndir, int nt,
-                                  int NP, double tc5, double *work) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nt) return;
-    double mk[4][16];
-    for (int k = 0; k < 4; ++k)
-        for (int l = 0; l < NP; ++l) mk[k][l] = 0.0;
-    for (int d = 0; d < ndir; ++d) {
-        const double c1 = cx[d], c2 = cy[d], dw = w[d];
-        const double a1 = c1 * (5.0 * c1 * c1 - 3.0) * dw, a2 = c2 * (5.0 * c1 * c1 - 1.0) * dw;
-        const double a3 = c1 * (5.0 * c2 * c2 - 1.0) * dw, a4 = c2 * (5.0 * c2 * c2 - 3.0) * dw;
-        const double *f = vdf + ((size_t)d * nt + i) * NP;
-        for (int l = 0; l < NP; ++l) {
-            const double fl = f[l];
-            mk[0][l] += a1 * fl; mk[1][l] += a2 * fl; mk[2][l] += a3 * fl; mk[3][l] += a4 * fl;
-        }
-    }
-    const CellRec<double> r = cells[i];
-    const double *Dx = ref + NP * NP, *Dy = ref + 2 * NP * NP;
-    double *o = work + (size_t)i * 7 * NP;
-    for (int m = 0; m < NP; ++m) {
-        double pxx = 0.0, pxy = 0.0, pyy = 0.0;
-        for (int l = 0; l < NP; ++l) {
-            const double gx = r.area2 * (r.gxa * Dx[l * NP + m] + r.gxb * Dy[l * NP + m]);
-            const double gy = r.area2 * (r.gya * Dx[l * NP + m] + r.gyb * Dy[l * NP + m]);
-            pxx += gx * mk[0][l] + gy * mk[1][l];
-            pxy += gx * mk[1][l] + gy * mk[2][l];
-            pyy += gx * mk[2][l] + gy * mk[3][l];
-        }
-        o[3 * NP + m] = (pxx + 0.5 * pyy) * tc5;
-        o[4 * NP + m] = 0.5 * pxy * tc5;
-        o[5 * NP + m] = 0.5 * pxy * tc5;
-        o[6 * NP + m] = (0.5 * pxx + pyy) * tc5;
-    }
-}
-
-// Kinetic wall-trace moments (global_solve.py:31-53), one thread per (wall face, face DOF).
-__global__ void wall_trace_kernel(const double *vdf, const double *tri_fc_fc, const double *cx,
-                                  const double *cy, const double *w, int ndir, int nt, int NP, int NF,
-                                  int nk, const int32_t *tri_list, const int32_t *lfc_list, double *out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nk * NF) return;
-    const int k = t / NF, m = t % NF;
-    const int tri = tri_list[k], lfc = lfc_list[k];
-    double c[16];
-    for (int l = 0; l < NP; ++l) c[l] = tri_fc_fc[(((size_t)l * NF + m) * nt + tri) * 3 + lfc];
-    double tb = 0.0, qxb = 0.0, qyb = 0.0;
-    for (int d = 0; d < ndir; ++d) {
-        const double *f = vdf + ((size_t)d * nt + tri) * NP;
-        double tt = 0.0;
-        for (int l = 0; l < NP; ++l) tt += f[l] * c[l];
-        tb += tt * w[d];
-        qxb += cx[d] * tt * w[d];
-        qyb += cy[d] * tt * w[d];
-    }
-    out[(size_t)k * 3 * NF + m] = tb;
-    out[(size_t)k * 3 * NF + NF + m] = qxb;
-    out[(size_t)k * 3 * NF + 2 * NF + m] = qyb;
-}
-
-// Damped correction (correction.py:29-75): one thread per (element, DOF).
-__global__ void correct_kernel(double *vdf, const double *uq, const double *cx, const double *cy,
-                               const double *w, const double *tri_hmin, int ndir, int nt, int NP,
-                               double cv, double vg, double tau_r, double tau_n, double tau_c,
-                               double tau_thr, int use_hmin, double *ts, double *qxs, double *qys) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nt * NP) return;
-    const int i = t / NP, m = t % NP;
-    const double drift = tau_c / tau_n * 3.0 / 4.0 / kPi / vg / vg;
-    const double tau_loc = use_hmin ? tau_r / tri_hmin[i] : tau_r;
-    const double beta = fmin(tau_loc, tau_thr) / tau_loc;
-    double tv = 0.0, qxv = 0.0, qyv = 0.0;
-    for (int d = 0; d < ndir; ++d) {
-        const double f = vdf[(size_t)d * nt * NP + t];
-        tv += f * w[d];
-        qxv += cx[d] * f * w[d];
-        qyv += cy[d] * f * w[d];
-    }
-    tv = tv / cv;
-    const double lt = (uq[(size_t)m * nt + i] - tv) * beta;
-    const double lqx = (uq[(size_t)(NP + m) * nt + i] - qxv) * beta;
-    const double lqy = (uq[(size_t)(2 * NP + m) * nt + i] - qyv) * beta;
-    const double eq = lt * cv / 4.0 / kPi;
-    for (int d = 0; d < ndir; ++d) {
-        double *f = vdf + (size_t)d * nt * NP + t;
-        *f = *f + eq + (cx[d] * lqx + cy[d] * lqy) * drift;
-    }
-    ts[(size_t)m * nt + i] = lt + tv;
-    qxs[(size_t)m * nt + i] = lqx + qxv;
-    qys[(size_t)m * nt + i] = lqy + qyv;
-}
-
 // Batched Gauss-Jordan inverse with partial pivoting, one warp per matrix,
 // the augmented [A | I] rows held in shared memory.
 __global__ void batched_inverse_kernel(const double *a, double *inv, int n, int m, int32_t *singular) {
@@ -999,29 +904,9 @@ int launch_transport_residual_scratch(pbte_ctx *c, const double *ts, const doubl
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
-int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s) {
-    const int th = 128;
-    hot_source_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(vdf, c->d_cells64, c->d_ref64, c->d_cx, c->d_cy,
-                                                              c->d_w, c->ndir, c->n_tris, c->nd, tc5, work);
-    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
-}
-
-int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk, const int32_t *tri_list,
-                      const int32_t *lfc_list, double *out, cudaStream_t s) {
-    if (nk <= 0) return PBTE_OK;
-    const int th = 128, total = nk * c->nf;
-    wall_trace_kernel<<<(total + th - 1) / th, th, 0, s>>>(vdf, tri_fc_fc, c->d_cx, c->d_cy, c->d_w, c->ndir,
-                                                          c->n_tris, c->nd, c->nf, nk, tri_list, lfc_list, out);
-    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
-}
-
-int launch_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_hmin, double tau_thr,
-                   int use_hmin, double *ts, double *qxs, double *qys, double *temp, double *qx, double *qy,
-                   cudaStream_t s) {
-    const int th = 256, total = c->n_tris * c->nd;
-    correct_kernel<<<(total + th - 1) / th, th, 0, s>>>(vdf, uq, c->d_cx, c->d_cy, c->d_w, tri_hmin, c->ndir,
-                                                       c->n_tris, c->nd, c->cv, c->vg, c->tau_r, c->tau_n,
-                                                       c->tau_c, tau_thr, use_hmin, ts, qxs, qys);
+int launch_element_integrals(pbte_ctx *c, const double *ts, const double *qxs, const double *qys, double *temp,
+                             double *qx, double *qy, cudaStream_t s) {
+    const int th = 256;
     element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts, qxs, qys, c->d_int_tri, c->n_tris, c->nd,
                                                                      c->cv, temp, qx, qy, nullptr);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;

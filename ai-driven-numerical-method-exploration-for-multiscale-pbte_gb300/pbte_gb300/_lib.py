@@ -17,7 +17,7 @@ CSRC = PKG_ROOT / "csrc"
 INCLUDE = REPO_ROOT / "include"
 LIB_PATH = PKG_ROOT / "_build" / "libpbte_gb300.so"
 SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_krylov.cu", "pbte_capi.cu",
-           "pbte_noalloc.cu", "pbte_output.cu", "pbte_trace.cu"]
+           "pbte_noalloc.cu", "pbte_output.cu", "pbte_trace.cu", "pbte_gsis.cu"]
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0

@@ -37,6 +37,36 @@ def test_device_trace_solve_matches_sparse_lu(cuda, periodic, b):
     assert _rel(x.cpu().numpy(), ref) < 1e-11
 
 
+@pytest.mark.parametrize("kind", ["adiabatic", "isothermal", "periodic", "deg3"])
+def test_gsis_step_matches_oracle(cuda, kind):
+    """One GSIS correction (hot source, trace right-hand side with the wall
+    traces, trace solve, local recovery, damped correction) from the same
+    seeded distribution, GPU against the oracle."""
+    from oracle.oracle import GSIS as OracleGSIS
+    from oracle.oracle import Oracle
+    if kind == "periodic":
+        case = periodic_case(2, 4, 8, 0.05, 0.005, accflag=1)
+    elif kind == "deg3":
+        case = small_case(3, 4, 8, 0.05, 0.005, accflag=1)
+    else:
+        case = small_case(2 if kind == "adiabatic" else 1, 4, 8, 0.05, 0.005, accflag=1,
+                          south="nonthermalising" if kind == "adiabatic" else "thermalising")
+    s = Solver(case)
+    o = Oracle(s.disc, nthreads=4)
+    og = OracleGSIS(o)
+    rng = np.random.default_rng(31)
+    o.vdf[:] = rng.standard_normal(o.vdf.shape)
+    s.vdf.copy_(torch.from_numpy(o.vdf))
+    og.apply()
+    s.acc.apply()
+    torch.cuda.synchronize()
+    assert _rel(s.acc.uq.cpu().numpy(), og.uq) < 1e-10
+    assert _rel(s.vdf.cpu().numpy(), o.vdf) < 1e-10
+    h = s.mom.host()
+    for k in ("ts", "qxs", "qys", "temp"):
+        assert _rel(h[k], getattr(o, k)) < 1e-10, k
+
+
 @pytest.mark.parametrize("name", ["gsis_deg2_adiabatic", "gsis_deg1_isothermal"])
 def test_gsis_device_and_host_trace_solves_agree(cuda, name):
     recs = {}
