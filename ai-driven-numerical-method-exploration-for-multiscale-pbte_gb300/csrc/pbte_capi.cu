@@ -119,6 +119,25 @@ int pbte_transport_residual(pbte_ctx *c, const double *ts, const double *qxs, co
     return pbte::launch_transport_residual(c, ts, qxs, qys, vdf, flux_wall, pbuf, num, den, S(stream));
 }
 
+int pbte_factorise_f32(pbte_ctx *c, void *stream) {
+    if (!c) return PBTE_ERR_ARG;
+    if (c->deg > 3) return PBTE_ERR_UNSUPPORTED;
+    if (!c->d_lu32) {
+        const size_t n = pbte::factor_count(c->n_udir, c->n_tris, c->nd * c->nd);
+        if (cudaMalloc((void **)&c->d_lu32, n * sizeof(float)) != cudaSuccess) {
+            c->d_lu32 = nullptr;
+            return PBTE_ERR_NOMEM;
+        }
+        c->device_bytes += n * sizeof(float);
+    }
+    int rc = pbte::launch_factorise32(c, S(stream));
+    if (rc) {
+        cudaFree(c->d_lu32);
+        c->d_lu32 = nullptr;
+    }
+    return rc;
+}
+
 int pbte_periodic_count(const pbte_ctx *c, int64_t *n_pfaces) {
     if (!c || !n_pfaces) return PBTE_ERR_ARG;
     *n_pfaces = c->n_pfaces;

@@ -142,7 +142,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_udir_rep, c->d_udir_twin, c->d_rf64, c->d_rf32, c->d_ri, c->d_mom_part,
                     c->d_cx32, c->d_cy32, c->d_w32, c->d_udir_of, c->d_uw32, c->d_ucx32, c->d_ucy32,
                     c->d_uw64, c->d_ucx64, c->d_ucy64, c->d_fresh, c->d_pface, c->d_ptri, c->d_pslot,
-                    c->d_psnap, c->d_gsis};
+                    c->d_psnap, c->d_gsis, c->d_lu32};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;

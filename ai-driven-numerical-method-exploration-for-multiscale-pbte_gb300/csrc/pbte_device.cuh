@@ -44,6 +44,7 @@ struct SweepParams {
     const int32_t *dir_class, *class_off, *class_nlev, *lvl_ptr, *lvl_cells;
     const double *lu;       // stored factors, factor_base() layout
     const int8_t *piv;
+    const float *lu32;      // stored FP32 factors (no interchanges), factor_base() layout
     const int32_t *udir_of; // ordinate -> distinct in-plane velocity (factor owner)
     int store_twin;         // ring sweep: also store the z-mirror twin's copy (0: folded consumers)
     int by_udir;            // ring sweep: row of the distinct velocity u instead of the ordinate d

@@ -96,6 +96,10 @@ struct pbte_ctx {
     float *d_S32 = nullptr;
     double *d_lu = nullptr;   // precomputed factors (optional), factor_base() layout
     int8_t *d_piv = nullptr;
+    // FP32 factors for the FP32 sweeps (optional; no row interchanges, 1/U_kk
+    // on the diagonal), factor_base() layout, made by pbte_factorise_f32 with
+    // the FP32 sweep's own in-register arithmetic
+    float *d_lu32 = nullptr;
     double *d_red = nullptr;  // reduction scratch
     int32_t *d_singular = nullptr;
     const int32_t *done = nullptr;  // optional device stop flag
@@ -151,6 +155,7 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
                          double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
                          double *qy, cudaStream_t s);
 int launch_factorise(pbte_ctx *c, cudaStream_t s);
+int launch_factorise32(pbte_ctx *c, cudaStream_t s);
 int launch_moments64(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys,
                      double *temp, double *qx, double *qy, cudaStream_t s);
 int launch_moments32(pbte_ctx *c, const float *vdf, double *ts, double *qxs, double *qys,

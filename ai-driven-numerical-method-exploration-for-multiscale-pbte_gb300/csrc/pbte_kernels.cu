@@ -595,6 +595,7 @@ static SweepParams<T> make_params(pbte_ctx *c) {
     P.fresh = c->d_fresh;
     P.pslot = nullptr;
     P.pb_rows = c->n_faces;
+    P.lu32 = c->d_lu32;
     P.singular = c->d_singular; P.done = c->done;
     P.nt = c->n_tris; P.n_faces = c->n_faces;
     P.inv_tau_c = (T)(1.0 / c->tau_c);
@@ -718,10 +719,10 @@ int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scal
     if (by_udir) {
         // rows by distinct velocity exist only in the ring sweep
         if (c->sweep_variant == 1) return PBTE_ERR_UNSUPPORTED;
-        return launch_ring<float, false>(c, P, s);
+        return c->d_lu32 ? launch_ring<float, true>(c, P, s) : launch_ring<float, false>(c, P, s);
     }
     if (c->sweep_variant != 1) {
-        const int rc = launch_ring<float, false>(c, P, s);
+        const int rc = c->d_lu32 ? launch_ring<float, true>(c, P, s) : launch_ring<float, false>(c, P, s);
         if (rc != PBTE_ERR_UNSUPPORTED || c->sweep_variant >= 2) return rc;
     }
     return sweep_dispatch<float, false>(c, P, s);

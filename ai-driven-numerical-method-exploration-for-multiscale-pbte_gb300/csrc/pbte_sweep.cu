@@ -225,7 +225,17 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
                 r.gya = __ldg(rf + kRGya * M + k);
                 r.gyb = __ldg(rf + kRGyb * M + k);
             }
-            if constexpr (PRECOMP) {
+            if constexpr (PRECOMP && sizeof(T) == 4) {
+                // stored FP32 factors (factorise32_kernel): no interchanges
+                const int p = (int)(k - (int64_t)cls * P.nt);
+                const float *lu = P.lu32 + factor_base(u, p, P.nt, NP * NP);
+#pragma unroll
+                for (int m = 0; m < NP; ++m) {
+                    piv[c][m] = m;
+#pragma unroll
+                    for (int l = 0; l < NP; ++l) A[c][m][l] = __ldg(lu + 32 * (m * NP + l));
+                }
+            } else if constexpr (PRECOMP) {
                 const int p = (int)(k - (int64_t)cls * P.nt);
                 const double *lu = P.lu + factor_base(u, p, P.nt, NP * NP);
                 const int8_t *pv = P.piv + factor_base(u, p, P.nt, NP);
@@ -451,5 +461,83 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
 template int launch_ring<double, false>(pbte_ctx *, const SweepParams<double> &, cudaStream_t);
 template int launch_ring<double, true>(pbte_ctx *, const SweepParams<double> &, cudaStream_t);
 template int launch_ring<float, false>(pbte_ctx *, const SweepParams<float> &, cudaStream_t);
+template int launch_ring<float, true>(pbte_ctx *, const SweepParams<float> &, cudaStream_t);
+
+// FP32 factors for the ring sweep, one thread per (distinct in-plane
+// velocity u, sweep position p): the FP32 records and the same arithmetic
+// as the sweep's in-register factorisation (assemble<float>, no
+// interchanges, __frcp_rn of the pivot), so a sweep with stored factors gives
+// the bits of one without.
+template <int DEG>
+__global__ void factorise32_kernel(SweepParams<float> P, const float *__restrict__ rf, int64_t M,
+                                   const int32_t *__restrict__ udir_rep, int n_udir, float *__restrict__ lu_out) {
+    constexpr int NP = Shape<DEG>::NP;
+    __shared__ float sref[6 * NP * NP];
+    for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
+    __syncthreads();
+    const size_t total = (size_t)n_udir * P.nt;
+    int sing = 0;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int u = (int)(t / P.nt), p = (int)(t % P.nt);
+        const int d = udir_rep[u];
+        const int64_t k = (int64_t)P.dir_class[d] * P.nt + p;
+        const float cx = (float)P.cx[d], cy = (float)P.cy[d];
+        Geo<float> r;
+        float s[3];
+#pragma unroll
+        for (int il = 0; il < 3; ++il) {
+            r.es[il] = rf[(kREs + il) * M + k];
+            s[il] = cx * rf[(kRNx + il) * M + k] + cy * rf[(kRNy + il) * M + k];
+        }
+        r.area2 = rf[kRA2 * M + k];
+        r.gxa = rf[kRGxa * M + k];
+        r.gxb = rf[kRGxb * M + k];
+        r.gya = rf[kRGya * M + k];
+        r.gyb = rf[kRGyb * M + k];
+        float A[NP][NP];
+        assemble<float, DEG>(sref, r, cx, cy, P.inv_tau_c, s, A);
+#pragma unroll
+        for (int kk = 0; kk < NP; ++kk) {
+            sing += (A[kk][kk] == 0.0f);
+            const float rr = __frcp_rn(A[kk][kk]);
+#pragma unroll
+            for (int ii = kk + 1; ii < NP; ++ii) {
+                A[ii][kk] *= rr;
+#pragma unroll
+                for (int j = kk + 1; j < NP; ++j) A[ii][j] -= A[ii][kk] * A[kk][j];
+            }
+            A[kk][kk] = rr;
+        }
+        float *o = lu_out + factor_base(u, p, P.nt, NP * NP);
+#pragma unroll
+        for (int m = 0; m < NP; ++m)
+#pragma unroll
+            for (int l = 0; l < NP; ++l) o[32 * (m * NP + l)] = A[m][l];
+    }
+    if (sing) atomicAdd(P.singular, sing);
+}
+
+int launch_factorise32(pbte_ctx *c, cudaStream_t s) {
+    if (c->deg > 3 || !c->d_lu32) return PBTE_ERR_UNSUPPORTED;
+    SweepParams<float> P{};
+    P.ref = c->d_ref32;
+    P.cx = c->d_cx;
+    P.cy = c->d_cy;
+    P.dir_class = c->d_dir_class;
+    P.nt = c->n_tris;
+    P.inv_tau_c = (float)(1.0 / c->tau_c);
+    P.singular = c->d_singular;
+    const int th = 128;
+    const size_t total = (size_t)c->n_udir * c->n_tris;
+    const int bl = (int)std::min<size_t>((total + th - 1) / th, 152 * 16);
+    const int64_t M = (int64_t)c->nclass * c->n_tris;
+    switch (c->deg) {
+        case 1: factorise32_kernel<1><<<bl, th, 0, s>>>(P, c->d_rf32, M, c->d_udir_rep, c->n_udir, c->d_lu32); break;
+        case 2: factorise32_kernel<2><<<bl, th, 0, s>>>(P, c->d_rf32, M, c->d_udir_rep, c->n_udir, c->d_lu32); break;
+        case 3: factorise32_kernel<3><<<bl, th, 0, s>>>(P, c->d_rf32, M, c->d_udir_rep, c->n_udir, c->d_lu32); break;
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
 
 }  // namespace pbte

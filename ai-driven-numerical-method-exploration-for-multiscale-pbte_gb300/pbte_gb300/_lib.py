@@ -135,6 +135,7 @@ _SIGS = {
     "pbte_nd_forward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp],
                         ctypes.c_int),
     "pbte_nd_backward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp], ctypes.c_int),
+    "pbte_factorise_f32": ([_vp, _vp], ctypes.c_int),
     "pbte_periodic_count": ([_vp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_periodic_gather": ([_vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_periodic_scatter": ([_vp, _vp, _vp, _vp], ctypes.c_int),

@@ -152,6 +152,13 @@ class SweepContext:
         self._num = torch.zeros(self.ndir, **f64)
         self._den = torch.zeros(self.ndir, **f64)
         self.lu = None   # the factors live inside the library in precomputed mode
+        # stored FP32 factors for the FP32 sweeps, on request (same bits as
+        # factoring in registers; measured no faster at P2, where the ring
+        # sweep is bound by its level chain)
+        self.fp32_factors = False
+        if (c.performance.fp32_factors and self.ndof <= 10 and not bd.has_periodic
+                and self.cxv.size * self.n_tris * self.ndof * self.ndof * 2.0 <= c.performance.max_operator_bytes):
+            self.factorise_f32()
 
     def __del__(self):
         h = getattr(self, "_ctx", None)
@@ -184,6 +191,17 @@ class SweepContext:
         and threads per group (0: 64, or 64 or 128)."""
         _lib.check(_lib.lib().pbte_set_ring_groups(self._ctx, int(groups)), "pbte_set_ring_groups")
         _lib.check(_lib.lib().pbte_set_ring_width(self._ctx, int(width)), "pbte_set_ring_width")
+
+    def factorise_f32(self, stream=None) -> None:
+        """Store FP32 element factors (one set per distinct in-plane velocity)
+        for the FP32 sweeps: same bits, no per-sweep assembly and
+        factorisation (``pbte_factorise_f32``)."""
+        _lib.check(_lib.lib().pbte_factorise_f32(self._ctx, _stream(stream)), "pbte_factorise_f32")
+        nlev, ncls, nbytes = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.check(_lib.lib().pbte_ctx_info(self._ctx, ctypes.byref(nlev), ctypes.byref(ncls),
+                                            ctypes.byref(nbytes)), "pbte_ctx_info")
+        self.device_bytes = nbytes.value
+        self.fp32_factors = True
 
     def schedule(self) -> dict:
         w, r, u = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

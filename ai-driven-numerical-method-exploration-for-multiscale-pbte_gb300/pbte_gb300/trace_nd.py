@@ -101,6 +101,23 @@ def dissect(adj_ptr: np.ndarray, adj: np.ndarray, xy: np.ndarray, leaf: int = 32
     return order
 
 
+_LINALG = {}
+
+
+def _linalg_device(dev: torch.device) -> torch.device:
+    """``dev`` if torch's dense factorisation runs there (its CUDA linear
+    algebra is a separately loaded library), else the host."""
+    if dev.type != "cuda":
+        return dev
+    if dev not in _LINALG:
+        try:
+            torch.linalg.lu_factor(torch.eye(2, dtype=torch.float64, device=dev))
+            _LINALG[dev] = dev
+        except RuntimeError:
+            _LINALG[dev] = torch.device("cpu")
+    return _LINALG[dev]
+
+
 class NestedDissectionSolver:
     """``solve(b) -> x`` for the trace matrix ``K`` (scipy sparse, face-major
     blocks of size ``block``: unknown ``f * block + c``), on ``device``."""
@@ -207,9 +224,11 @@ class NestedDissectionSolver:
 
     # -- factorisation -----------------------------------------------------------
     def _factor(self, nodes, Kb, KT, b):
-        """Fronts assembled and factorised on ``self.device``; G and H written
-        into their slices of ``Gd`` / ``Hd``."""
-        dev = self.device
+        """Fronts assembled and factorised on ``self.device`` (or on the host
+        where the device's dense linear-algebra library cannot be loaded); G
+        and H written into their slices of ``Gd`` / ``Hd``."""
+        dst = self.device
+        dev = _linalg_device(dst)
         f64 = dict(dtype=torch.float64, device=dev)
         n_faces = Kb.shape[0] // b
         loc = np.full(n_faces, -1, dtype=np.int64)
@@ -244,8 +263,10 @@ class NestedDissectionSolver:
             F = Fp.permute(0, 2, 1, 3).reshape(nf * b, nf * b)
             del Fp
             F11, F12, F21, F22 = F[:o, :o], F[:o, o:], F[o:, :o], F[o:, o:]
-            G = self.Gd[g_off:g_off + m * o].view(m, o)
-            H = self.Hd[h_off:h_off + o * m].view(o, m)
+            Gdst = self.Gd[g_off:g_off + m * o].view(m, o)
+            Hdst = self.Hd[h_off:h_off + o * m].view(o, m)
+            G = Gdst if dev == dst else torch.empty((m, o), **f64)
+            H = Hdst if dev == dst else torch.empty((o, m), **f64)
             if o:
                 LU, piv = torch.linalg.lu_factor(F11)
                 perm = np.arange(o)
@@ -264,6 +285,9 @@ class NestedDissectionSolver:
                     H[:, o:] = -(Uinv @ U12)
             else:
                 S = F22.clone()
+            if dev != dst:
+                Gdst.copy_(G)
+                Hdst.copy_(H)
             if nd.parent is not None:
                 upd[id(nd)] = S.contiguous()
             del F

@@ -16,7 +16,10 @@ JSON line keys beyond the driver contract: ``roofline`` (the FP32 sweep,
 timed live with CUDA events on its stream), ``cpu_baseline`` (the C oracle on
 the host cores, one solve), ``e2e`` (the public API from host arrays:
 context creation + solve + results to host), ``fp64`` (the plain FP64 GPU
-drop-in on the same steps), ``latency_ms`` (p50/p99 of the timed steps).
+drop-in on the same steps), ``latency_ms`` (p50/p99 of the timed steps),
+``batched`` (two copies of each case solved concurrently), ``gsis`` (the FP64
+GSIS drop-in at Kn_R = 0.01 with the device trace solve, beside the
+per-iteration time with the host trace solve).
 
 ``--impl reference`` times the reference algorithm's CPU implementation (the
 C oracle, OpenMP over ordinates on all host cores) on the same workload.
@@ -311,6 +314,36 @@ def main():
         d2h = sum(v.nbytes for v in out)
     e2e = len(e2e_t) / sum(e2e_t)
 
+    # GSIS at Kn_R = 0.01, where GMRES(30) needs ~6000 sweeps: the FP64 GSIS
+    # drop-in with the device trace solve (one solve after an untimed one),
+    # and the per-iteration time of the same step with the host SuperLU trace
+    # solve pybte uses (20 iterations)
+    gsis = None
+    if rank == 0:
+        from pbte_gb300.config import square_case
+
+        def gsis_case(where, tmax=200_000):
+            c = square_case(GRID, DEG, NPOLE, NAZIM, tau_r=0.01, tau_n=0.001, accflag=1, tol=1e-8, tmax=tmax)
+            c.performance.trace_solver = where
+            return c
+
+        g = Solver(gsis_case("device"), device=str(dev))
+        g.run()
+        g.reset()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        grec = g.run()
+        torch.cuda.synchronize(dev)
+        tg = time.perf_counter() - t0
+        h = Solver(gsis_case("host", tmax=20), device=str(dev))
+        hrec = h.run()
+        gsis = {"kn_r": 0.01, "value": round(1.0 / tg, 4), "unit": "solves/s", "converged": bool(grec.converged),
+                "iterations": int(grec.iterations), "ms_per_iteration": round(1e3 * tg / grec.iterations, 3),
+                "host_trace_ms_per_iteration": round(1e3 * hrec.wall_clock / hrec.iterations, 3),
+                "trace_solve": "device nested dissection", "setup_s": round(g.setup_seconds, 2),
+                "trace_factor_entries": int(g.acc.solver.factor_entries)}
+        del g, h
+
     peak, kind = read_peaks()
     roof = sweep_roofline(solvers[1.0], peak, kind)
     cpu = None
@@ -333,7 +366,7 @@ def main():
                 "fp64": {"value": round(fp64_rate, 4), "unit": "solves/s",
                          "speedup_mixed_over_fp64": round(value / world / fp64_rate, 3),
                          "speedup_batched_mixed_over_fp64": round(batched["value"] / fp64_rate, 3)},
-                "batched": batched,
+                "batched": batched, "gsis": gsis,
                 "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
                 "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches)}

@@ -119,6 +119,13 @@ int pbte_sweep(pbte_ctx *ctx, const double *ts, const double *qxs, const double 
                double *vdf, const double *flux_wall, const double *pbuf, int use_pbuf,
                void *stream);
 
+/* Store FP32 element factors for the FP32 sweeps (P1-P3): one set per
+ * distinct in-plane velocity, made with the FP32 sweep's own arithmetic, so
+ * FP32 sweeps give the same bits with or without them; afterwards the FP32
+ * sweeps load instead of assembling and factoring.  4 * ndof^2 bytes per
+ * (element, distinct velocity).  No reference counterpart (FP32 path). */
+int pbte_factorise_f32(pbte_ctx *ctx, void *stream);
+
 /* Periodic faces of the context (faces with a periodic boundary, in
  * increasing face index) and their partner elements' DOFs, the periodic
  * block of the Krylov state (pybte/krylov.py:74-110):

@@ -131,6 +131,32 @@ def test_fp32_sweep_close_to_fp64(cuda):
 
 
 @pytest.mark.parametrize("deg", [1, 2, 3])
+@pytest.mark.parametrize("mesh", ["cavity:5:smootherstep", "cavity:40"])
+def test_stored_fp32_factors_match_register_factorisation(cuda, deg, mesh):
+    """FP32 sweeps with the factors stored by pbte_factorise_f32 against the
+    same sweeps factoring in registers: the factoriser uses the sweep's own
+    FP32 arithmetic, so the two agree to FP32 rounding (bit for bit where the
+    compiler contracts both alike)."""
+    s = Solver(small_case(deg, 4, 8, 0.5, 0.05, mesh=mesh))
+    assert not s.ctx.fp32_factors
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 13)
+    s.ctx.wall_flux(s.vdf)
+    out = []
+    for stored in (False, True):
+        if stored:
+            s.ctx.factorise_f32()
+        v32 = torch.zeros(s.vdf.shape, dtype=torch.float32, device=s.device)
+        s.ctx.sweep_f32((s.mom.ts, s.mom.qxs, s.mom.qys), v32, s.ctx.flux_wall)
+        torch.cuda.synchronize()
+        out.append(v32.double().cpu().numpy())
+    assert _rel(out[1], out[0]) < 1e-6
+    o.wall_flux()
+    o.sweep()
+    assert _rel(out[1], o.vdf) < 2e-5
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
 def test_fused_fp32_product_matches_separate_calls(cuda, deg):
     """pbte_fixed_point_f32 (sources, sweep, moments and emission in one call,
     z-mirror twins folded) against pbte_sweep_f32 + pbte_moments_f32 +
