@@ -142,7 +142,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_udir_rep, c->d_udir_twin, c->d_rf64, c->d_rf32, c->d_ri, c->d_mom_part,
                     c->d_cx32, c->d_cy32, c->d_w32, c->d_udir_of, c->d_uw32, c->d_ucx32, c->d_ucy32,
                     c->d_uw64, c->d_ucx64, c->d_ucy64, c->d_fresh, c->d_pface, c->d_ptri, c->d_pslot,
-                    c->d_psnap, c->d_gsis, c->d_lu32};
+                    c->d_psnap, c->d_gsis, c->d_lu32, c->d_tickets};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     delete c;
@@ -490,6 +490,11 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     TRY(alloc((size_t)4096, &c->d_red, &c->device_bytes));
     TRY(alloc((size_t)((ndir + 31) / 32) * 3 * nd * nt, &c->d_mom_part, &c->device_bytes));
     TRY(alloc((size_t)4 * nd * nt, &c->d_gsis, &c->device_bytes));
+    TRY(alloc((size_t)(nt + 31) / 32, &c->d_tickets, &c->device_bytes));
+    if (cudaMemset(c->d_tickets, 0, sizeof(uint32_t) * ((nt + 31) / 32)) != cudaSuccess) {
+        pbte_ctx_destroy(c);
+        return PBTE_ERR_CUDA;
+    }
     TRY(alloc((size_t)1, &c->d_singular, &c->device_bytes));
     if (cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
 

@@ -138,6 +138,7 @@ struct pbte_ctx {
     int32_t *d_pslot = nullptr;     // [n_faces]: row of a periodic face in the compact buffers, else -1
     double *d_psnap = nullptr;      // [ndir][n_pfaces][nd]: partner values before a source-iteration sweep
     double *d_gsis = nullptr;       // [4][n_tris * nd]: GSIS moment rows / correction coefficients
+    uint32_t *d_tickets = nullptr;  // [ceil(n_tris / 32)]: last-block tickets of the folded epilogue (kept 0)
 };
 
 // launchers (pbte_kernels.cu)

@@ -362,84 +362,135 @@ __global__ void wall_flux_np_kernel(const T *vdf, const WallFace *walls, const C
 // (ordinate rep[u]) is read with the pair's summed weight uw[u].
 // ---------------------------------------------------------------------------
 
-// vdf rows by distinct velocity: vdf[u][element dof]
-__global__ void moments_partial_fold_kernel(const float *vdf, const float *ucx, const float *ucy, const float *uw,
-                                            int nu, int total, double *part, const int32_t *done) {
+// The folded FP32 product's epilogue in one launch: blocks (tile, chunk) of
+// 32 elements x NP DOFs take the moment sums of a chunk of kMomChunk distinct
+// velocities; the last chunk block of a tile to finish (a per-tile ticket)
+// adds the chunks in order and forms the tile's moments and element
+// integrals, with moments_combine_kernel's and element_integrals_kernel's
+// arithmetic.  Blocks past the tiles (chunk 0 only) take the adiabatic-wall
+// emission: a warp per wall face, distinct velocities over lanes, FP32
+// products, FP64 sums reduced by shuffles in a fixed order.
+template <int NP>
+__global__ void __launch_bounds__(32 * NP) fold_epilogue_kernel(
+    const float *vdf, const float *ucx32, const float *ucy32, const float *uw32, int nu, int nt, double cv,
+    double *part, uint32_t *tickets, double *ts, double *qxs, double *qys, const double *int_tri, double *temp,
+    double *qx, double *qy, const WallFace *walls, int nwall, const CellRec<double> *cells, const float *ref_edge,
+    const double *ucx, const double *ucy, const double *uw, double *fw_out, const int32_t *done) {
     if (stopped(done)) return;
+    const int ntiles = (nt + 31) / 32;
+    const int total = nt * NP;
+    if ((int)blockIdx.x >= ntiles) {
+        if (blockIdx.y != 0 || !fw_out) return;
+        const int lane = threadIdx.x % 32;
+        const int f = ((int)blockIdx.x - ntiles) * NP + threadIdx.x / 32;
+        if (f >= nwall) return;
+        const WallFace wf = walls[f];
+        const float es = (float)cells[wf.tri].es[wf.lfc];
+        const float *R = ref_edge + (size_t)wf.lfc * NP * NP;
+        double acc[NP];
+#pragma unroll
+        for (int m = 0; m < NP; ++m) acc[m] = 0.0;
+        double s2 = 0.0;
+        for (int u = lane; u < nu; u += 32) {
+            const double un = ucx[u] * wf.nx + ucy[u] * wf.ny;
+            if (un < 0.0) {
+                const float *fr = vdf + ((size_t)u * nt + wf.tri) * NP;
+                float fl[NP];
+#pragma unroll
+                for (int l = 0; l < NP; ++l) fl[l] = fr[l];
+                const double uwv = un * uw[u];
+#pragma unroll
+                for (int m = 0; m < NP; ++m) {
+                    float a = 0.f;
+#pragma unroll
+                    for (int l = 0; l < NP; ++l) a += fl[l] * (es * R[m * NP + l]);
+                    acc[m] += uwv * (double)a;
+                }
+            } else {
+                s2 -= un * uw[u];
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+            for (int m = 0; m < NP; ++m) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], o);
+            s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+        }
+        if (lane == 0) {
+            double *out = fw_out + (size_t)wf.face * NP;
+#pragma unroll
+            for (int m = 0; m < NP; ++m) out[m] = -acc[m] / s2;
+        }
+        return;
+    }
     __shared__ float sw[kMomChunk], sx[kMomChunk], sy[kMomChunk];
-    const int ch = blockIdx.y;
+    __shared__ double mt[3][32 * NP];
+    __shared__ bool last;
+    const int ch = blockIdx.y, nch = gridDim.y;
     const int u0 = ch * kMomChunk, u1 = min(nu, u0 + kMomChunk);
     if ((int)threadIdx.x < u1 - u0) {
-        sw[threadIdx.x] = uw[u0 + threadIdx.x];
-        sx[threadIdx.x] = ucx[u0 + threadIdx.x];
-        sy[threadIdx.x] = ucy[u0 + threadIdx.x];
+        sw[threadIdx.x] = uw32[u0 + threadIdx.x];
+        sx[threadIdx.x] = ucx32[u0 + threadIdx.x];
+        sy[threadIdx.x] = ucy32[u0 + threadIdx.x];
     }
     __syncthreads();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= total) return;
-    const float *f = vdf + (size_t)u0 * total + t;
-    float a = 0.f, bx = 0.f, by = 0.f;
+    const int t = blockIdx.x * 32 * NP + threadIdx.x;
+    const bool live = t < total;
+    if (live) {
+        const float *f = vdf + (size_t)u0 * total + t;
+        float a = 0.f, bx = 0.f, by = 0.f;
 #pragma unroll 8
-    for (int k = 0; k < u1 - u0; ++k) {
-        const float fw = f[(size_t)k * total] * sw[k];
-        a += fw;
-        bx += sx[k] * fw;
-        by += sy[k] * fw;
+        for (int k = 0; k < u1 - u0; ++k) {
+            const float fw = f[(size_t)k * total] * sw[k];
+            a += fw;
+            bx += sx[k] * fw;
+            by += sy[k] * fw;
+        }
+        double *p = part + (size_t)ch * 3 * total;
+        p[t] = a;
+        p[total + t] = bx;
+        p[2 * total + t] = by;
     }
-    double *p = part + (size_t)ch * 3 * total;
-    p[t] = a;
-    p[total + t] = bx;
-    p[2 * total + t] = by;
-}
-
-// Adiabatic-wall emission, folded (vdf rows by distinct velocity): one warp
-// per wall face, distinct velocities over lanes, FP32 products, FP64 sums
-// reduced by shuffles in a fixed order.
-template <int NP>
-__global__ void wall_flux_fold_kernel(const float *vdf, const WallFace *walls, int nwall, const CellRec<double> *cells,
-                                      const float *ref_edge, const double *ucx, const double *ucy, const double *uw,
-                                      int nu, int nt, double *fw_out, const int32_t *done) {
-    if (stopped(done)) return;
-    const int lane = threadIdx.x % 32;
-    const int f = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32;
-    if (f >= nwall) return;
-    const WallFace wf = walls[f];
-    const float es = (float)cells[wf.tri].es[wf.lfc];
-    const float *R = ref_edge + (size_t)wf.lfc * NP * NP;
-    double acc[NP];
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&tickets[blockIdx.x], 1u) == (unsigned)(nch - 1);
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (live) {
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+        for (int c = 0; c < nch; ++c) {
+            const volatile double *p = part + (size_t)c * 3 * total;
+            s0 += p[t];
+            s1 += p[total + t];
+            s2 += p[2 * total + t];
+        }
+        const int i = t / NP, l = t % NP;
+        ts[(size_t)l * nt + i] = s0 / cv;
+        qxs[(size_t)l * nt + i] = s1;
+        qys[(size_t)l * nt + i] = s2;
+        mt[0][threadIdx.x] = s0 / cv;
+        mt[1][threadIdx.x] = s1;
+        mt[2][threadIdx.x] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x < 32 && temp) {
+        const int i = blockIdx.x * 32 + threadIdx.x;
+        if (i < nt) {
+            double a = 0.0, bx = 0.0, by = 0.0;
 #pragma unroll
-    for (int m = 0; m < NP; ++m) acc[m] = 0.0;
-    double s2 = 0.0;
-    for (int u = lane; u < nu; u += 32) {
-        const double un = ucx[u] * wf.nx + ucy[u] * wf.ny;
-        if (un < 0.0) {
-            const float *fr = vdf + ((size_t)u * nt + wf.tri) * NP;
-            float fl[NP];
-#pragma unroll
-            for (int l = 0; l < NP; ++l) fl[l] = fr[l];
-            const double uwv = un * uw[u];
-#pragma unroll
-            for (int m = 0; m < NP; ++m) {
-                float a = 0.f;
-#pragma unroll
-                for (int l = 0; l < NP; ++l) a += fl[l] * (es * R[m * NP + l]);
-                acc[m] += uwv * (double)a;
+            for (int l = 0; l < NP; ++l) {
+                const double it = int_tri[(size_t)l * nt + i];
+                a += mt[0][threadIdx.x * NP + l] * cv * it / cv;
+                bx += mt[1][threadIdx.x * NP + l] * it;
+                by += mt[2][threadIdx.x * NP + l] * it;
             }
-        } else {
-            s2 -= un * uw[u];
+            temp[i] = a;
+            qx[i] = bx;
+            qy[i] = by;
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-        for (int m = 0; m < NP; ++m) acc[m] += __shfl_xor_sync(0xffffffffu, acc[m], o);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, o);
-    }
-    if (lane == 0) {
-        double *out = fw_out + (size_t)wf.face * NP;
-#pragma unroll
-        for (int m = 0; m < NP; ++m) out[m] = -acc[m] / s2;
-    }
+    if (threadIdx.x == 0) tickets[blockIdx.x] = 0u;
 }
 
 // Step residual and mass; out[0] = residual, out[1] = sum(temp); t_old <- temp.
@@ -820,29 +871,22 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
         if (rc == PBTE_OK && fw_out) rc = wall_flux_impl<float>(c, vdf32, fw_out, s);
         return rc;
     }
-    const int total = c->n_tris * c->nd, th = 256;
+    // moments, element integrals and wall emission in one launch
     const int nch = (c->n_udir + kMomChunk - 1) / kMomChunk;
-    moments_partial_fold_kernel<<<dim3((total + th - 1) / th, nch), th, 0, s>>>(
-        vdf32, c->d_ucx32, c->d_ucy32, c->d_uw32, c->n_udir, total, c->d_mom_part, c->done);
-    moments_combine_kernel<<<(total + th - 1) / th, th, 0, s>>>(c->d_mom_part, nch, c->n_tris, c->nd, c->cv, ts_out,
-                                                               qxs_out, qys_out, c->done);
-    if (temp)
-        element_integrals_kernel<<<(c->n_tris + th - 1) / th, th, 0, s>>>(ts_out, qxs_out, qys_out, c->d_int_tri,
-                                                                         c->n_tris, c->nd, c->cv, temp, qx, qy,
-                                                                         c->done);
-    if (c->n_wall_ad && fw_out) {
-        const int wpb = 4;   // wall faces (warps) per block
-        const int bl = (c->n_wall_ad + wpb - 1) / wpb;
-        const float *ref_edge = c->d_ref32 + 3 * c->nd * c->nd;
-        auto go = [&](auto kern) {
-            kern<<<bl, 32 * wpb, 0, s>>>(vdf32, c->d_wall_ad, c->n_wall_ad, c->d_cells64, ref_edge, c->d_ucx64,
-                                         c->d_ucy64, c->d_uw64, c->n_udir, c->n_tris, fw_out, c->done);
-        };
-        switch (c->nd) {
-            case 3: go(wall_flux_fold_kernel<3>); break;
-            case 6: go(wall_flux_fold_kernel<6>); break;
-            default: go(wall_flux_fold_kernel<10>); break;
-        }
+    const int ntiles = (c->n_tris + 31) / 32;
+    const int nwall = fw_out ? c->n_wall_ad : 0;
+    const float *ref_edge = c->d_ref32 + 3 * c->nd * c->nd;
+    auto go = [&](auto kern, int np) {
+        const int wall_blocks = (nwall + np - 1) / np;
+        kern<<<dim3(ntiles + wall_blocks, nch), 32 * np, 0, s>>>(
+            vdf32, c->d_ucx32, c->d_ucy32, c->d_uw32, c->n_udir, c->n_tris, c->cv, c->d_mom_part, c->d_tickets,
+            ts_out, qxs_out, qys_out, c->d_int_tri, temp, qx, qy, c->d_wall_ad, nwall, c->d_cells64, ref_edge,
+            c->d_ucx64, c->d_ucy64, c->d_uw64, fw_out, c->done);
+    };
+    switch (c->nd) {
+        case 3: go(fold_epilogue_kernel<3>, 3); break;
+        case 6: go(fold_epilogue_kernel<6>, 6); break;
+        default: go(fold_epilogue_kernel<10>, 10); break;
     }
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
