@@ -257,10 +257,11 @@ def main():
         for k in range(args.steps):
             ms, rec = timed(solvers, k)
             times.append(ms)
-            # per FP32 Arnoldi column: sources, sweep, moments (2), wall flux,
-            # CGS2 (3), rotation, next basis vector; per FP64 product:
-            # sources, sweep, moments (2), element integrals, wall flux
-            launches += 10 * rec.diagnostics["fp32_sweeps"] + 6 * rec.diagnostics["fp64_sweeps"]
+            # per FP32 Arnoldi column: sources, sweep, epilogue (moments,
+            # integrals, wall emission), CGS2 (3), rotation, next basis
+            # vector; per FP64 product: sources, sweep, moments (2), element
+            # integrals, wall flux
+            launches += 8 * rec.diagnostics["fp32_sweeps"] + 6 * rec.diagnostics["fp64_sweeps"]
     clocks = clk.summary()
     total = max_over_ranks(float(sum(times)), dist)
     value = replica_throughput(args.steps, total * 1e-3, world)

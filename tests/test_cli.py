@@ -1,6 +1,7 @@
 """The command line (pybte's ``python -m pybte run/info`` with JSON case
 files, plus ``square`` for the benchmark square)."""
 import json
+import os
 import subprocess
 import sys
 from pathlib import Path
@@ -19,8 +20,9 @@ CASE = {"iteration": {"tol": 1e-8, "tmax": 2000}, "velmesh": {"npole": 4, "nazim
 
 
 def _cli(*args, cwd):
+    env = {**os.environ, "PYTHONPATH": os.pathsep.join([str(PKG), os.environ.get("PYTHONPATH", "")])}
     return subprocess.run([sys.executable, "-m", "pbte_gb300", *args], cwd=cwd, capture_output=True, text=True,
-                          env={"PYTHONPATH": str(PKG), "PATH": "/usr/bin:/bin"}, timeout=600)
+                          env=env, timeout=600)
 
 
 def test_info(tmp_path):
