@@ -128,6 +128,9 @@ class GSIS:
         nd, nf = disc.ndof, c.ndof_fc
         self.nd, self.nf = nd, nf
         self.variant = c.scheme.acc_variant
+        if c.scheme.defect_omega != 0.0 or c.scheme.defect_anderson:
+            raise NotImplementedError("scheme.defect_omega / defect_anderson (pybte's experimental defect "
+                                      "repair, off by default there) are not implemented")
         st = np.asarray(c.scheme.stabilisation, dtype=float).copy()
         if c.scheme.scale_by_hmin:
             st[1] /= m.hmin

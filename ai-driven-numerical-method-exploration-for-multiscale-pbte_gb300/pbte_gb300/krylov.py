@@ -366,6 +366,42 @@ class ArnoldiGraphs:
         return self.h_host[:j + 2].numpy().copy()
 
 
+class MomentPreconditioner:
+    """Approximate ``(I - T)^-1`` by the GSIS macroscopic system
+    (``pybte/krylov.py:369-414``, ``scheme.krylov_precond``): the moment
+    blocks of a residual become the source of the HDG local problems, whose
+    trace system is solved (with the wall traces of a zero distribution) and
+    whose recovered ``T, q_x, q_y`` replace them; the rest of the vector
+    passes through.  pybte notes it helps in the diffusive limit and hurts in
+    the ballistic one, and leaves it off by default."""
+
+    def __init__(self, solver, acc, sign: float = -1.0, blocks=(0, 1, 2)):
+        self.s = solver
+        self.acc = acc
+        self.nd, self.nt = solver.ndof, solver.n_tris
+        self.k = self.nd * self.nt
+        self.sign = sign
+        self.blocks = blocks
+        self.calls = 0
+        self.zero_vdf = torch.zeros_like(solver.vdf)
+        self.work = torch.zeros((self.nt, 7 * self.nd), dtype=torch.float64, device=solver.device)
+
+    def __call__(self, r: torch.Tensor) -> torch.Tensor:
+        a, nd, nt, k = self.acc, self.nd, self.nt, self.k
+        self.work.zero_()
+        for slot, blk in enumerate(self.blocks):
+            if blk is not None:
+                self.work[:, blk * nd:(blk + 1) * nd] = self.sign * r[slot * k:(slot + 1) * k].view(nd, nt).T
+        aa_src = torch.bmm(a.inv_aa_sol, self.work.unsqueeze(-1)).squeeze(-1).T.contiguous()   # (7nd, n)
+        ffa = a.rhs(aa_src, self.zero_vdf)
+        u_trace = a.solver.solve(ffa.reshape(-1)).reshape(-1, 3 * a.nf)
+        uq = aa_src.T + torch.einsum("ilpr,ilr->ip", a.aa_trace, u_trace[a.tri_faces])              # (n, 7nd)
+        out = r.clone()
+        out[:3 * k] = uq.T[:3 * nd].reshape(-1)
+        self.calls += 1
+        return out
+
+
 def _back_substitute(r, y):
     out = np.array(y, dtype=float)
     for i in range(out.size - 1, -1, -1):
@@ -375,28 +411,31 @@ def _back_substitute(r, y):
 
 
 def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, max_basis=None,
-          callback=None, arnoldi: ArnoldiGraphs | None = None):
+          callback=None, arnoldi: ArnoldiGraphs | None = None, precond=None):
     """GMRES for ``A x = b`` with device vectors (``pybte/krylov.py:150-246``).
     With ``arnoldi`` (graphs of ``A`` for the same operator) each product and
-    its orthogonalisation is one graph replay.  Returns ``(x, converged,
-    n_matvec)``."""
+    its orthogonalisation is one graph replay.  ``precond``: a left
+    preconditioner ``M`` (the residuals and products are ``M (b - A x)`` and
+    ``M A q``, as pybte's); it takes the host-driven loop.  Returns
+    ``(x, converged, n_matvec)``."""
     n = b.numel()
     x = torch.zeros_like(b) if x0 is None else x0.clone()
     maxiter = int(n if maxiter is None else maxiter)
     m_cap = maxiter if max_basis is None else max(1, min(int(max_basis), maxiter))
-    if arnoldi is not None and m_cap <= arnoldi.m_cap:
+    if arnoldi is not None and m_cap <= arnoldi.m_cap and precond is None:
         return _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, arnoldi)
+    apply_m = (lambda v: v) if precond is None else precond
     nmv = 0
     converged = halted = False
     while nmv < maxiter and not converged and not halted:
         if bool(torch.any(x != 0).item()):
-            r = b - matvec(x)
+            r = apply_m(b - matvec(x))
             nmv += 1
             if callback is not None and callback(float(torch.linalg.vector_norm(r).item())):
                 halted = True
                 break
         else:
-            r = b.clone()
+            r = apply_m(b.clone())
         beta = float(torch.linalg.vector_norm(r).item())
         if beta <= tol_abs:
             converged = True
@@ -408,7 +447,7 @@ def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, 
         q[0] = r / beta
         cols, cs, sn, gam = [], [], [], [beta]
         for j in range(m):
-            w = matvec(q[j])
+            w = apply_m(matvec(q[j]))
             nmv += 1
             qj = q[:j + 1]
             c1 = qj @ w
@@ -625,7 +664,11 @@ def run_krylov(solver, callback=None, progress_every: int = 0):
             reached = n
         return reached >= 0 and n - reached > max(64, reached // 4)
 
-    ar = cached(solver, ("arnoldi64", cap), lambda: ArnoldiGraphs(op, g, cap)) if cap <= 63 else None
+    precond = None
+    if c.scheme.krylov_precond and getattr(solver, "acc", None) is not None:
+        precond = MomentPreconditioner(solver, solver.acc)
+    ar = (cached(solver, ("arnoldi64", cap), lambda: ArnoldiGraphs(op, g, cap))
+          if cap <= 63 and precond is None else None)
     if ar is not None:
         ar.set_g(g)
         ar.on_product = product
@@ -637,7 +680,7 @@ def run_krylov(solver, callback=None, progress_every: int = 0):
             break
         reached = -1
         x, _, _ = gmres(matvec, g, x0=x, tol_abs=target, maxiter=budget, max_basis=cap, callback=on_residual,
-                        arnoldi=ar)
+                        arnoldi=ar, precond=precond)
         sweep(x)
         op.publish()
         final = solver.ctx.true_residual(solver.mom, solver.vdf)
@@ -653,6 +696,6 @@ def run_krylov(solver, callback=None, progress_every: int = 0):
     solver.ctx.sweep_count += op.sweeps
     masses = [solver.mom.mass] * len(residuals)
     return solver._record(len(residuals), converged, residuals, masses, wall, "KRYLOV",
-                          extra={"krylov_size": op.n, "krylov_periodic_state": 0, "krylov_basis_cap": cap,
-                                 "krylov_precond": False, "transport_residual": final},
+                          extra={"krylov_size": op.n, "krylov_periodic_state": op.nper, "krylov_basis_cap": cap,
+                                 "krylov_precond": precond is not None, "transport_residual": final},
                           true_res=true_res if want_true else None)

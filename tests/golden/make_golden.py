@@ -303,9 +303,51 @@ def periodic(ref: Path) -> dict:
     return meta
 
 
+def krylov_precond(ref: Path) -> dict:
+    """6. GMRES(30) with pybte's moment preconditioner
+    (``scheme.krylov_precond``, ``pybte/krylov.py:369-414``) on the 5 x 5
+    cavity, diffusive (tau_R = 0.01) and ballistic (tau_R = 1) ends."""
+    sys.path[:0] = [str(ref / "solver-python"), str(ref / "solver-python" / "tools")]
+    from make_meshes import build
+    from pybte import Case, Solver
+    from pybte import krylov as rkrylov
+
+    tmp = _scratch()
+    msh = tmp / "A1_Nx6_Ny6.msh"
+    msh.write_text(build(5, "cavity", "smootherstep"))
+    meta, out = {}, {}
+    orig_cap = rkrylov.krylov_basis_cap
+    rkrylov.krylov_basis_cap = lambda *a: 30
+    for name, tau_r in (("precond_diffusive", 0.01), ("precond_ballistic", 1.0)):
+        c = Case.from_dict({
+            "iteration": {"tol": 1e-8, "tmax": 20000},
+            "scheme": {"accflag": 1, "method": "krylov", "krylov_precond": True},
+            "velmesh": {"npole": 4, "nazim": 8}, "dg": {"deg": 1},
+            "flow": {"cv": 1.0, "vg": 1.0, "tau_r": tau_r, "tau_n": 0.1 * tau_r, "tau_thr": 1.0},
+            "mesh": {"file": str(msh)},
+            "boundaries": [{"name": "SWall", "phyid": 11, "type": "thermalising", "temp": 0.0},
+                           {"name": "NWall", "phyid": 12, "type": "thermalising", "temp": 1.0},
+                           {"name": "EWall", "phyid": 13, "type": "thermalising", "temp": -0.5},
+                           {"name": "WWall", "phyid": 14, "type": "thermalising", "temp": 0.5}],
+            "output": {"field": False, "runtime_log": False, "run_record": False}}, basedir=str(tmp))
+        rec = Solver(c).run()
+        out[f"{name}_temp"] = rec.temp
+        out[f"{name}_ts"] = rec.temp_dofs
+        meta[name] = {"tau_r": tau_r, "iterations": int(rec.iterations), "converged": bool(rec.converged),
+                      "mass": float(rec.mass)}
+        print(name, rec.iterations, rec.converged, flush=True)
+    rkrylov.krylov_basis_cap = orig_cap
+    np.savez_compressed(OUT / "krylov_precond.npz", **out)
+    return meta
+
+
 if __name__ == "__main__":
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if "--periodic-only" in sys.argv[2:]:
+    if "--precond-only" in sys.argv[2:]:
+        m = json.loads((OUT / "golden_meta.json").read_text())
+        m.update(krylov_precond(Path(ref_root)))
+        (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
+    elif "--periodic-only" in sys.argv[2:]:
         m = json.loads((OUT / "golden_meta.json").read_text())
         m.update(periodic(Path(ref_root)))
         (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))

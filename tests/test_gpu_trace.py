@@ -67,6 +67,23 @@ def test_gsis_step_matches_oracle(cuda, kind):
         assert _rel(h[k], getattr(o, k)) < 1e-10, k
 
 
+@pytest.mark.parametrize("name", ["precond_diffusive", "precond_ballistic"])
+def test_krylov_moment_preconditioner_matches_reference(cuda, name):
+    """GMRES(30) with pybte's moment preconditioner (scheme.krylov_precond)
+    against pybte's own run: sweeps within 2 %, temperatures within 1e-8."""
+    from cases import golden, meta
+    m = meta()[name]
+    z = golden("krylov_precond")
+    c = small_case(1, 4, 8, m["tau_r"], 0.1 * m["tau_r"], south="thermalising", accflag=1, method="krylov",
+                   krylov_restart=30)
+    c.scheme.krylov_precond = True
+    rec = Solver(c).run()
+    assert rec.converged == m["converged"]
+    assert rec.diagnostics["krylov_precond"] is True
+    assert abs(rec.iterations - m["iterations"]) <= max(2, int(0.02 * m["iterations"]))
+    assert _rel(rec.temp, z[f"{name}_temp"]) < 1e-8
+
+
 @pytest.mark.parametrize("name", ["gsis_deg2_adiabatic", "gsis_deg1_isothermal"])
 def test_gsis_device_and_host_trace_solves_agree(cuda, name):
     recs = {}
