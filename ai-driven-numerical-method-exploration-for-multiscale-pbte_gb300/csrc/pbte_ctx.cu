@@ -14,9 +14,11 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <thread>
 #include <unordered_map>
 #include <vector>
 
@@ -277,21 +279,33 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
 
     // ---- direction classes and wavefront levels -------------------------
     // sign pattern of c.n over the interior and periodic faces, hashed
-    // (FNV-1a) and then compared in full against the class representative
-    std::vector<int32_t> iface_tri, iface_lfc;
-    for (int f = 0; f < d->n_faces; ++f)
-        if (d->face_bc[f] < 0 || pslot[f] >= 0) {
-            int t = d->face_tri[f * 2 + 0] >= 0 ? d->face_tri[f * 2 + 0] : d->face_tri[f * 2 + 1];
-            int l = d->face_tri[f * 2 + 0] >= 0 ? d->face_lfc[f * 2 + 0] : d->face_lfc[f * 2 + 1];
-            iface_tri.push_back(t);
-            iface_lfc.push_back(l);
+    // (FNV-1a) and then compared in full against the class representative.
+    // A face's sign depends only on the exact bits of its normal, so the
+    // pattern is taken over the distinct normals (a handful on structured
+    // meshes, at most one per face): the same classes as face by face.
+    std::vector<double> unx, uny;
+    {
+        std::unordered_map<uint64_t, std::vector<int>> seen;   // hash of the bits -> distinct ids
+        auto bits = [](double v) { uint64_t u; std::memcpy(&u, &v, sizeof u); return u; };
+        for (int f = 0; f < d->n_faces; ++f) {
+            if (!(d->face_bc[f] < 0 || pslot[f] >= 0)) continue;
+            const int t = d->face_tri[f * 2 + 0] >= 0 ? d->face_tri[f * 2 + 0] : d->face_tri[f * 2 + 1];
+            const int l = d->face_tri[f * 2 + 0] >= 0 ? d->face_lfc[f * 2 + 0] : d->face_lfc[f * 2 + 1];
+            const double nx = d->nx[t * 3 + l], ny = d->ny[t * 3 + l];
+            const uint64_t h = bits(nx) * 0x9E3779B97F4A7C15ull ^ bits(ny);
+            auto &ids = seen[h];
+            bool dup = false;
+            for (int q : ids)
+                if (bits(unx[q]) == bits(nx) && bits(uny[q]) == bits(ny)) { dup = true; break; }
+            if (dup) continue;
+            ids.push_back((int)unx.size());
+            unx.push_back(nx);
+            uny.push_back(ny);
         }
+    }
     auto pattern = [&](int dir, std::vector<int8_t> &p) {
-        p.resize(iface_tri.size());
-        for (size_t k = 0; k < iface_tri.size(); ++k) {
-            int t = iface_tri[k], l = iface_lfc[k];
-            p[k] = sgn(d->cxv[dir] * d->nx[t * 3 + l] + d->cyv[dir] * d->ny[t * 3 + l]);
-        }
+        p.resize(unx.size());
+        for (size_t k = 0; k < unx.size(); ++k) p[k] = sgn(d->cxv[dir] * unx[k] + d->cyv[dir] * uny[k]);
     };
     std::unordered_multimap<uint64_t, int> by_hash;  // hash -> class id
     std::vector<int> class_rep;
@@ -317,7 +331,6 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     c->nclass = (int)class_rep.size();
     std::vector<int32_t> lvl_cells((size_t)c->nclass * nt), lvl_ptr, class_off(c->nclass),
         class_nlev(c->nclass);
-    std::vector<int32_t> level, indeg, queue, count, pos(nt), far_idx;
     const size_t M = (size_t)c->nclass * nt;   // field stride of the sweep records
     std::vector<double> rf64(M * pbte::kNumRecReal);
     std::vector<float> rf32(M * pbte::kNumRecReal);
@@ -327,17 +340,21 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     // R = 1 + the largest level gap of an in-sweep dependency, W = widest level
     std::vector<int32_t> up_slot((size_t)c->nclass * nt * 3, -1), class_W(c->nclass), class_R(c->nclass);
     std::vector<uint8_t> fresh(c->n_pfaces ? (size_t)c->nclass * nt : 0, 0);
-    std::vector<int32_t> succ_ptr, succ, rpos;
-    for (int k = 0; k < c->nclass; ++k) {
+    // The classes are independent: each builds its levels, ring slots and
+    // records into its own stretch of the shared arrays, on host threads.
+    struct ClassOut {
+        int status = PBTE_OK, nlev = 0, W = 0, R = 1, nfar = 0;
+        std::vector<int32_t> count;   // level offsets within the class, nlev + 1
+    };
+    std::vector<ClassOut> cls_out(c->nclass);
+    auto build_class = [&](int k, ClassOut &o) {
+        std::vector<int32_t> level, indeg, queue, count, pos(nt), far_idx, succ_ptr, succ, rpos;
         int dir = class_rep[k];
         uint8_t *fr = c->n_pfaces ? fresh.data() + (size_t)k * nt : nullptr;
         if (fr) {
             // a periodic inflow reads this sweep's partner value when the
             // partner comes first in pybte's order for these directions
-            if (!reference_order(d, d->cxv[dir], d->cyv[dir], rpos)) {
-                pbte_ctx_destroy(c);
-                return PBTE_ERR_CYCLE;
-            }
+            if (!reference_order(d, d->cxv[dir], d->cyv[dir], rpos)) { o.status = PBTE_ERR_CYCLE; return; }
             for (int i = 0; i < nt; ++i)
                 for (int il = 0; il < 3; ++il) {
                     const int fc = d->tri_faces[i * 3 + il];
@@ -348,8 +365,8 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
                 }
         }
         if (!levels_for(d, d->cxv[dir], d->cyv[dir], fr, level, indeg, queue, succ_ptr, succ)) {
-            pbte_ctx_destroy(c);
-            return PBTE_ERR_CYCLE;
+            o.status = PBTE_ERR_CYCLE;
+            return;
         }
         int nlev = 0;
         for (int i = 0; i < nt; ++i) nlev = std::max(nlev, level[i] + 1);
@@ -358,9 +375,6 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         int W = 0;
         for (int L = 0; L < nlev; ++L) W = std::max(W, count[L + 1]);
         for (int L = 0; L < nlev; ++L) count[L + 1] += count[L];
-        class_off[k] = (int32_t)lvl_ptr.size();
-        class_nlev[k] = nlev;
-        for (int L = 0; L <= nlev; ++L) lvl_ptr.push_back(count[L] + k * nt);
         std::vector<int32_t> fill(count.begin(), count.end() - 1);
         for (int i = 0; i < nt; ++i) {
             pos[i] = fill[level[i]] - count[level[i]];
@@ -393,7 +407,6 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
                 }
             }
         }
-        c->far_max = std::max(c->far_max, nfar);
         for (int p = 0; p < nt; ++p) {
             const size_t kp = (size_t)k * nt + p;
             const int i = lvl_cells[kp];
@@ -426,9 +439,38 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
             ri[pbte::kIFarOut * M + kp] = far_idx[i];
             ri[pbte::kIKind * M + kp] = (int32_t)kinds;
         }
-        c->nlev_max = std::max(c->nlev_max, nlev);
-        c->ring_W = std::max(c->ring_W, W);
-        c->ring_R = std::max(c->ring_R, R);
+        o.nlev = nlev;
+        o.W = W;
+        o.R = R;
+        o.nfar = nfar;
+        o.count = std::move(count);
+    };
+    {
+        std::atomic<int> next{0};
+        auto worker = [&]() {
+            for (int k = next++; k < c->nclass; k = next++) build_class(k, cls_out[k]);
+        };
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const int nth = (int)std::min<unsigned>({hw, 16u, (unsigned)c->nclass});
+        std::vector<std::thread> pool;
+        try {
+            for (int t = 1; t < nth; ++t) pool.emplace_back(worker);
+        } catch (...) {
+            // no more threads: the calling thread takes the remaining classes
+        }
+        worker();
+        for (auto &th : pool) th.join();
+    }
+    for (int k = 0; k < c->nclass; ++k) {
+        const ClassOut &o = cls_out[k];
+        if (o.status != PBTE_OK) { pbte_ctx_destroy(c); return o.status; }
+        class_off[k] = (int32_t)lvl_ptr.size();
+        class_nlev[k] = o.nlev;
+        for (int L = 0; L <= o.nlev; ++L) lvl_ptr.push_back(o.count[L] + k * nt);
+        c->far_max = std::max(c->far_max, o.nfar);
+        c->nlev_max = std::max(c->nlev_max, o.nlev);
+        c->ring_W = std::max(c->ring_W, o.W);
+        c->ring_R = std::max(c->ring_R, o.R);
     }
     // z-mirror twins: ordinates with the same in-plane velocity (and weight)
     // see the same transport; one block sweeps the pair and stores both
