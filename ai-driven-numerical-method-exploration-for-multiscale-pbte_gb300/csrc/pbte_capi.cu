@@ -172,6 +172,28 @@ int pbte_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_h
     return pbte::launch_correct(c, vdf, uq, tri_hmin, tau_thr, use_hmin, ts, qxs, qys, temp, qx, qy, S(stream));
 }
 
+int pbte_gmres_columns_f32(pbte_ctx *c, const pbte_gmres_cycle_f32 *a, int32_t j0, int32_t j1, void *stream) {
+    if (!c || !a || j0 < 0 || j1 <= j0 || j1 >= 64 || !a->Q || !a->uin || !a->uout || !a->w || !a->state) return PBTE_ERR_ARG;
+    if (a->ldq < a->n || a->ldr < j1) return PBTE_ERR_ARG;
+    const int32_t *before = c->done;
+    c->done = a->state;
+    int rc = PBTE_OK;
+    for (int32_t j = j0; j < j1 && rc == PBTE_OK; ++j) {
+        rc = pbte_fixed_point_f32(c, a->ts, a->qxs, a->qys, a->flux_wall_in, a->wall_scale, a->vdf32, a->ts_out,
+                                  a->qxs_out, a->qys_out, a->flux_wall_out, a->temp, a->qx, a->qy, stream);
+        if (rc == PBTE_OK)
+            rc = pbte_arnoldi_column_f32(a->Q, a->ldq, j + 1, a->uout, a->g, a->w, a->n, a->h, a->scratch,
+                                         a->scratch_len, a->state, stream);
+        if (rc == PBTE_OK)
+            rc = pbte_gmres_givens(j, a->h, a->R, a->ldr, a->cs, a->sn, a->gam, a->tol_abs, a->state, a->hist,
+                                   stream);
+        if (rc == PBTE_OK)
+            rc = pbte_gmres_next_basis_f32(j, a->w, a->h, a->Q, a->ldq, a->uin, a->n, a->state, stream);
+    }
+    c->done = before;
+    return rc;
+}
+
 int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int32_t *singular, void *stream) {
     if (!a || !inv || !singular || n < 0 || m <= 0) return PBTE_ERR_ARG;
     return pbte::launch_batched_inverse(a, inv, n, m, singular, S(stream));

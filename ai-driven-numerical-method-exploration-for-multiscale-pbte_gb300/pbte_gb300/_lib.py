@@ -90,6 +90,19 @@ class CaseDesc(ctypes.Structure):
                 ("int_tri", _d)]
 
 
+class GmresCycleF32(ctypes.Structure):
+    """Mirror of ``pbte_gmres_cycle_f32`` (the buffers of
+    ``pbte_gmres_columns_f32``)."""
+    _fields_ = [("ts", _vp), ("qxs", _vp), ("qys", _vp), ("flux_wall_in", _vp),
+                ("wall_scale", ctypes.c_double), ("vdf32", _vp),
+                ("ts_out", _vp), ("qxs_out", _vp), ("qys_out", _vp), ("flux_wall_out", _vp),
+                ("temp", _vp), ("qx", _vp), ("qy", _vp),
+                ("Q", _vp), ("ldq", ctypes.c_int64), ("uout", _vp), ("g", _vp), ("uin", _vp), ("w", _vp),
+                ("n", ctypes.c_int64), ("h", _vp), ("scratch", _vp), ("scratch_len", ctypes.c_int64),
+                ("R", _vp), ("ldr", ctypes.c_int32), ("cs", _vp), ("sn", _vp), ("gam", _vp),
+                ("tol_abs", _vp), ("state", _vp), ("hist", _vp)]
+
+
 _SIGS = {
     "pbte_ctx_create": ([ctypes.POINTER(CaseDesc), ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
     "pbte_ctx_destroy": ([_vp], ctypes.c_int),
@@ -127,6 +140,8 @@ _SIGS = {
                               ctypes.c_int),
     "pbte_gmres_next_basis_f32": ([ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp, _vp],
                                   ctypes.c_int),
+    "pbte_gmres_columns_f32": ([_vp, ctypes.POINTER(GmresCycleF32), ctypes.c_int32, ctypes.c_int32, _vp],
+                               ctypes.c_int),
     "pbte_hot_source": ([_vp, _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],

@@ -16,6 +16,7 @@ decided on the true transport residual.  ``iterations`` counts sweeps.
 """
 from __future__ import annotations
 
+import ctypes
 import time
 
 import numpy as np
@@ -242,6 +243,10 @@ class ArnoldiGraphs:
     #: columns per captured chunk of a cycle (the host checks the stop state
     #: after each chunk)
     CHUNK = 10
+    #: a chunk of a cycle with the FP32 product and basis is issued by one
+    #: native call (``pbte_gmres_columns_f32``) instead of four calls per
+    #: column from Python: the same launches, recorded and issued faster
+    native_columns = True
 
     def _cycle_buffers(self) -> None:
         if getattr(self, "cycle_graphs", None) is not None:
@@ -259,12 +264,37 @@ class ArnoldiGraphs:
         self.state_host = torch.zeros(4, dtype=torch.int32, pin_memory=True)
         self.cycle_graphs = {}
 
+    def _cycle_desc(self):
+        """The buffers of a cycle with the FP32 product and FP32 basis, for
+        ``pbte_gmres_columns_f32`` (which issues a chunk's launches from
+        native code); None for the other forms."""
+        op = self.op
+        if op.precision == "fp64" or self.dtype != torch.float32 or op.per:
+            return None
+        p = op._ptr
+        ts, qxs, qys, fw, _ = op._views(op.uin)
+        ots, oqxs, oqys, ofw, _ = op._views(op.uout)
+        ints = (op.temp, op.qx, op.qy) if op.integrals else (None, None, None)
+        return _lib.GmresCycleF32(
+            ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), p(fw), 0.0 if op.homogeneous else 1.0,
+            op.vdf.data_ptr(), ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(), p(ofw), *(p(t) for t in ints),
+            self.Q.data_ptr(), self.Q.stride(0), op.uout.data_ptr(), p(self.g), op.uin.data_ptr(),
+            self.w.data_ptr(), self.n, self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(),
+            self.R.data_ptr(), self.m_cap, self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(),
+            self.tol.data_ptr(), self.state.data_ptr(), self.hist.data_ptr())
+
     def _record_cycle(self, j0: int, j1: int) -> None:
         """Columns j0..j1-1: product, CGS2, rotation, next basis vector; all
         of it skipped once the stop state is set."""
         L = _lib.lib()
         s = torch.cuda.current_stream().cuda_stream
         n, ctx = self.n, self.op.s.ctx.handle
+        if self.native_columns:
+            if getattr(self, "_desc", None) is None:
+                self._desc = self._cycle_desc()
+            if self._desc is not None:
+                _lib.check(L.pbte_gmres_columns_f32(ctx, ctypes.byref(self._desc), j0, j1, s), "gmres_columns_f32")
+                return
         _lib.check(L.pbte_set_done_flag(ctx, self.state.data_ptr()), "set_done_flag")
         try:
             for j in range(j0, j1):

@@ -265,6 +265,41 @@ int pbte_gmres_next_basis(int32_t j, const double *w, const double *h, double *Q
 int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float *Q, int64_t ldq,
                               double *uin, int64_t n, const int32_t *state, void *stream);
 
+/* Columns j0..j1-1 of a GMRES restart cycle with the FP32 fixed-point
+ * product, issued from native code (one call records a whole chunk of a
+ * captured cycle): per column pbte_fixed_point_f32 on the operator input,
+ * pbte_arnoldi_column_f32 (rows j+1, done = state), pbte_gmres_givens and
+ * pbte_gmres_next_basis_f32, with `state` installed as the context's stop
+ * flag for the duration (pbte_set_done_flag), exactly the launches of
+ * those calls made one by one -- gmres_full's column loop
+ * (pybte/krylov.py:190-240) for the mixed solver's inner GMRES.  The
+ * operator views (ts/qxs/qys/flux_wall_in of the input uin, the outputs of
+ * uout) are those pbte_fixed_point_f32 takes; flux_wall_in/out may be NULL
+ * without adiabatic walls, temp/qx/qy may be NULL.  0 <= j0 < j1,
+ * j1 + 1 <= rows of Q, j1 < 64. */
+typedef struct {
+    const double *ts, *qxs, *qys, *flux_wall_in;   /* operator input: views of uin */
+    double wall_scale;
+    float *vdf32;                                  /* FP32 distribution scratch */
+    double *ts_out, *qxs_out, *qys_out, *flux_wall_out, *temp, *qx, *qy;  /* views of uout */
+    float *Q;                                      /* basis rows, leading dimension ldq */
+    int64_t ldq;
+    const double *uout, *g;                        /* g may be NULL */
+    double *uin;
+    float *w;
+    int64_t n;
+    double *h, *scratch;
+    int64_t scratch_len;
+    double *R;
+    int32_t ldr;
+    double *cs, *sn, *gam;
+    const double *tol_abs;
+    int32_t *state;
+    double *hist;
+} pbte_gmres_cycle_f32;
+int pbte_gmres_columns_f32(pbte_ctx *ctx, const pbte_gmres_cycle_f32 *cyc, int32_t j0, int32_t j1,
+                           void *stream);
+
 /* GSIS per-iteration kernels (pybte/acceleration/):
  * third-order moment source, hot_source.py:29-58 -> work[n_tris][7*ndof];
  * kinetic wall-trace moments, global_solve.py:31-53 -> out[nk][3*ndof_fc];

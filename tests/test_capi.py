@@ -57,3 +57,20 @@ def test_cgs2_rejects_short_scratch_on_the_host():
         assert fn(p, 4, 1, p, 4, p, p, short, None) == -1
     for fn in (L.pbte_arnoldi_column, L.pbte_arnoldi_column_f32):
         assert fn(p, 4, 1, p, None, p, 4, p, p, short, None, None) == -1
+
+
+def test_gmres_cycle_struct_matches_header():
+    """The ctypes mirror of pbte_gmres_cycle_f32 names the header's members
+    in the header's order."""
+    text = HEADER.read_text()
+    end = text.index("} pbte_gmres_cycle_f32;")
+    body = re.sub(r"/\*.*?\*/", "", text[text.rindex("typedef struct {", 0, end):end], flags=re.S)
+    names = [m for line in body.splitlines()[1:] for m in re.findall(r"\**\s*(\w+)\s*(?=[,;])", line)]
+    assert names == [f for f, _ in _lib.GmresCycleF32._fields_]
+
+
+def test_gmres_columns_rejects_bad_arguments_on_the_host():
+    L = _lib.lib()
+    cyc = _lib.GmresCycleF32()
+    assert L.pbte_gmres_columns_f32(None, ctypes.byref(cyc), 0, 1, None) == -1
+    assert L.pbte_gmres_columns_f32(None, None, 0, 1, None) == -1

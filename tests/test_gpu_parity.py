@@ -287,6 +287,28 @@ def test_device_gmres_cycles_match_host_rotations(cuda, graphs):
     assert _rel(a.temp_dofs, b.temp_dofs) < 1e-10 and _rel(a.qx_dofs, b.qx_dofs) < 1e-10
 
 
+@pytest.mark.parametrize("graphs", [True, False])
+def test_native_gmres_columns_issue_the_same_launches(cuda, monkeypatch, graphs):
+    """The mixed solve's inner cycles with each chunk issued by one native
+    call (pbte_gmres_columns_f32) against the same launches issued column by
+    column from Python, captured or direct: bit for bit the same solve."""
+    from pbte_gb300.krylov import ArnoldiGraphs
+    base = dict(deg=2, npole=4, nazim=8, tau_r=0.2, tau_n=0.02, method="krylov", precision="mixed",
+                krylov_restart=12)
+    out = {}
+    for native in (True, False):
+        monkeypatch.setattr(ArnoldiGraphs, "native_columns", native)
+        s = Solver(small_case(**base))
+        s.use_graphs = graphs
+        out[native] = s.run()
+        s.release()
+    a, b = out[True], out[False]
+    assert a.converged and b.converged
+    assert a.diagnostics["fp32_sweeps"] == b.diagnostics["fp32_sweeps"] > 0
+    assert a.iterations == b.iterations
+    assert np.array_equal(a.temp_dofs, b.temp_dofs) and np.array_equal(a.qx_dofs, b.qx_dofs)
+
+
 @pytest.mark.parametrize("m", [21, 42, 70, 105])
 def test_batched_inverse_sizes(cuda, m):
     """The HDG element inverses (7 N_p: P1 21 ... P4 105) against LAPACK."""
