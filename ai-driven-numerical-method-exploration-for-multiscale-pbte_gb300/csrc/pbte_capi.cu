@@ -175,20 +175,39 @@ int pbte_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_h
 int pbte_gmres_columns_f32(pbte_ctx *c, const pbte_gmres_cycle_f32 *a, int32_t j0, int32_t j1, void *stream) {
     if (!c || !a || j0 < 0 || j1 <= j0 || j1 >= 64 || !a->Q || !a->uin || !a->uout || !a->w || !a->state) return PBTE_ERR_ARG;
     if (a->ldq < a->n || a->ldr < j1) return PBTE_ERR_ARG;
+    if (!a->ts || !a->qxs || !a->qys || !a->vdf32 || !a->ts_out || !a->qxs_out || !a->qys_out) return PBTE_ERR_ARG;
+    if (c->n_wall_ad && (!a->flux_wall_in || !a->flux_wall_out)) return PBTE_ERR_ARG;
+    if ((a->temp == nullptr) != (a->qx == nullptr) || (a->temp == nullptr) != (a->qy == nullptr)) return PBTE_ERR_ARG;
+    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
+    // the operator input is the state itself ([ts | qxs | qys | ...] = uin):
+    // then the basis update can also form the next product's moment sources
+    const int64_t k = (int64_t)c->nd * c->n_tris;
+    const bool state_input = a->ts == a->uin && a->qxs == a->uin + k && a->qys == a->uin + 2 * k;
     const int32_t *before = c->done;
     c->done = a->state;
     int rc = PBTE_OK;
+    // the basis update of column j also leaves column j+1's moment sources
+    // (launch_next_basis_sources), so only a call's first product forms them
+    bool have_sources = false;
     for (int32_t j = j0; j < j1 && rc == PBTE_OK; ++j) {
-        rc = pbte_fixed_point_f32(c, a->ts, a->qxs, a->qys, a->flux_wall_in, a->wall_scale, a->vdf32, a->ts_out,
-                                  a->qxs_out, a->qys_out, a->flux_wall_out, a->temp, a->qx, a->qy, stream);
+        rc = pbte::launch_fixed_point32(c, a->ts, a->qxs, a->qys, a->flux_wall_in, a->wall_scale, a->vdf32,
+                                        a->ts_out, a->qxs_out, a->qys_out, a->flux_wall_out, a->temp, a->qx, a->qy,
+                                        S(stream), !have_sources);
         if (rc == PBTE_OK)
             rc = pbte_arnoldi_column_f32(a->Q, a->ldq, j + 1, a->uout, a->g, a->w, a->n, a->h, a->scratch,
                                          a->scratch_len, a->state, stream);
         if (rc == PBTE_OK)
             rc = pbte_gmres_givens(j, a->h, a->R, a->ldr, a->cs, a->sn, a->gam, a->tol_abs, a->state, a->hist,
                                    stream);
-        if (rc == PBTE_OK)
-            rc = pbte_gmres_next_basis_f32(j, a->w, a->h, a->Q, a->ldq, a->uin, a->n, a->state, stream);
+        if (rc == PBTE_OK) {
+            const bool fuse = state_input;
+            rc = fuse ? pbte::launch_next_basis_sources(c, j, a->w, a->h, a->Q, a->ldq, a->uin, a->n, a->state,
+                                                        S(stream))
+                      : PBTE_ERR_UNSUPPORTED;
+            have_sources = rc == PBTE_OK;
+            if (rc == PBTE_ERR_UNSUPPORTED)
+                rc = pbte_gmres_next_basis_f32(j, a->w, a->h, a->Q, a->ldq, a->uin, a->n, a->state, stream);
+        }
     }
     c->done = before;
     return rc;

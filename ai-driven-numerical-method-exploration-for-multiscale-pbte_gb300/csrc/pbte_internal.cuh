@@ -151,10 +151,16 @@ int launch_sweep32(pbte_ctx *c, float *vdf32, const double *flux_wall, double wa
                    cudaStream_t s, bool store_twin = true, bool by_udir = false);
 // the FP32 fixed-point product with z-mirror twins folded (one copy per
 // in-plane velocity written and read): sources, sweep, moments, emission
+// with_sources = false: the moment sources of the inputs are already in
+// d_S32 (left by launch_next_basis_sources)
 int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
                          const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
                          double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
-                         double *qy, cudaStream_t s);
+                         double *qy, cudaStream_t s, bool with_sources = true);
+// GMRES next basis vector (FP32 basis) plus the moment sources of the next
+// FP32 product into d_S32; PBTE_ERR_UNSUPPORTED for N_p other than 3, 6, 10
+int launch_next_basis_sources(pbte_ctx *c, int j, const float *w, const double *h, float *Q, int64_t ldq,
+                              double *uin, int64_t n, const int32_t *state, cudaStream_t s);
 int launch_factorise(pbte_ctx *c, cudaStream_t s);
 int launch_factorise32(pbte_ctx *c, cudaStream_t s);
 int launch_moments64(pbte_ctx *c, const double *vdf, double *ts, double *qxs, double *qys,

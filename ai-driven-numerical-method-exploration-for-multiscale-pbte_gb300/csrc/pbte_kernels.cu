@@ -850,15 +850,67 @@ static int wall_flux_impl(pbte_ctx *c, const T *vdf, double *fw, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
+// q_{j+1} = w / h[j+1] as gmres_next_basis_kernel<float> does (row j+1 of
+// the basis, widened into the operator input uin), one thread per state
+// entry; a thread of the moment block (entry t = b * NP * nt + m * nt + e:
+// moment b, DOF m, element e) also forms source entry (e, b, m) of the next
+// sweep with sources_np_kernel's arithmetic, from the element's widened
+// values of moment b (the other DOFs' entries are read again: they are in
+// L1/L2).  Nothing once state[0] != 0.
+template <int NP>
+__global__ void next_basis_sources_kernel(int j, const float *__restrict__ w, const double *__restrict__ h,
+                                          float *__restrict__ Q, long long ldq, double *__restrict__ uin,
+                                          long long n, const int32_t *state, const CellRec<double> *cells,
+                                          const double *__restrict__ ref_mass, float *__restrict__ S, int nt) {
+    if (*(volatile const int32_t *)state != 0) return;
+    const float hn = (float)h[j + 1];
+    float *q = Q + (size_t)(j + 1) * ldq;
+    const long long k = (long long)NP * nt;
+    for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n;
+         t += (long long)gridDim.x * blockDim.x) {
+        const float f = w[t] / hn;
+        q[t] = f;
+        uin[t] = (double)f;
+        if (t < 3 * k) {
+            const int b = (int)(t / k);
+            const long long r = t - b * k;
+            const int m = (int)(r / nt), e = (int)(r - (long long)m * nt);
+            const float *wb = w + b * k + e;
+            double acc = 0.0;
+#pragma unroll
+            for (int l = 0; l < NP; ++l) acc += ref_mass[l * NP + m] * (double)(wb[(long long)l * nt] / hn);
+            S[((size_t)e * 3 + b) * NP + m] = (float)(cells[e].area2 * acc);
+        }
+    }
+}
+
+int launch_next_basis_sources(pbte_ctx *c, int j, const float *w, const double *h, float *Q, int64_t ldq,
+                              double *uin, int64_t n, const int32_t *state, cudaStream_t s) {
+    const long long k = (long long)c->nd * c->n_tris;
+    if (n < 3 * k || ldq < n) return PBTE_ERR_ARG;
+    const int th = 256;
+    const int bl = (int)std::min<long long>((n + th - 1) / th, 152 * 8);
+    auto go = [&](auto kern) {
+        kern<<<bl, th, 0, s>>>(j, w, h, Q, ldq, uin, n, state, c->d_cells64, c->d_ref64, c->d_S32, c->n_tris);
+        return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+    };
+    switch (c->nd) {
+        case 3: return go(next_basis_sources_kernel<3>);
+        case 6: return go(next_basis_sources_kernel<6>);
+        case 10: return go(next_basis_sources_kernel<10>);
+        default: return PBTE_ERR_UNSUPPORTED;
+    }
+}
+
 int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
                          const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
                          double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
-                         double *qy, cudaStream_t s) {
+                         double *qy, cudaStream_t s, bool with_sources) {
     // folded kernels exist for N_p = 3, 6, 10 and the ring sweep (which
     // writes rows by distinct velocity u); otherwise every ordinate is
     // stored and read
     bool fold = c->nd == 3 || c->nd == 6 || c->nd == 10;
-    int rc = launch_sources(c, ts, qxs, qys, true, s);
+    int rc = with_sources ? launch_sources(c, ts, qxs, qys, true, s) : PBTE_OK;
     if (rc) return rc;
     if (fold) {
         rc = launch_sweep32(c, vdf32, fw_in, wall_scale, s, false, true);

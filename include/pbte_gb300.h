@@ -275,8 +275,11 @@ int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float 
  * (pybte/krylov.py:190-240) for the mixed solver's inner GMRES.  The
  * operator views (ts/qxs/qys/flux_wall_in of the input uin, the outputs of
  * uout) are those pbte_fixed_point_f32 takes; flux_wall_in/out may be NULL
- * without adiabatic walls, temp/qx/qy may be NULL.  0 <= j0 < j1,
- * j1 + 1 <= rows of Q, j1 < 64. */
+ * without adiabatic walls, temp/qx/qy may be NULL.  When ts/qxs/qys are the
+ * first 3 * ndof * n_tris entries of uin in that order (the Krylov state),
+ * the basis update of column j also forms column j+1's moment sources
+ * (the same FP64 arithmetic), so only the call's first product launches
+ * them.  0 <= j0 < j1, j1 + 1 <= rows of Q, j1 < 64. */
 typedef struct {
     const double *ts, *qxs, *qys, *flux_wall_in;   /* operator input: views of uin */
     double wall_scale;
