@@ -194,11 +194,9 @@ int pbte_gmres_columns_f32(pbte_ctx *c, const pbte_gmres_cycle_f32 *a, int32_t j
                                         a->ts_out, a->qxs_out, a->qys_out, a->flux_wall_out, a->temp, a->qx, a->qy,
                                         S(stream), !have_sources);
         if (rc == PBTE_OK)
-            rc = pbte_arnoldi_column_f32(a->Q, a->ldq, j + 1, a->uout, a->g, a->w, a->n, a->h, a->scratch,
-                                         a->scratch_len, a->state, stream);
-        if (rc == PBTE_OK)
-            rc = pbte_gmres_givens(j, a->h, a->R, a->ldr, a->cs, a->sn, a->gam, a->tol_abs, a->state, a->hist,
-                                   stream);
+            rc = pbte::arnoldi_column_givens_f32(a->Q, a->ldq, j + 1, a->uout, a->g, a->w, a->n, a->h, a->scratch,
+                                                 a->scratch_len, a->R, a->ldr, a->cs, a->sn, a->gam, a->tol_abs,
+                                                 a->state, a->hist, S(stream));
         if (rc == PBTE_OK) {
             const bool fuse = state_input;
             rc = fuse ? pbte::launch_next_basis_sources(c, j, a->w, a->h, a->Q, a->ldq, a->uin, a->n, a->state,

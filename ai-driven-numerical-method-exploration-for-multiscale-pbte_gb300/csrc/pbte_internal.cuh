@@ -157,6 +157,12 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
                          const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
                          double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
                          double *qy, cudaStream_t s, bool with_sources = true);
+// pbte_arnoldi_column_f32 + pbte_gmres_givens for column rows - 1, the
+// rotation run by the last block of the CGS2 norm pass (pbte_krylov.cu)
+int arnoldi_column_givens_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
+                              float *w, int64_t n, double *h, double *scratch, int64_t scratch_len, double *R,
+                              int32_t ldr, double *cs, double *sn, double *gam, const double *tol_abs,
+                              int32_t *state, double *hist, cudaStream_t s);
 // GMRES next basis vector (FP32 basis) plus the moment sources of the next
 // FP32 product into d_S32; PBTE_ERR_UNSUPPORTED for N_p other than 3, 6, 10
 int launch_next_basis_sources(pbte_ctx *c, int j, const float *w, const double *h, float *Q, int64_t ldq,

@@ -174,6 +174,21 @@ __device__ __forceinline__ void dot_rows(const V *__restrict__ Q, long long ldq,
     }
 }
 
+// A GMRES Givens step (gmres_givens_kernel's arguments) for the last block of
+// the norm pass to run once h[j+1] is known; j < 0: none.
+struct GivensStep {
+    int j;
+    const double *h;
+    double *R;
+    int ldr;
+    double *cs, *sn, *gam;
+    const double *tol_abs;
+    int32_t *state;
+    double *hist;
+};
+
+__device__ void givens_column(const GivensStep &a);
+
 // MODE 0: x = w (or, with uout, x = qj - (uout - g), stored into w), then
 //         out[k] = sum_t Q[k][t] x[t].
 // MODE 1: x = w - Q^T c, stored into w, then out[k] = Q[k] . x and
@@ -185,7 +200,8 @@ __global__ void __launch_bounds__(kT) cgs2_pass_kernel(const V *__restrict__ Q, 
                                                        double *scratch, double *out, const double *add,
                                                        double *out_plus, const V *__restrict__ qj,
                                                        const double *__restrict__ uout,
-                                                       const double *__restrict__ g, const int32_t *done) {
+                                                       const double *__restrict__ g, const int32_t *done,
+                                                       GivensStep gv) {
     __shared__ double wsum[kWarps][kMaxRows];
     __shared__ V csh[kMaxRows];
     // a device-side stop flag set by an earlier launch: every block returns
@@ -245,6 +261,11 @@ __global__ void __launch_bounds__(kT) cgs2_pass_kernel(const V *__restrict__ Q, 
     if (last_block(S.ticket)) {
         finish_rows(S.part, nrow, out, add, out_plus, MODE == 2);
         if (threadIdx.x == 0) *S.ticket = 0u;
+        if (MODE == 2 && gv.j >= 0) {
+            // the rotation of this column, now that h[j+1] is written
+            __syncthreads();
+            if (threadIdx.x < 32) givens_column(gv);
+        }
     }
 }
 
@@ -253,7 +274,9 @@ __global__ void __launch_bounds__(kT) cgs2_pass_kernel(const V *__restrict__ Q, 
 // done (optional): every launch returns at once while *done != 0.
 template <typename V>
 int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, double *scratch, int64_t scratch_len,
-         const double *uout, const double *g, const int32_t *done, void *stream) {
+         const double *uout, const double *g, const int32_t *done, void *stream,
+         GivensStep gv = GivensStep{-1, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr}) {
+    const GivensStep none{-1, nullptr, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     if (!Q || !w || !h || !scratch || rows < 1 || rows > kMaxRows || n < 1 || ldq < n) return PBTE_ERR_ARG;
     if (scratch_len < PBTE_CGS2_SCRATCH) return PBTE_ERR_ARG;
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
@@ -262,11 +285,11 @@ int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, doub
     const long long nchunk = (n + (long long)kT * kE - 1) / ((long long)kT * kE);
     const int nb = (int)std::min<long long>(nchunk, kMaxBlocks);
     cgs2_pass_kernel<V, 0><<<nb, kT, 0, s>>>(Q, ldq, rows, w, nullptr, n, scratch, S.c1, nullptr, nullptr, qj,
-                                             uout, g, done);
+                                             uout, g, done, none);
     cgs2_pass_kernel<V, 1><<<nb, kT, 0, s>>>(Q, ldq, rows, w, S.c1, n, scratch, S.c2, S.c1, h,   // h = c1 + c2
-                                             nullptr, nullptr, nullptr, done);
+                                             nullptr, nullptr, nullptr, done, none);
     cgs2_pass_kernel<V, 2><<<nb, kT, 0, s>>>(Q, ldq, rows, w, S.c2, n, scratch, h + rows, nullptr, nullptr,
-                                             nullptr, nullptr, nullptr, done);
+                                             nullptr, nullptr, nullptr, done, gv);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
@@ -276,48 +299,50 @@ int cgs2(const V *Q, int64_t ldq, int32_t rows, V *w, int64_t n, double *h, doub
 // R, the residual estimates gam, and the stop state: state[0] = 1 when
 // |gam[j+1]| <= *tol_abs, 2 when h[j+1] == 0 (breakdown), state[1] = columns
 // done, hist[j] = |gam[j+1]|.  One thread; nothing runs once state[0] != 0.
-__global__ void gmres_givens_kernel(int j, const double *h, double *R, int ldr, double *cs, double *sn,
-                                    double *gam, const double *tol_abs, int32_t *state, double *hist) {
+__device__ void givens_column(const GivensStep &a) {
     // the column and the rotations are staged in shared memory by the warp
     // (independent loads), then lane 0 runs the sequential rotations
     __shared__ double col[kMaxRows + 1], c_s[kMaxRows], s_s[kMaxRows];
-    if (*(volatile const int32_t *)state != 0) return;
-    for (int i = threadIdx.x; i <= j + 1; i += blockDim.x) col[i] = h[i];
-    for (int i = threadIdx.x; i < j; i += blockDim.x) {
-        c_s[i] = cs[i];
-        s_s[i] = sn[i];
+    const int j = a.j;
+    if (*(volatile const int32_t *)a.state != 0) return;
+    for (int i = threadIdx.x; i <= j + 1; i += 32) col[i] = a.h[i];
+    for (int i = threadIdx.x; i < j; i += 32) {
+        c_s[i] = a.cs[i];
+        s_s[i] = a.sn[i];
     }
     __syncwarp();
     if (threadIdx.x == 0) {
         const double hn = col[j + 1];
-        double a = col[0];
+        double x = col[0];
         for (int i = 0; i < j; ++i) {
             const double b = col[i + 1];
-            col[i] = c_s[i] * a + s_s[i] * b;
-            a = -s_s[i] * a + c_s[i] * b;
+            col[i] = c_s[i] * x + s_s[i] * b;
+            x = -s_s[i] * x + c_s[i] * b;
         }
-        col[j] = a;
+        col[j] = x;
         const double d = hypot(col[j], col[j + 1]);
-        double c = 1.0, s = 0.0;
+        double c = 1.0, sv = 0.0;
         if (d != 0.0) {
             c = col[j] / d;
-            s = col[j + 1] / d;
+            sv = col[j + 1] / d;
         }
-        cs[j] = c;
-        sn[j] = s;
+        a.cs[j] = c;
+        a.sn[j] = sv;
         col[j] = d;
-        const double g = gam[j];
-        gam[j + 1] = -s * g;
-        gam[j] = c * g;
-        const double res = fabs(-s * g);
-        hist[j] = res;
-        state[1] = j + 1;
-        if (res <= *tol_abs) state[0] = 1;
-        else if (hn == 0.0) state[0] = 2;
+        const double gj = a.gam[j];
+        a.gam[j + 1] = -sv * gj;
+        a.gam[j] = c * gj;
+        const double res = fabs(-sv * gj);
+        a.hist[j] = res;
+        a.state[1] = j + 1;
+        if (res <= *a.tol_abs) a.state[0] = 1;
+        else if (hn == 0.0) a.state[0] = 2;
     }
     __syncwarp();
-    for (int i = threadIdx.x; i <= j; i += blockDim.x) R[(size_t)j * ldr + i] = col[i];
+    for (int i = threadIdx.x; i <= j; i += 32) a.R[(size_t)j * a.ldr + i] = col[i];
 }
+
+__global__ void gmres_givens_kernel(GivensStep a) { givens_column(a); }
 
 // q_{j+1} = w / h[j+1] into row j+1 of the basis, and widened into the
 // operator's FP64 input for the next product; nothing once state[0] != 0.
@@ -346,6 +371,22 @@ int next_basis(int32_t j, const V *w, const double *h, V *Q, int64_t ldq, double
 }
 
 }  // namespace
+
+namespace pbte {
+// pbte_arnoldi_column_f32 then pbte_gmres_givens for column j = rows - 1,
+// the rotation run by the last block of the norm pass (one launch fewer)
+int arnoldi_column_givens_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
+                              float *w, int64_t n, double *h, double *scratch, int64_t scratch_len, double *R,
+                              int32_t ldr, double *cs, double *sn, double *gam, const double *tol_abs,
+                              int32_t *state, double *hist, cudaStream_t s) {
+    const int j = rows - 1;
+    if (!uout || j < 0 || j + 1 >= kMaxRows + 1 || ldr < j + 1 || !h || !R || !cs || !sn || !gam || !tol_abs ||
+        !state || !hist)
+        return PBTE_ERR_ARG;
+    return cgs2<float>(Q, ldq, rows, w, n, h, scratch, scratch_len, uout, g, state, s,
+                       GivensStep{j, h, R, ldr, cs, sn, gam, tol_abs, state, hist});
+}
+}  // namespace pbte
 
 // h[0..rows-1] = c1 + c2 and h[rows] = ||w|| after the two passes; `scratch`
 // holds scratch_len >= PBTE_CGS2_SCRATCH doubles, zero before the first call.
@@ -379,8 +420,8 @@ extern "C" int pbte_gmres_givens(int32_t j, const double *h, double *R, int32_t 
     if (j < 0 || j + 1 >= kMaxRows + 1 || ldr < j + 1 || !h || !R || !cs || !sn || !gam || !tol_abs || !state ||
         !hist)
         return PBTE_ERR_ARG;
-    gmres_givens_kernel<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>(j, h, R, ldr, cs, sn, gam, tol_abs,
-                                                                              state, hist);
+    gmres_givens_kernel<<<1, 32, 0, reinterpret_cast<cudaStream_t>(stream)>>>(
+        GivensStep{j, h, R, ldr, cs, sn, gam, tol_abs, state, hist});
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 

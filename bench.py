@@ -258,12 +258,12 @@ def main():
             ms, rec = timed(solvers, k)
             times.append(ms)
             # per FP32 Arnoldi column: sweep, epilogue (moments, integrals,
-            # wall emission), CGS2 (3), rotation, next basis vector with the
-            # next column's moment sources; one sources launch per inner
-            # cycle's first chunk at least; per FP64 product: sources, sweep,
-            # moments (2), element integrals, wall flux
+            # wall emission), CGS2 (3, the rotation in the last one's tail),
+            # next basis vector with the next column's moment sources; one
+            # sources launch per inner cycle's first chunk at least; per FP64
+            # product: sources, sweep, moments (2), element integrals, wall flux
             d = rec.diagnostics
-            launches += 7 * d["fp32_sweeps"] + d["outer_steps"] + 6 * d["fp64_sweeps"]
+            launches += 6 * d["fp32_sweeps"] + d["outer_steps"] + 6 * d["fp64_sweeps"]
     clocks = clk.summary()
     total = max_over_ranks(float(sum(times)), dist)
     value = replica_throughput(args.steps, total * 1e-3, world)

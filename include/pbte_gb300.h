@@ -267,11 +267,13 @@ int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float 
 
 /* Columns j0..j1-1 of a GMRES restart cycle with the FP32 fixed-point
  * product, issued from native code (one call records a whole chunk of a
- * captured cycle): per column pbte_fixed_point_f32 on the operator input,
- * pbte_arnoldi_column_f32 (rows j+1, done = state), pbte_gmres_givens and
- * pbte_gmres_next_basis_f32, with `state` installed as the context's stop
- * flag for the duration (pbte_set_done_flag), exactly the launches of
- * those calls made one by one -- gmres_full's column loop
+ * captured cycle): per column the work of pbte_fixed_point_f32 on the
+ * operator input, pbte_arnoldi_column_f32 (rows j+1, done = state),
+ * pbte_gmres_givens and pbte_gmres_next_basis_f32 with their arithmetic,
+ * with `state` installed as the context's stop flag for the duration
+ * (pbte_set_done_flag); the rotation runs in the last block of the CGS2
+ * norm pass -- the same numbers as those calls made one by one, in fewer
+ * launches.  gmres_full's column loop
  * (pybte/krylov.py:190-240) for the mixed solver's inner GMRES.  The
  * operator views (ts/qxs/qys/flux_wall_in of the input uin, the outputs of
  * uout) are those pbte_fixed_point_f32 takes; flux_wall_in/out may be NULL
