@@ -290,8 +290,10 @@ def test_device_gmres_cycles_match_host_rotations(cuda, graphs):
 @pytest.mark.parametrize("graphs", [True, False])
 def test_native_gmres_columns_issue_the_same_launches(cuda, monkeypatch, graphs):
     """The mixed solve's inner cycles with each chunk issued by one native
-    call (pbte_gmres_columns_f32) against the same launches issued column by
-    column from Python, captured or direct: bit for bit the same solve."""
+    call (pbte_gmres_columns_f32: the rotation in the CGS2 norm pass, the
+    next sources with the basis update) against the separate calls issued
+    column by column from Python, captured or direct: the same arithmetic,
+    bit for bit the same solve."""
     from pbte_gb300.krylov import ArnoldiGraphs
     base = dict(deg=2, npole=4, nazim=8, tau_r=0.2, tau_n=0.02, method="krylov", precision="mixed",
                 krylov_restart=12)
