@@ -133,7 +133,90 @@ bool reference_order(const pbte_case_desc *d, double cx, double cy, std::vector<
     return true;
 }
 
+// Direction classes: the sign pattern of c.n over the interior and periodic
+// faces (each face seen from its first side), hashed (FNV-1a) and then
+// compared in full against the class representative; classes are numbered
+// by first appearance.  A face's sign depends only on the exact bits of its
+// normal, so the pattern is taken over the distinct normals (a handful on
+// structured meshes, at most one per face): the same classes as face by face.
+void direction_classes(const pbte_case_desc *d, std::vector<int32_t> &dir_class, std::vector<int> &class_rep) {
+    std::vector<double> unx, uny;
+    {
+        std::unordered_map<uint64_t, std::vector<int>> seen;   // hash of the bits -> distinct ids
+        auto bits = [](double v) { uint64_t u; std::memcpy(&u, &v, sizeof u); return u; };
+        for (int f = 0; f < d->n_faces; ++f) {
+            const int bc = d->face_bc[f];
+            if (!(bc < 0 || d->bc_type[bc] == 3)) continue;
+            const int t = d->face_tri[f * 2 + 0] >= 0 ? d->face_tri[f * 2 + 0] : d->face_tri[f * 2 + 1];
+            const int l = d->face_tri[f * 2 + 0] >= 0 ? d->face_lfc[f * 2 + 0] : d->face_lfc[f * 2 + 1];
+            const double nx = d->nx[t * 3 + l], ny = d->ny[t * 3 + l];
+            const uint64_t h = bits(nx) * 0x9E3779B97F4A7C15ull ^ bits(ny);
+            auto &ids = seen[h];
+            bool dup = false;
+            for (int q : ids)
+                if (bits(unx[q]) == bits(nx) && bits(uny[q]) == bits(ny)) { dup = true; break; }
+            if (dup) continue;
+            ids.push_back((int)unx.size());
+            unx.push_back(nx);
+            uny.push_back(ny);
+        }
+    }
+    auto pattern = [&](int dir, std::vector<int8_t> &p) {
+        p.resize(unx.size());
+        for (size_t k = 0; k < unx.size(); ++k) p[k] = sgn(d->cxv[dir] * unx[k] + d->cyv[dir] * uny[k]);
+    };
+    std::unordered_multimap<uint64_t, int> by_hash;  // hash -> class id
+    class_rep.clear();
+    dir_class.assign(d->ndir, 0);
+    std::vector<int8_t> pat, pat2;
+    for (int dir = 0; dir < d->ndir; ++dir) {
+        pattern(dir, pat);
+        uint64_t h = 1469598103934665603ull;
+        for (int8_t v : pat) { h ^= (uint8_t)v; h *= 1099511628211ull; }
+        int found = -1;
+        auto range = by_hash.equal_range(h);
+        for (auto it = range.first; it != range.second && found < 0; ++it) {
+            pattern(class_rep[it->second], pat2);
+            if (pat2 == pat) found = it->second;
+        }
+        if (found < 0) {
+            found = (int)class_rep.size();
+            class_rep.push_back(dir);
+            by_hash.emplace(h, found);
+        }
+        dir_class[dir] = found;
+    }
+}
+
+// face arrays a case description must hold for the host-side scheduling
+bool desc_faces_valid(const pbte_case_desc *d) {
+    if (!d->face_bc || !d->face_tri || !d->face_lfc || !d->nx || !d->ny || !d->cxv || !d->cyv ||
+        (d->nbc > 0 && !d->bc_type))
+        return false;
+    for (int f = 0; f < d->n_faces; ++f) {
+        const int bc = d->face_bc[f];
+        if (bc >= d->nbc) return false;
+        for (int side = 0; side < 2; ++side) {
+            const int t = d->face_tri[f * 2 + side], l = d->face_lfc[f * 2 + side];
+            if (t >= d->n_tris || (t >= 0 && (l < 0 || l > 2))) return false;
+        }
+        if (d->face_tri[f * 2] < 0 && d->face_tri[f * 2 + 1] < 0) return false;
+    }
+    return true;
+}
+
 }  // namespace
+
+extern "C" int pbte_direction_classes(const pbte_case_desc *d, int32_t *dir_class, int32_t *n_classes) {
+    if (!d || !dir_class || !n_classes || d->n_tris <= 0 || d->ndir <= 0 || d->n_faces <= 0) return PBTE_ERR_ARG;
+    if (!desc_faces_valid(d)) return PBTE_ERR_ARG;
+    std::vector<int32_t> cls;
+    std::vector<int> rep;
+    direction_classes(d, cls, rep);
+    std::memcpy(dir_class, cls.data(), sizeof(int32_t) * cls.size());
+    *n_classes = (int32_t)rep.size();
+    return PBTE_OK;
+}
 
 extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
     if (!c) return PBTE_OK;
@@ -278,56 +361,9 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     }
 
     // ---- direction classes and wavefront levels -------------------------
-    // sign pattern of c.n over the interior and periodic faces, hashed
-    // (FNV-1a) and then compared in full against the class representative.
-    // A face's sign depends only on the exact bits of its normal, so the
-    // pattern is taken over the distinct normals (a handful on structured
-    // meshes, at most one per face): the same classes as face by face.
-    std::vector<double> unx, uny;
-    {
-        std::unordered_map<uint64_t, std::vector<int>> seen;   // hash of the bits -> distinct ids
-        auto bits = [](double v) { uint64_t u; std::memcpy(&u, &v, sizeof u); return u; };
-        for (int f = 0; f < d->n_faces; ++f) {
-            if (!(d->face_bc[f] < 0 || pslot[f] >= 0)) continue;
-            const int t = d->face_tri[f * 2 + 0] >= 0 ? d->face_tri[f * 2 + 0] : d->face_tri[f * 2 + 1];
-            const int l = d->face_tri[f * 2 + 0] >= 0 ? d->face_lfc[f * 2 + 0] : d->face_lfc[f * 2 + 1];
-            const double nx = d->nx[t * 3 + l], ny = d->ny[t * 3 + l];
-            const uint64_t h = bits(nx) * 0x9E3779B97F4A7C15ull ^ bits(ny);
-            auto &ids = seen[h];
-            bool dup = false;
-            for (int q : ids)
-                if (bits(unx[q]) == bits(nx) && bits(uny[q]) == bits(ny)) { dup = true; break; }
-            if (dup) continue;
-            ids.push_back((int)unx.size());
-            unx.push_back(nx);
-            uny.push_back(ny);
-        }
-    }
-    auto pattern = [&](int dir, std::vector<int8_t> &p) {
-        p.resize(unx.size());
-        for (size_t k = 0; k < unx.size(); ++k) p[k] = sgn(d->cxv[dir] * unx[k] + d->cyv[dir] * uny[k]);
-    };
-    std::unordered_multimap<uint64_t, int> by_hash;  // hash -> class id
     std::vector<int> class_rep;
-    std::vector<int32_t> dir_class(ndir);
-    std::vector<int8_t> pat, pat2;
-    for (int dir = 0; dir < ndir; ++dir) {
-        pattern(dir, pat);
-        uint64_t h = 1469598103934665603ull;
-        for (int8_t v : pat) { h ^= (uint8_t)v; h *= 1099511628211ull; }
-        int found = -1;
-        auto range = by_hash.equal_range(h);
-        for (auto it = range.first; it != range.second && found < 0; ++it) {
-            pattern(class_rep[it->second], pat2);
-            if (pat2 == pat) found = it->second;
-        }
-        if (found < 0) {
-            found = (int)class_rep.size();
-            class_rep.push_back(dir);
-            by_hash.emplace(h, found);
-        }
-        dir_class[dir] = found;
-    }
+    std::vector<int32_t> dir_class;
+    direction_classes(d, dir_class, class_rep);
     c->nclass = (int)class_rep.size();
     std::vector<int32_t> lvl_cells((size_t)c->nclass * nt), lvl_ptr, class_off(c->nclass),
         class_nlev(c->nclass);

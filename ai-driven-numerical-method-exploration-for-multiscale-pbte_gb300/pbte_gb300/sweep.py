@@ -76,6 +76,54 @@ class Moments:
                 ("ts", "qxs", "qys", "temp", "qx", "qy")}
 
 
+def case_desc(disc: Discretisation):
+    """The ``pbte_case_desc`` of a case and the host arrays it points into
+    (keep them alive while the descriptor is used)."""
+    c = disc.case
+    it, m, bd = disc.integrals, disc.mesh, disc.bcdata
+    cx, cy, dw = disc.vel.flat()
+    a = dict(
+        cxv=np.ascontiguousarray(cx), cyv=np.ascontiguousarray(cy), domega=np.ascontiguousarray(dw),
+        ref_mass=np.ascontiguousarray(it.ref_mass), ref_dx=np.ascontiguousarray(it.ref_dx),
+        ref_dy=np.ascontiguousarray(it.ref_dy), ref_edge=np.ascontiguousarray(it.ref_edge),
+        edge_dofs=np.ascontiguousarray(disc.edge_dofs, dtype=np.int32),
+        area2=np.ascontiguousarray(it.area2), dxi=np.ascontiguousarray(it.dxi),
+        deta=np.ascontiguousarray(it.deta), edge_scale=np.ascontiguousarray(it.edge_scale),
+        nx=np.ascontiguousarray(m.tri_normal[:, :, 0]), ny=np.ascontiguousarray(m.tri_normal[:, :, 1]),
+        tri_faces=np.ascontiguousarray(m.tri_faces, dtype=np.int32),
+        upwind_tri=np.ascontiguousarray(disc.upwind_tri, dtype=np.int32),
+        edge_map=np.ascontiguousarray(disc.edge_map, dtype=np.int32),
+        face_bc=np.ascontiguousarray(m.face_bc, dtype=np.int32),
+        face_tri=np.ascontiguousarray(m.face_tri, dtype=np.int32),
+        face_lfc=np.ascontiguousarray(m.face_lfc, dtype=np.int32),
+        bc_type=np.ascontiguousarray(bd.bc_type, dtype=np.int32),
+        bc_temp=np.ascontiguousarray(bd.bc_temp), int_tri=np.ascontiguousarray(it.int_tri))
+
+    def P(x):
+        return x.ctypes.data_as(ctypes.POINTER(ctypes.c_int32 if x.dtype == np.int32 else ctypes.c_double))
+
+    desc = _lib.CaseDesc(m.n_tris, m.n_faces, disc.ndof, c.ndof_fc, cx.size,
+                         int(bd.bc_type.size), c.flow.cv, c.flow.vg, c.flow.tau_r, c.flow.tau_n,
+                         c.tau_c, *(P(a[k]) for k in (
+                             "cxv", "cyv", "domega", "ref_mass", "ref_dx", "ref_dy", "ref_edge",
+                             "edge_dofs", "area2", "dxi", "deta", "edge_scale", "nx", "ny",
+                             "tri_faces", "upwind_tri", "edge_map", "face_bc", "face_tri",
+                             "face_lfc", "bc_type", "bc_temp", "int_tri")))
+    return desc, a
+
+
+def direction_classes(disc: Discretisation) -> np.ndarray:
+    """Each ordinate's direction class, as the context schedules them
+    (``pbte_direction_classes``; host only)."""
+    desc, keep = case_desc(disc)
+    out = np.zeros(disc.vel.flat()[0].size, dtype=np.int32)
+    n = ctypes.c_int32()
+    _lib.check(_lib.lib().pbte_direction_classes(ctypes.byref(desc), out.ctypes.data, ctypes.byref(n)),
+               "pbte_direction_classes")
+    del keep
+    return out
+
+
 class SweepContext:
     """The compact operators on the device plus the sweep schedule."""
 
@@ -106,34 +154,7 @@ class SweepContext:
         self.sweep_count = 0
         self.use_pbuf = False
 
-        a = dict(
-            cxv=self.cxv, cyv=self.cyv, domega=self.domega,
-            ref_mass=np.ascontiguousarray(it.ref_mass), ref_dx=np.ascontiguousarray(it.ref_dx),
-            ref_dy=np.ascontiguousarray(it.ref_dy), ref_edge=np.ascontiguousarray(it.ref_edge),
-            edge_dofs=np.ascontiguousarray(disc.edge_dofs, dtype=np.int32),
-            area2=np.ascontiguousarray(it.area2), dxi=np.ascontiguousarray(it.dxi),
-            deta=np.ascontiguousarray(it.deta), edge_scale=np.ascontiguousarray(it.edge_scale),
-            nx=np.ascontiguousarray(m.tri_normal[:, :, 0]), ny=np.ascontiguousarray(m.tri_normal[:, :, 1]),
-            tri_faces=np.ascontiguousarray(m.tri_faces, dtype=np.int32),
-            upwind_tri=np.ascontiguousarray(disc.upwind_tri, dtype=np.int32),
-            edge_map=np.ascontiguousarray(disc.edge_map, dtype=np.int32),
-            face_bc=np.ascontiguousarray(m.face_bc, dtype=np.int32),
-            face_tri=np.ascontiguousarray(m.face_tri, dtype=np.int32),
-            face_lfc=np.ascontiguousarray(m.face_lfc, dtype=np.int32),
-            bc_type=np.ascontiguousarray(bd.bc_type, dtype=np.int32),
-            bc_temp=np.ascontiguousarray(bd.bc_temp), int_tri=np.ascontiguousarray(it.int_tri))
-        self._host = a
-
-        def P(x):
-            return x.ctypes.data_as(ctypes.POINTER(ctypes.c_int32 if x.dtype == np.int32 else ctypes.c_double))
-
-        desc = _lib.CaseDesc(self.n_tris, self.n_faces, self.ndof, c.ndof_fc, self.ndir,
-                             int(bd.bc_type.size), c.flow.cv, c.flow.vg, c.flow.tau_r, c.flow.tau_n,
-                             c.tau_c, *(P(a[k]) for k in (
-                                 "cxv", "cyv", "domega", "ref_mass", "ref_dx", "ref_dy", "ref_edge",
-                                 "edge_dofs", "area2", "dxi", "deta", "edge_scale", "nx", "ny",
-                                 "tri_faces", "upwind_tri", "edge_map", "face_bc", "face_tri",
-                                 "face_lfc", "bc_type", "bc_temp", "int_tri")))
+        desc, self._host = case_desc(disc)
         handle = ctypes.c_void_p()
         with device_lock, torch.cuda.device(self.device):
             empty_graveyard()

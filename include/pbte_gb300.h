@@ -84,6 +84,15 @@ typedef struct {
 int pbte_ctx_create(const pbte_case_desc *desc, int precompute, pbte_ctx **out);
 int pbte_ctx_destroy(pbte_ctx *ctx);
 
+/* The direction classes pbte_ctx_create schedules with, host only (no GPU
+ * needed): dir_class[ndir] receives each ordinate's class -- ordinates whose
+ * c.n has the same sign on every interior and periodic face (seen from the
+ * face's first side) share one level schedule -- numbered by first
+ * appearance, *n_classes their count.  Reads the face arrays, normals and
+ * ordinates of desc.  No reference counterpart (pybte orders each direction
+ * on its own, pybte/ordering.py:61-140). */
+int pbte_direction_classes(const pbte_case_desc *desc, int32_t *dir_class, int32_t *n_classes);
+
 /* Sweep kernel selection: 0 automatic (ring-pipelined when the level ring
  * fits in shared memory, else level-serial), 1 level-serial, 2 ring only
  * (PBTE_ERR_UNSUPPORTED from the sweep if it does not fit).  No reference

@@ -1,0 +1,53 @@
+"""Direction classes as the context schedules them (pbte_direction_classes,
+host only) against the face-by-face sign patterns formed here with numpy, on
+meshes whose face normals take a few values (structured squares) and many
+(graded squares, a periodic channel)."""
+import numpy as np
+import pytest
+
+from cases import periodic_case, small_case
+from pbte_gb300 import _lib
+from pbte_gb300.discretisation import Discretisation
+from pbte_gb300.sweep import direction_classes
+
+
+def numpy_classes(disc):
+    """Sign of c.n on every interior and periodic face (from the face's first
+    side), grouped by first appearance."""
+    m, bd = disc.mesh, disc.bcdata
+    cx, cy, _ = disc.vel.flat()
+    fb = np.asarray(m.face_bc)
+    bc_type = np.asarray(bd.bc_type)
+    include = (fb < 0) | ((fb >= 0) & (bc_type[np.maximum(fb, 0)] == 3))
+    ft, fl = np.asarray(m.face_tri), np.asarray(m.face_lfc)
+    side = np.where(ft[:, 0] >= 0, 0, 1)
+    rows = np.arange(ft.shape[0])
+    t, lf = ft[rows, side][include], fl[rows, side][include]
+    nx, ny = m.tri_normal[t, lf, 0], m.tri_normal[t, lf, 1]
+    pat = np.sign(np.outer(cx, nx) + np.outer(cy, ny)).astype(np.int8)
+    seen, out = {}, np.empty(cx.size, dtype=np.int32)
+    for d in range(cx.size):
+        out[d] = seen.setdefault(pat[d].tobytes(), len(seen))
+    return out
+
+
+@pytest.mark.parametrize("mesh", ["cavity:12", "cavity:5:smootherstep", "cavity:10:smootherstep", "channel:9"])
+@pytest.mark.parametrize("ang", [(4, 8), (8, 32)])
+def test_direction_classes_match_face_by_face_patterns(mesh, ang):
+    try:
+        _lib.lib()
+    except RuntimeError as e:
+        pytest.skip(f"library unavailable: {e}")
+    disc = Discretisation.build(small_case(1, *ang, 1.0, 0.1, mesh=mesh))
+    got = direction_classes(disc)
+    assert np.array_equal(got, numpy_classes(disc))
+    assert got.max() + 1 == len(set(got.tolist()))
+
+
+def test_direction_classes_with_periodic_faces():
+    try:
+        _lib.lib()
+    except RuntimeError as e:
+        pytest.skip(f"library unavailable: {e}")
+    disc = Discretisation.build(periodic_case(1, 8, 32, 1.0, 0.1, mesh="channel:12"))
+    assert np.array_equal(direction_classes(disc), numpy_classes(disc))
