@@ -218,6 +218,47 @@ extern "C" int pbte_direction_classes(const pbte_case_desc *d, int32_t *dir_clas
     return PBTE_OK;
 }
 
+extern "C" int pbte_direction_levels(const pbte_case_desc *d, int32_t dir, int32_t *level, int32_t *n_levels) {
+    if (!d || !level || !n_levels || d->n_tris <= 0 || d->n_faces <= 0 || dir < 0 || dir >= d->ndir)
+        return PBTE_ERR_ARG;
+    if (!desc_faces_valid(d) || !d->tri_faces || !d->upwind_tri) return PBTE_ERR_ARG;
+    const int nt = d->n_tris;
+    for (int i = 0; i < nt * 3; ++i) {
+        const int fc = d->tri_faces[i], nb = d->upwind_tri[i];
+        if (fc < 0 || fc >= d->n_faces || nb >= nt) return PBTE_ERR_ARG;
+    }
+    const double cx = d->cxv[dir], cy = d->cyv[dir];
+    std::vector<uint8_t> fresh;
+    bool periodic = false;
+    for (int f = 0; f < d->n_faces && !periodic; ++f) periodic = d->face_bc[f] >= 0 && d->bc_type[d->face_bc[f]] == 3;
+    if (periodic) {
+        // the rule pbte_ctx_create applies per direction class
+        std::vector<int32_t> rpos;
+        if (!reference_order(d, cx, cy, rpos)) return PBTE_ERR_CYCLE;
+        fresh.assign(nt, 0);
+        for (int i = 0; i < nt; ++i)
+            for (int il = 0; il < 3; ++il) {
+                const int fc = d->tri_faces[i * 3 + il];
+                const int bc = d->face_bc[fc];
+                if (bc < 0 || d->bc_type[bc] != 3) continue;
+                const int p = d->upwind_tri[i * 3 + il];
+                if (p < 0) continue;
+                const double s = cx * d->nx[i * 3 + il] + cy * d->ny[i * 3 + il];
+                if (s < 0.0 && rpos[p] < rpos[i]) fresh[i] |= (uint8_t)(1u << il);
+            }
+    }
+    std::vector<int32_t> lv, indeg, queue, succ_ptr, succ;
+    if (!levels_for(d, cx, cy, periodic ? fresh.data() : nullptr, lv, indeg, queue, succ_ptr, succ))
+        return PBTE_ERR_CYCLE;
+    int nlev = 0;
+    for (int i = 0; i < nt; ++i) {
+        level[i] = lv[i];
+        nlev = std::max(nlev, lv[i] + 1);
+    }
+    *n_levels = nlev;
+    return PBTE_OK;
+}
+
 extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
     if (!c) return PBTE_OK;
     void *ptrs[] = {c->d_cx, c->d_cy, c->d_w, c->d_cells64, c->d_cells32, c->d_ref64, c->d_ref32,

@@ -107,6 +107,8 @@ _SIGS = {
     "pbte_ctx_create": ([ctypes.POINTER(CaseDesc), ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
     "pbte_ctx_destroy": ([_vp], ctypes.c_int),
     "pbte_direction_classes": ([ctypes.POINTER(CaseDesc), _vp, ctypes.POINTER(ctypes.c_int32)], ctypes.c_int),
+    "pbte_direction_levels": ([ctypes.POINTER(CaseDesc), ctypes.c_int32, _vp, ctypes.POINTER(ctypes.c_int32)],
+                              ctypes.c_int),
     "pbte_ctx_info": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64),
                        ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_sweep": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int, _vp], ctypes.c_int),

@@ -124,6 +124,18 @@ def direction_classes(disc: Discretisation) -> np.ndarray:
     return out
 
 
+def direction_levels(disc: Discretisation, d: int) -> np.ndarray:
+    """The wavefront level of every element for ordinate ``d``, as the
+    context schedules it (``pbte_direction_levels``; host only)."""
+    desc, keep = case_desc(disc)
+    out = np.zeros(disc.mesh.n_tris, dtype=np.int32)
+    n = ctypes.c_int32()
+    _lib.check(_lib.lib().pbte_direction_levels(ctypes.byref(desc), int(d), out.ctypes.data, ctypes.byref(n)),
+               "pbte_direction_levels")
+    del keep
+    return out
+
+
 class SweepContext:
     """The compact operators on the device plus the sweep schedule."""
 

@@ -93,6 +93,13 @@ int pbte_ctx_destroy(pbte_ctx *ctx);
  * on its own, pybte/ordering.py:61-140). */
 int pbte_direction_classes(const pbte_case_desc *desc, int32_t *dir_class, int32_t *n_classes);
 
+/* The wavefront level of every element for ordinate `dir`, host only: level
+ * = 1 + the deepest element it waits for in the sweep (an interior upwind
+ * neighbour, or a periodic partner that comes earlier in pybte's TRI_ORDER,
+ * pybte/ordering.py:61-140), as pbte_ctx_create schedules the ordinate's
+ * class; level[n_tris], *n_levels the count.  PBTE_ERR_CYCLE on a cycle. */
+int pbte_direction_levels(const pbte_case_desc *desc, int32_t dir, int32_t *level, int32_t *n_levels);
+
 /* Sweep kernel selection: 0 automatic (ring-pipelined when the level ring
  * fits in shared memory, else level-serial), 1 level-serial, 2 ring only
  * (PBTE_ERR_UNSUPPORTED from the sweep if it does not fit).  No reference

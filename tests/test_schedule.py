@@ -51,3 +51,44 @@ def test_direction_classes_with_periodic_faces():
         pytest.skip(f"library unavailable: {e}")
     disc = Discretisation.build(periodic_case(1, 8, 32, 1.0, 0.1, mesh="channel:12"))
     assert np.array_equal(direction_classes(disc), numpy_classes(disc))
+
+
+def numpy_levels(disc, d, order):
+    """Wavefront levels restated: walking pybte's TRI_ORDER for ordinate d,
+    an element sits one level past the deepest element it waits for: an
+    interior upwind neighbour, or a periodic partner earlier in that order."""
+    m, bd = disc.mesh, disc.bcdata
+    cx, cy, _ = disc.vel.flat()
+    up = np.asarray(disc.upwind_tri)
+    fb = np.asarray(m.face_bc)
+    bc_type = np.asarray(bd.bc_type)
+    pos = np.empty(m.n_tris, dtype=np.int64)
+    pos[order] = np.arange(m.n_tris)
+    s = cx[d] * m.tri_normal[:, :, 0] + cy[d] * m.tri_normal[:, :, 1]
+    level = np.zeros(m.n_tris, dtype=np.int64)
+    for i in order:
+        for il in range(3):
+            nb, f = up[i, il], m.tri_faces[i, il]
+            if nb < 0 or not s[i, il] < 0.0:
+                continue
+            if fb[f] >= 0 and not (bc_type[fb[f]] == 3 and pos[nb] < pos[i]):
+                continue
+            level[i] = max(level[i], level[nb] + 1)
+    return level
+
+
+@pytest.mark.parametrize("kind", ["cavity:12", "cavity:10:smootherstep", "periodic"])
+def test_direction_levels_match_order_walk(kind):
+    try:
+        _lib.lib()
+    except RuntimeError as e:
+        pytest.skip(f"library unavailable: {e}")
+    from oracle.oracle import reference_order
+    from pbte_gb300.sweep import direction_levels
+    case = periodic_case(1, 4, 8, 1.0, 0.1, mesh="channel:12") if kind == "periodic" else \
+        small_case(1, 4, 8, 1.0, 0.1, mesh=kind)
+    disc = Discretisation.build(case)
+    order, _ = reference_order(disc)
+    for d in range(order.shape[0]):
+        got = direction_levels(disc, d)
+        assert np.array_equal(got, numpy_levels(disc, d, order[d])), d
