@@ -525,7 +525,15 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
     {
         std::atomic<int> next{0};
         auto worker = [&]() {
-            for (int k = next++; k < c->nclass; k = next++) build_class(k, cls_out[k]);
+            for (int k = next++; k < c->nclass; k = next++) {
+                try {
+                    build_class(k, cls_out[k]);
+                } catch (...) {
+                    // host allocation failed: reported as a status, no
+                    // exception leaves the worker (or the C ABI)
+                    cls_out[k].status = PBTE_ERR_NOMEM;
+                }
+            }
         };
         const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
         const int nth = (int)std::min<unsigned>({hw, 16u, (unsigned)c->nclass});
