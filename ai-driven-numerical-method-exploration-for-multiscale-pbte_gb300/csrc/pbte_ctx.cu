@@ -207,7 +207,7 @@ bool desc_faces_valid(const pbte_case_desc *d) {
 
 }  // namespace
 
-extern "C" int pbte_direction_classes(const pbte_case_desc *d, int32_t *dir_class, int32_t *n_classes) {
+static int direction_classes_impl(const pbte_case_desc *d, int32_t *dir_class, int32_t *n_classes) {
     if (!d || !dir_class || !n_classes || d->n_tris <= 0 || d->ndir <= 0 || d->n_faces <= 0) return PBTE_ERR_ARG;
     if (!desc_faces_valid(d)) return PBTE_ERR_ARG;
     std::vector<int32_t> cls;
@@ -218,7 +218,7 @@ extern "C" int pbte_direction_classes(const pbte_case_desc *d, int32_t *dir_clas
     return PBTE_OK;
 }
 
-extern "C" int pbte_direction_levels(const pbte_case_desc *d, int32_t dir, int32_t *level, int32_t *n_levels) {
+static int direction_levels_impl(const pbte_case_desc *d, int32_t dir, int32_t *level, int32_t *n_levels) {
     if (!d || !level || !n_levels || d->n_tris <= 0 || d->n_faces <= 0 || dir < 0 || dir >= d->ndir)
         return PBTE_ERR_ARG;
     if (!desc_faces_valid(d) || !d->tri_faces || !d->upwind_tri) return PBTE_ERR_ARG;
@@ -259,6 +259,22 @@ extern "C" int pbte_direction_levels(const pbte_case_desc *d, int32_t dir, int32
     return PBTE_OK;
 }
 
+extern "C" int pbte_direction_classes(const pbte_case_desc *d, int32_t *dir_class, int32_t *n_classes) {
+    try {
+        return direction_classes_impl(d, dir_class, n_classes);
+    } catch (...) {
+        return PBTE_ERR_NOMEM;
+    }
+}
+
+extern "C" int pbte_direction_levels(const pbte_case_desc *d, int32_t dir, int32_t *level, int32_t *n_levels) {
+    try {
+        return direction_levels_impl(d, dir, level, n_levels);
+    } catch (...) {
+        return PBTE_ERR_NOMEM;
+    }
+}
+
 extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
     if (!c) return PBTE_OK;
     void *ptrs[] = {c->d_cx, c->d_cy, c->d_w, c->d_cells64, c->d_cells32, c->d_ref64, c->d_ref32,
@@ -275,7 +291,7 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
     return PBTE_OK;
 }
 
-extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx **out) {
+static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **out) {
     if (!d || !out) return PBTE_ERR_ARG;
     *out = nullptr;
     const int nt = d->n_tris, nd = d->ndof, nf = d->ndof_fc, ndir = d->ndir;
@@ -640,6 +656,16 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
 #undef TRY
     *out = c;
     return PBTE_OK;
+}
+
+// No C++ exception leaves the C ABI: a failed host allocation is a status.
+extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx **out) {
+    try {
+        return ctx_create_impl(d, precompute, out);
+    } catch (...) {
+        if (out) *out = nullptr;
+        return PBTE_ERR_NOMEM;
+    }
 }
 
 extern "C" int pbte_ctx_info(const pbte_ctx *c, int64_t *nlev, int64_t *ncls, int64_t *bytes) {
