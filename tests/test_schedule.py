@@ -92,3 +92,28 @@ def test_direction_levels_match_order_walk(kind):
     for d in range(order.shape[0]):
         got = direction_levels(disc, d)
         assert np.array_equal(got, numpy_levels(disc, d, order[d])), d
+
+
+def test_host_schedule_entries_reject_bad_arguments():
+    import ctypes
+
+    try:
+        L = _lib.lib()
+    except RuntimeError as e:
+        pytest.skip(f"library unavailable: {e}")
+    from pbte_gb300.sweep import case_desc
+    disc = Discretisation.build(small_case(1, 4, 8, 1.0, 0.1, mesh="cavity:4"))
+    desc, keep = case_desc(disc)
+    n = ctypes.c_int32()
+    cls = np.zeros(disc.vel.flat()[0].size, dtype=np.int32)
+    lev = np.zeros(disc.mesh.n_tris, dtype=np.int32)
+    assert L.pbte_direction_classes(None, cls.ctypes.data, ctypes.byref(n)) == -1
+    assert L.pbte_direction_classes(ctypes.byref(desc), None, ctypes.byref(n)) == -1
+    assert L.pbte_direction_levels(ctypes.byref(desc), -1, lev.ctypes.data, ctypes.byref(n)) == -1
+    assert L.pbte_direction_levels(ctypes.byref(desc), cls.size, lev.ctypes.data, ctypes.byref(n)) == -1
+    assert L.pbte_direction_levels(ctypes.byref(desc), 0, lev.ctypes.data, ctypes.byref(n)) == 0
+    assert n.value == lev.max() + 1
+    bad = np.array(keep["face_bc"])
+    bad[0] = 1000                                  # a boundary condition index past nbc
+    desc.face_bc = bad.ctypes.data_as(ctypes.POINTER(ctypes.c_int32))
+    assert L.pbte_direction_classes(ctypes.byref(desc), cls.ctypes.data, ctypes.byref(n)) == -1
