@@ -261,7 +261,10 @@ def main():
             # wall emission), CGS2 (3, the rotation in the last one's tail),
             # next basis vector with the next column's moment sources; one
             # sources launch per inner cycle's first chunk at least; per FP64
-            # product: sources, sweep, moments (2), element integrals, wall flux
+            # product: sources, sweep, moments (2), element integrals, wall flux.
+            # Not counted: the launches of a ten-column chunk's columns after
+            # the cycle's stop, which return at their first instruction
+            # (a lower bound, then)
             d = rec.diagnostics
             launches += 6 * d["fp32_sweeps"] + d["outer_steps"] + 6 * d["fp64_sweeps"]
     clocks = clk.summary()
