@@ -7,6 +7,7 @@ task (``tasks/t01-square/reference/*.npz``).  Needs the reference checkout,
 so it runs only where that is mounted:
 
     PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
+    (sections alone: --config-only, --precond-only, --periodic-only, --field-only)
 
 The fixtures are plain arrays; nothing at test time reads the reference.
 """
@@ -341,9 +342,72 @@ def krylov_precond(ref: Path) -> dict:
     return meta
 
 
+def config_errors(ref: Path) -> None:
+    """pybte's ``Case.from_dict`` on invalid and coerced case dictionaries:
+    the exception type each raises (a boundary's type is checked when its
+    code is read) and, where it loads, the coerced values; written to
+    config_errors.json.  ``from_dict`` reads no mesh, so no file is needed."""
+    sys.path[:0] = [str(ref / "solver-python")]
+    import copy
+
+    from pybte import Case
+
+    walls = [{"name": "SWall", "phyid": 11, "type": "nonthermalising", "temp": 0.0},
+             {"name": "NWall", "phyid": 12, "type": "thermalising", "temp": 1.0},
+             {"name": "EWall", "phyid": 13, "type": "thermalising", "temp": -0.5},
+             {"name": "WWall", "phyid": 14, "type": "thermalising", "temp": 0.5}]
+    base = {"iteration": {"tol": 1e-8, "tmax": 100}, "scheme": {"accflag": 0},
+            "velmesh": {"npole": 4, "nazim": 8}, "dg": {"deg": 2},
+            "flow": {"cv": 1.0, "vg": 1.0, "tau_r": 1.0, "tau_n": 0.1, "tau_thr": 1.0},
+            "mesh": {"file": "A1_Nx11_Ny11.msh"}, "boundaries": walls}
+    variants = [
+        ("valid", {}),
+        ("tol as a string", {"iteration": {"tol": "1.0e-8", "tmax": "100"}}),
+        ("odd nazim", {"velmesh": {"npole": 4, "nazim": 7}}),
+        ("kernel upper case", {"performance": {"kernel": "NUMPY"}}),
+        ("boundary type upper case", {"boundaries": [dict(walls[0], type="Thermalising")] + walls[1:]}),
+        ("scheme.method", {"scheme": {"method": "multigrid"}}),
+        ("scheme.krylov_max_bytes", {"scheme": {"krylov_max_bytes": 0}}),
+        ("scheme.krylov_max_rounds", {"scheme": {"krylov_max_rounds": 0}}),
+        ("scheme.defect_every", {"scheme": {"defect_every": -1}}),
+        ("scheme.defect_anderson", {"scheme": {"defect_anderson": -2}}),
+        ("scheme.defect_omega", {"scheme": {"defect_omega": 1.5}}),
+        ("scheme.on_cycle", {"scheme": {"on_cycle": "ignore"}}),
+        ("scheme.acc_variant", {"scheme": {"acc_variant": "C"}}),
+        ("scheme.stabilisation", {"scheme": {"stabilisation": [1.0, 1.0]}}),
+        ("flow.tau_r", {"flow": {"cv": 1.0, "vg": 1.0, "tau_r": 0.0, "tau_n": 0.1}}),
+        ("flow.tau_n", {"flow": {"cv": 1.0, "vg": 1.0, "tau_r": 1.0, "tau_n": -0.1}}),
+        ("flow.vg", {"flow": {"cv": 1.0, "vg": 0.0, "tau_r": 1.0, "tau_n": 0.1}}),
+        ("velmesh.nazim", {"velmesh": {"npole": 4, "nazim": 1}}),
+        ("dg.deg", {"dg": {"deg": 5}}),
+        ("performance.kernel", {"performance": {"kernel": "opencl"}}),
+        ("performance.threads", {"performance": {"threads": -1}}),
+        ("boundary type", {"boundaries": [dict(walls[0], type="mirror")] + walls[1:]}),
+        ("unknown key", {"flow": {"cv": 1.0, "vg": 1.0, "tau_r": 1.0, "tau_n": 0.1, "viscosity": 1.0}}),
+        ("unknown boundary key", {"boundaries": [dict(walls[0], colour="red")] + walls[1:]}),
+    ]
+    out = []
+    for label, mod in variants:
+        d = copy.deepcopy(base)
+        d.update(copy.deepcopy(mod))
+        rec = {"label": label, "case": d}
+        try:
+            c = Case.from_dict(d)
+            rec["codes"] = [b.code for b in c.boundaries]
+            rec["result"] = "ok"
+            rec["values"] = {"tol": c.iteration.tol, "tmax": c.iteration.tmax, "nazim": c.velmesh.nazim,
+                             "kernel": c.performance.kernel}
+        except Exception as e:                       # the type is the fixture
+            rec["result"] = type(e).__name__
+        out.append(rec)
+    (OUT / "config_errors.json").write_text(json.dumps(out, indent=1, sort_keys=True))
+
+
 if __name__ == "__main__":
     ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if "--precond-only" in sys.argv[2:]:
+    if "--config-only" in sys.argv[2:]:
+        config_errors(Path(ref_root))
+    elif "--precond-only" in sys.argv[2:]:
         m = json.loads((OUT / "golden_meta.json").read_text())
         m.update(krylov_precond(Path(ref_root)))
         (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
