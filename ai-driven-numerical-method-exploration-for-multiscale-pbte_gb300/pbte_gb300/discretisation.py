@@ -116,9 +116,12 @@ def _edge_maps(mesh: Mesh, basis: Basis, edofs, bcdata, bc_codes, xoff, yoff):
             continue
         mine = pos[ids][:, edofs[il], :]                               # (k, nf, 2)
         theirs = pos[upwind[ids, il]] + shift[ids, il][:, None, :]     # (k, nd, 2)
-        dist = np.linalg.norm(mine[:, :, None, :] - theirs[:, None, :, :], axis=-1)
-        best = dist.argmin(axis=-1)
-        if np.take_along_axis(dist, best[..., None], -1).max() > 1e-8 * h:
+        # squared distances: the partner node is the one that coincides
+        dx = mine[:, :, None, 0] - theirs[:, None, :, 0]
+        dy = mine[:, :, None, 1] - theirs[:, None, :, 1]
+        d2 = dx * dx + dy * dy
+        best = d2.argmin(axis=-1)
+        if np.sqrt(np.take_along_axis(d2, best[..., None], -1).max()) > 1e-8 * h:
             raise ValueError("non-conforming mesh: an edge node has no partner node "
                              "in the neighbouring element")
         emap[ids, il] = best

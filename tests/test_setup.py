@@ -69,3 +69,45 @@ def test_ordinates_sum_to_4pi_and_have_z_twins():
 def test_square_counts():
     disc = Discretisation.build(small_case(2, 4, 8, 1.0, 0.1, mesh="cavity:64"))
     assert disc.n_tris == 8192 and disc.mesh.n_faces == 12416
+
+
+def _edge_maps_brute_force(mesh, basis, edofs, bcdata, bc_codes, xoff, yoff):
+    """Each edge node's partner: the nearest of all the neighbour's nodes
+    (Euclidean norm), the partner's nodes shifted by a periodic offset."""
+    from pbte_gb300.constants import BC_PERIODIC
+    from pbte_gb300.discretisation import _dof_positions
+    n, nf = mesh.n_tris, edofs.shape[1]
+    pos = _dof_positions(mesh, basis)
+    upwind = mesh.tri_neighbour.astype(np.int64).copy()
+    shift = np.zeros((n, 3, 2))
+    fb = mesh.face_bc[mesh.tri_faces]
+    code = np.where(fb >= 0, bc_codes[np.clip(fb, 0, None)] if bc_codes.size else 0, 0)
+    for i, il in zip(*np.nonzero((fb >= 0) & (code == BC_PERIODIC))):
+        fc = mesh.tri_faces[i, il]
+        upwind[i, il] = bcdata.periodic_tri[fc]
+        bcp = mesh.face_bc[mesh.face_pair[fc]]
+        shift[i, il] = (xoff[bcp], yoff[bcp])
+    emap = np.full((n, 3, nf), -1, dtype=np.int64)
+    for i in range(n):
+        for il in range(3):
+            if upwind[i, il] < 0:
+                continue
+            theirs = pos[upwind[i, il]] + shift[i, il]
+            for b in range(nf):
+                emap[i, il, b] = np.linalg.norm(theirs - pos[i, edofs[il][b]], axis=-1).argmin()
+    return upwind.astype(np.int32), emap.astype(np.int32)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3, 4])
+@pytest.mark.parametrize("kind", ["cavity:6", "cavity:5:smootherstep", "periodic"])
+def test_edge_maps_match_brute_force(deg, kind):
+    from cases import periodic_case, small_case
+    case = periodic_case(deg, 4, 8, 1.0, 0.1, mesh="channel:6") if kind == "periodic" else \
+        small_case(deg, 4, 8, 1.0, 0.1, mesh=kind)
+    disc = Discretisation.build(case)
+    xoff = np.asarray([b.xoff for b in case.boundaries], dtype=float)
+    yoff = np.asarray([b.yoff for b in case.boundaries], dtype=float)
+    up, em = _edge_maps_brute_force(disc.mesh, disc.basis, disc.edge_dofs, disc.bcdata,
+                                    np.asarray(case.bc_codes()), xoff, yoff)
+    assert np.array_equal(disc.upwind_tri, up)
+    assert np.array_equal(disc.edge_map, em)
