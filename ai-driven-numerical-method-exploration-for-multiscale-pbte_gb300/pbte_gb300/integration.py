@@ -61,10 +61,6 @@ def _mom(a: int, b: int, extra: int = 2) -> float:
 @dataclass
 class Integrals:
     int_tri: np.ndarray
-    int_tri_tri: np.ndarray
-    int_tri_tri_x: np.ndarray
-    int_tri_tri_y: np.ndarray
-    int_tri_fc: np.ndarray
     int_fc_fc: np.ndarray
     int_fc: np.ndarray
     # compact form -------------------------------------------------------
@@ -80,6 +76,57 @@ class Integrals:
     # GPU sweep needs only the compact form, and these take ~90 % of the setup
     _face_fn: object = field(default=None, repr=False)
     _face: dict = field(default_factory=dict, repr=False)
+    # pybte's per-element volume tensors (mass, gradients, edge masses) are
+    # scalings of the compact form; formed on first use (the oracle, the GSIS
+    # setup), since the GPU sweep reads the compact form only
+    _vol: dict = field(default_factory=dict, repr=False)
+
+    def _volume(self, name: str) -> np.ndarray:
+        if not self._vol:
+            a2 = self.area2
+            self._vol["int_tri_tri"] = self.ref_mass[:, :, None] * a2[None, None, :]
+            self._vol["int_tri_tri_x"] = (self.dxi[:, 0, None, None] * self.ref_dx
+                                          + self.dxi[:, 1, None, None] * self.ref_dy) * a2[:, None, None]
+            self._vol["int_tri_tri_y"] = (self.deta[:, 0, None, None] * self.ref_dx
+                                          + self.deta[:, 1, None, None] * self.ref_dy) * a2[:, None, None]
+            self._vol["int_tri_fc"] = self.edge_scale[:, :, None, None] * self.ref_edge[None]
+        return self._vol[name]
+
+    @property
+    def int_tri_tri(self) -> np.ndarray:
+        return self._volume("int_tri_tri")
+
+    @int_tri_tri.setter
+    def int_tri_tri(self, v: np.ndarray) -> None:
+        self._volume("int_tri_tri")
+        self._vol["int_tri_tri"] = v
+
+    @property
+    def int_tri_tri_x(self) -> np.ndarray:
+        return self._volume("int_tri_tri_x")
+
+    @int_tri_tri_x.setter
+    def int_tri_tri_x(self, v: np.ndarray) -> None:
+        self._volume("int_tri_tri_x")
+        self._vol["int_tri_tri_x"] = v
+
+    @property
+    def int_tri_tri_y(self) -> np.ndarray:
+        return self._volume("int_tri_tri_y")
+
+    @int_tri_tri_y.setter
+    def int_tri_tri_y(self, v: np.ndarray) -> None:
+        self._volume("int_tri_tri_y")
+        self._vol["int_tri_tri_y"] = v
+
+    @property
+    def int_tri_fc(self) -> np.ndarray:
+        return self._volume("int_tri_fc")
+
+    @int_tri_fc.setter
+    def int_tri_fc(self, v: np.ndarray) -> None:
+        self._volume("int_tri_fc")
+        self._vol["int_tri_fc"] = v
 
     def _faces(self, k: int) -> np.ndarray:
         if k not in self._face:
@@ -151,7 +198,6 @@ def build_integrals(mesh: Mesh, basis: Basis, np_fc: int = 15, bc_codes=None,
     ref_edge = np.einsum("mk,ekl,nl->emn", C, e_e, C)
 
     int_tri = ref_tri[:, None] * area2[None, :]
-    int_tri_tri = ref_mass[:, :, None] * area2[None, None, :]
 
     x = nodes[mesh.tri_nodes, 0]
     y = nodes[mesh.tri_nodes, 1]
@@ -160,14 +206,11 @@ def build_integrals(mesh: Mesh, basis: Basis, np_fc: int = 15, bc_codes=None,
     ss = (x2 - x1) * (y3 - y1) - (x3 - x1) * (y2 - y1)
     dxi = np.stack([(y3 - y1) / ss, (y1 - y2) / ss], 1)
     deta = np.stack([(x1 - x3) / ss, (x2 - x1) / ss], 1)
-    int_tri_tri_x = (dxi[:, 0, None, None] * ref_dx + dxi[:, 1, None, None] * ref_dy) * area2[:, None, None]
-    int_tri_tri_y = (deta[:, 0, None, None] * ref_dx + deta[:, 1, None, None] * ref_dy) * area2[:, None, None]
 
     len12 = np.sqrt((x2 - x1) ** 2 + (y2 - y1) ** 2)
     len23 = np.sqrt((x3 - x2) ** 2 + (y3 - y2) ** 2)
     len31 = np.sqrt((x3 - x1) ** 2 + (y3 - y1) ** 2)
     edge_scale = np.stack([len12, len23 / sqrt(2.0), len31], 1)
-    int_tri_fc = edge_scale[:, :, None, None] * ref_edge[None]
 
     # face basis on [-1, 1]
     e_line = np.array([[2.0 / (m + l + 1) if (m + l) % 2 == 0 else 0.0
@@ -181,9 +224,7 @@ def build_integrals(mesh: Mesh, basis: Basis, np_fc: int = 15, bc_codes=None,
     def faces():
         return _face_tensors(mesh, basis, np_fc, bc_codes, bc_xoff, bc_yoff, chunk)
 
-    return Integrals(int_tri=int_tri, int_tri_tri=int_tri_tri, int_tri_tri_x=int_tri_tri_x,
-                     int_tri_tri_y=int_tri_tri_y, int_tri_fc=int_tri_fc,
-                     int_fc_fc=int_fc_fc, int_fc=int_fc, ref_mass=ref_mass, ref_dx=ref_dx,
+    return Integrals(int_tri=int_tri, int_fc_fc=int_fc_fc, int_fc=int_fc, ref_mass=ref_mass, ref_dx=ref_dx,
                      ref_dy=ref_dy, ref_edge=ref_edge, area2=area2, dxi=dxi, deta=deta,
                      edge_scale=edge_scale, _face_fn=faces)
 
