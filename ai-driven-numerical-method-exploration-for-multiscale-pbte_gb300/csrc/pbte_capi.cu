@@ -129,6 +129,7 @@ int pbte_factorise_f32(pbte_ctx *c, void *stream) {
             return PBTE_ERR_NOMEM;
         }
         c->device_bytes += n * sizeof(float);
+        pbte::g_live_bytes += (long long)(n * sizeof(float));
     }
     int rc = pbte::launch_factorise32(c, S(stream));
     if (rc) {
@@ -173,7 +174,7 @@ int pbte_correct(pbte_ctx *c, double *vdf, const double *uq, const double *tri_h
 }
 
 int pbte_gmres_columns_f32(pbte_ctx *c, const pbte_gmres_cycle_f32 *a, int32_t j0, int32_t j1, void *stream) {
-    if (!c || !a || j0 < 0 || j1 <= j0 || j1 >= 64 || !a->Q || !a->uin || !a->uout || !a->w || !a->state) return PBTE_ERR_ARG;
+    if (!c || !a || j0 < 0 || j1 <= j0 || j1 >= PBTE_MAX_BASIS || !a->Q || !a->uin || !a->uout || !a->w || !a->state) return PBTE_ERR_ARG;
     if (a->ldq < a->n || a->ldr < j1) return PBTE_ERR_ARG;
     if (!a->ts || !a->qxs || !a->qys || !a->vdf32 || !a->ts_out || !a->qxs_out || !a->qys_out) return PBTE_ERR_ARG;
     if (c->n_wall_ad && (!a->flux_wall_in || !a->flux_wall_out)) return PBTE_ERR_ARG;

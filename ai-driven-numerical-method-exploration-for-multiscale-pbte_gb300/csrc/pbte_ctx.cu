@@ -24,6 +24,10 @@
 
 #include "pbte_internal.cuh"
 
+namespace pbte {
+std::atomic<long long> g_live_bytes{0};
+}
+
 namespace {
 
 template <typename T>
@@ -31,6 +35,7 @@ int upload(const T *h, size_t n, T **d, size_t *bytes) {
     if (n == 0) { *d = nullptr; return PBTE_OK; }
     if (cudaMalloc((void **)d, n * sizeof(T)) != cudaSuccess) return PBTE_ERR_NOMEM;
     *bytes += n * sizeof(T);
+    pbte::g_live_bytes += (long long)(n * sizeof(T));
     if (cudaMemcpy(*d, h, n * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return PBTE_ERR_CUDA;
     return PBTE_OK;
 }
@@ -40,6 +45,7 @@ int alloc(size_t n, T **d, size_t *bytes) {
     if (n == 0) { *d = nullptr; return PBTE_OK; }
     if (cudaMalloc((void **)d, n * sizeof(T)) != cudaSuccess) return PBTE_ERR_NOMEM;
     *bytes += n * sizeof(T);
+    pbte::g_live_bytes += (long long)(n * sizeof(T));
     return PBTE_OK;
 }
 
@@ -287,9 +293,25 @@ extern "C" int pbte_ctx_destroy(pbte_ctx *c) {
                     c->d_psnap, c->d_gsis, c->d_lu32, c->d_tickets};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    pbte::g_live_bytes -= (long long)c->device_bytes;
     delete c;
     return PBTE_OK;
 }
+
+namespace {
+// Owns a context under construction: destroys it unless released.
+struct CtxGuard {
+    pbte_ctx *c;
+    ~CtxGuard() {
+        if (c) pbte_ctx_destroy(c);
+    }
+    pbte_ctx *release() {
+        pbte_ctx *p = c;
+        c = nullptr;
+        return p;
+    }
+};
+}  // namespace
 
 static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **out) {
     if (!d || !out) return PBTE_ERR_ARG;
@@ -299,7 +321,11 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
     if (nt <= 0 || ndir <= 0 || d->n_faces <= 0 || deg < 1 || deg > 4 ||
         nd != (deg + 1) * (deg + 2) / 2)
         return PBTE_ERR_ARG;
-    pbte_ctx *c = new pbte_ctx();
+    // the guard destroys the half-built context on every early return and on
+    // a C++ exception (a failed host allocation), so neither leaks it
+    CtxGuard guard{new pbte_ctx()};
+    pbte_ctx *c = guard.c;
+    if (cudaGetDevice(&c->device) != cudaSuccess) return PBTE_ERR_CUDA;
     c->n_tris = nt; c->n_faces = d->n_faces; c->nd = nd; c->nf = nf; c->ndir = ndir;
     c->nbc = d->nbc; c->deg = deg;
     c->cv = d->cv; c->vg = d->vg; c->tau_r = d->tau_r; c->tau_n = d->tau_n; c->tau_c = d->tau_c;
@@ -307,7 +333,7 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
     c->h_cy.assign(d->cyv, d->cyv + ndir);
     c->h_w.assign(d->domega, d->domega + ndir);
     int rc = PBTE_OK;
-#define TRY(x) do { rc = (x); if (rc != PBTE_OK) { pbte_ctx_destroy(c); return rc; } } while (0)
+#define TRY(x) do { rc = (x); if (rc != PBTE_OK) return rc; } while (0)
 
     // ---- element records -------------------------------------------------
     std::vector<pbte::CellRec<double>> r64(nt);
@@ -324,20 +350,20 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
             r.nx[il] = d->nx[i * 3 + il];
             r.ny[il] = d->ny[i * 3 + il];
             int fc = d->tri_faces[i * 3 + il];
-            if (fc < 0 || fc >= d->n_faces) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+            if (fc < 0 || fc >= d->n_faces) { return PBTE_ERR_ARG; }
             r.face[il] = fc;
             r.upw[il] = d->upwind_tri[i * 3 + il];
             int bc = d->face_bc[fc];
             if (bc < 0) {
                 r.kind[il] = 0;
-                if (r.upw[il] < 0 || r.upw[il] >= nt) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+                if (r.upw[il] < 0 || r.upw[il] >= nt) { return PBTE_ERR_ARG; }
             } else {
-                if (bc >= d->nbc) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+                if (bc >= d->nbc) { return PBTE_ERR_ARG; }
                 int t = d->bc_type[bc];
                 if (t == 1) { r.kind[il] = 1; r.bval[il] = d->cv / four_pi * d->bc_temp[bc]; }
                 else if (t == 2) r.kind[il] = 2;
                 else if (t == 3) { r.kind[il] = 3; c->has_periodic = true; }
-                else { pbte_ctx_destroy(c); return PBTE_ERR_UNSUPPORTED; }
+                else { return PBTE_ERR_UNSUPPORTED; }
             }
             for (int b = 0; b < nf; ++b) {
                 int v = r.upw[il] >= 0 ? d->edge_map[(i * 3 + il) * nf + b] : 0;
@@ -404,7 +430,7 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
         const int side = d->face_tri[f * 2 + 0] >= 0 ? 0 : 1;
         const int t = d->face_tri[f * 2 + side], l = d->face_lfc[f * 2 + side];
         const int partner = d->upwind_tri[t * 3 + l];
-        if (partner < 0 || partner >= nt) { pbte_ctx_destroy(c); return PBTE_ERR_ARG; }
+        if (partner < 0 || partner >= nt) { return PBTE_ERR_ARG; }
         pslot[f] = (int32_t)pface.size();
         pface.push_back(f);
         ptri.push_back(partner);
@@ -564,7 +590,7 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
     }
     for (int k = 0; k < c->nclass; ++k) {
         const ClassOut &o = cls_out[k];
-        if (o.status != PBTE_OK) { pbte_ctx_destroy(c); return o.status; }
+        if (o.status != PBTE_OK) { return o.status; }
         class_off[k] = (int32_t)lvl_ptr.size();
         class_nlev[k] = o.nlev;
         for (int L = 0; L <= o.nlev; ++L) lvl_ptr.push_back(o.count[L] + k * nt);
@@ -635,11 +661,10 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
     TRY(alloc((size_t)4 * nd * nt, &c->d_gsis, &c->device_bytes));
     TRY(alloc((size_t)(nt + 31) / 32, &c->d_tickets, &c->device_bytes));
     if (cudaMemset(c->d_tickets, 0, sizeof(uint32_t) * ((nt + 31) / 32)) != cudaSuccess) {
-        pbte_ctx_destroy(c);
         return PBTE_ERR_CUDA;
     }
     TRY(alloc((size_t)1, &c->d_singular, &c->device_bytes));
-    if (cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
+    if (cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) { return PBTE_ERR_CUDA; }
 
     if (precompute) {
         TRY(alloc(pbte::factor_count(c->n_udir, nt, nd * nd), &c->d_lu, &c->device_bytes));
@@ -647,14 +672,13 @@ static int ctx_create_impl(const pbte_case_desc *d, int precompute, pbte_ctx **o
         TRY(pbte::launch_factorise(c, 0));
         int32_t bad = 0;
         if (cudaMemcpy(&bad, c->d_singular, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) {
-            pbte_ctx_destroy(c);
             return PBTE_ERR_CUDA;
         }
-        if (bad) { pbte_ctx_destroy(c); return PBTE_ERR_SINGULAR; }
+        if (bad) { return PBTE_ERR_SINGULAR; }
     }
-    if (cudaDeviceSynchronize() != cudaSuccess) { pbte_ctx_destroy(c); return PBTE_ERR_CUDA; }
+    if (cudaDeviceSynchronize() != cudaSuccess) { return PBTE_ERR_CUDA; }
 #undef TRY
-    *out = c;
+    *out = guard.release();
     return PBTE_OK;
 }
 
@@ -666,6 +690,21 @@ extern "C" int pbte_ctx_create(const pbte_case_desc *d, int precompute, pbte_ctx
         if (out) *out = nullptr;
         return PBTE_ERR_NOMEM;
     }
+}
+
+extern "C" int pbte_singular_count(pbte_ctx *c, int64_t *count, int reset) {
+    if (!c || !count) return PBTE_ERR_ARG;
+    int32_t v = 0;
+    if (cudaMemcpy(&v, c->d_singular, sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess) return PBTE_ERR_CUDA;
+    *count = v;
+    if (reset && cudaMemset(c->d_singular, 0, sizeof(int32_t)) != cudaSuccess) return PBTE_ERR_CUDA;
+    return PBTE_OK;
+}
+
+extern "C" int pbte_device_bytes_live(int64_t *bytes) {
+    if (!bytes) return PBTE_ERR_ARG;
+    *bytes = pbte::g_live_bytes.load();
+    return PBTE_OK;
 }
 
 extern "C" int pbte_ctx_info(const pbte_ctx *c, int64_t *nlev, int64_t *ncls, int64_t *bytes) {

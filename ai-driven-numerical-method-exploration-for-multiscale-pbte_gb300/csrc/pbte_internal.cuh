@@ -4,11 +4,15 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <vector>
 
 #include "pbte_gb300.h"
 
 namespace pbte {
+
+// device bytes held by all live contexts (pbte_device_bytes_live)
+extern std::atomic<long long> g_live_bytes;
 
 constexpr double kPi = 3.141592653589793238462643383279502884;
 constexpr int kMaxNf = 5;   // deg <= 4
@@ -72,6 +76,7 @@ struct WallFace {
 
 struct pbte_ctx {
     int n_tris = 0, n_faces = 0, nd = 0, nf = 0, ndir = 0, nbc = 0, deg = 0;
+    int device = -1;   // the CUDA device current when the context was created
     double cv = 1, vg = 1, tau_r = 1, tau_n = 1, tau_c = 1;
     std::vector<double> h_cx, h_cy, h_w;
     bool has_periodic = false;
@@ -185,6 +190,8 @@ int launch_transport_residual_scratch(pbte_ctx *c, const double *ts, const doubl
                                       const double *vdf, const double *fw, double *num, double *den,
                                       double *S, cudaStream_t s);
 int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s);
+int launch_gsis_hot_apply(pbte_ctx *c, const pbte_gsis_ops *o, const double *vdf, double tc5, double *aa_src,
+                          cudaStream_t s);
 int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk,
                       const int32_t *tri_list, const int32_t *lfc_list, double *out,
                       cudaStream_t s);

@@ -3,11 +3,10 @@
 //
 // Who needs it.  pbte_transport_residual keeps its per-element moment sources
 // in scratch owned by the context.  Some callers cannot allocate device
-// memory at all where they call from -- code that runs while another stream
-// is being captured into a CUDA graph in global capture mode (cudaMalloc is
-// illegal then), or a host that hands the whole device to its own memory pool
-// -- and some must not touch the context's scratch because a sweep may be
-// using it.  This entry point allocates nothing: its scratch is a file-scope
+// memory at all where they call from -- a host that hands the whole device to
+// its own memory pool, where a cudaMalloc behind the pool's back fails or
+// breaks its accounting -- and some must not touch the context's scratch
+// because a sweep may be using it.  This entry point allocates nothing: its scratch is a file-scope
 // __device__ array of kScratchDoubles doubles (4 MiB) that every GPU loading
 // the library holds until the process exits.
 //
@@ -18,6 +17,9 @@
 //    cudaGetSymbolAddress (with that device current); under lazy module
 //    loading that is also when the runtime commits the array's 4 MiB.  Make
 //    that first call before any stream capture begins.
+//  - Call it with the context's device current: the array's address is per
+//    device, so a call on another device is refused (PBTE_ERR_ARG).
+//  - Periodic faces are refused (PBTE_ERR_UNSUPPORTED).
 //  - All calls share the one array: calls whose kernels overlap on the GPU
 //    race.  The array carries nothing from one call to the next (each call
 //    overwrites all of it that it reads), so nothing needs clearing.
@@ -59,6 +61,10 @@ extern "C" int pbte_transport_residual_noalloc(pbte_ctx *c, const double *ts, co
     if (!c || !ts || !qxs || !qys || !vdf || !num || !den) return PBTE_ERR_ARG;
     if (c->n_wall_ad && !flux_wall) return PBTE_ERR_ARG;
     if (3LL * c->nd * c->n_tris > kScratchDoubles) return PBTE_ERR_ARG;
+    if (c->has_periodic) return PBTE_ERR_UNSUPPORTED;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return PBTE_ERR_CUDA;
+    if (dev != c->device) return PBTE_ERR_ARG;
     double *S = scratch_address();
     if (!S) return PBTE_ERR_CUDA;
     return pbte::launch_transport_residual_scratch(c, ts, qxs, qys, vdf, flux_wall, num, den, S,

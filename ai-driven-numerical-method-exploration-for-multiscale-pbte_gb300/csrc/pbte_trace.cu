@@ -45,7 +45,9 @@ __device__ __forceinline__ double gather_updates(const int64_t *cptr, const int6
 __global__ void __launch_bounds__(kThreads) nd_forward_kernel(const int4 *items, const NodeMeta *meta,
                                                               const int32_t *idx, const int64_t *cptr,
                                                               const int64_t *csrc, const double *G,
-                                                              const double *b, double *z, double *delta) {
+                                                              const double *b, double *z, double *delta,
+                                                              const int32_t *done) {
+    if (done != nullptr && *(volatile const int32_t *)done != 0) return;
     extern __shared__ double v[];
     const int4 it = items[blockIdx.x];
     const NodeMeta mt = meta[it.x];
@@ -69,7 +71,9 @@ __global__ void __launch_bounds__(kThreads) nd_forward_kernel(const int4 *items,
 
 __global__ void __launch_bounds__(kThreads) nd_backward_kernel(const int4 *items, const NodeMeta *meta,
                                                                const int32_t *idx, const double *H,
-                                                               const double *z, double *x) {
+                                                               const double *z, double *x,
+                                                               const int32_t *done) {
+    if (done != nullptr && *(volatile const int32_t *)done != 0) return;
     extern __shared__ double w[];
     const int4 it = items[blockIdx.x];
     const NodeMeta mt = meta[it.x];
@@ -107,7 +111,7 @@ int shm_for(K kern, int32_t n_values, size_t *shm) {
 
 extern "C" int pbte_nd_forward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
                                const int64_t *cptr, const int64_t *csrc, const double *G, const double *b,
-                               double *z, double *delta, int32_t max_own, void *stream) {
+                               double *z, double *delta, int32_t max_own, const int32_t *done, void *stream) {
     if (!items || !meta || !idx || !cptr || !csrc || !G || !b || !z || !delta || n_items < 0) return PBTE_ERR_ARG;
     if (n_items == 0) return PBTE_OK;
     size_t shm = 0;
@@ -115,18 +119,19 @@ extern "C" int pbte_nd_forward(const int32_t *items, int32_t n_items, const int6
     if (rc) return rc;
     nd_forward_kernel<<<n_items, kThreads, shm, reinterpret_cast<cudaStream_t>(stream)>>>(
         reinterpret_cast<const int4 *>(items), reinterpret_cast<const NodeMeta *>(meta), idx, cptr, csrc, G, b, z,
-        delta);
+        delta, done);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
 extern "C" int pbte_nd_backward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
-                                const double *H, const double *z, double *x, int32_t max_front, void *stream) {
+                                const double *H, const double *z, double *x, int32_t max_front, const int32_t *done,
+                                void *stream) {
     if (!items || !meta || !idx || !H || !z || !x || n_items < 0) return PBTE_ERR_ARG;
     if (n_items == 0) return PBTE_OK;
     size_t shm = 0;
     int rc = shm_for(nd_backward_kernel, max_front, &shm);
     if (rc) return rc;
     nd_backward_kernel<<<n_items, kThreads, shm, reinterpret_cast<cudaStream_t>(stream)>>>(
-        reinterpret_cast<const int4 *>(items), reinterpret_cast<const NodeMeta *>(meta), idx, H, z, x);
+        reinterpret_cast<const int4 *>(items), reinterpret_cast<const NodeMeta *>(meta), idx, H, z, x, done);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }

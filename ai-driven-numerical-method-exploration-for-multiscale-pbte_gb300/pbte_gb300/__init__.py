@@ -12,7 +12,7 @@ from .config import Case, square_case
 from .discretisation import Discretisation
 
 __all__ = ["Case", "square_case", "Discretisation", "Solver", "SweepContext", "Moments",
-           "RunRecord", "build"]
+           "RunRecord", "SweepCycleError", "build"]
 
 
 def build(force: bool = False):
@@ -24,7 +24,7 @@ def __getattr__(name):
     if name in ("Solver", "RunRecord"):
         from . import solver
         return getattr(solver, name)
-    if name in ("SweepContext", "Moments"):
+    if name in ("SweepContext", "Moments", "SweepCycleError"):
         from . import sweep
         return getattr(sweep, name)
     raise AttributeError(name)

@@ -21,7 +21,16 @@ SOURCES = ["pbte_ctx.cu", "pbte_kernels.cu", "pbte_sweep.cu", "pbte_krylov.cu", 
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 PBTE_OK = 0
-CGS2_SCRATCH = 1220 * 64   # PBTE_CGS2_SCRATCH
+MAX_BASIS = 1024           # PBTE_MAX_BASIS
+
+
+def cgs2_scratch(rows: int) -> int:
+    """PBTE_CGS2_SCRATCH_ROWS(rows): doubles of scratch a CGS2 over ``rows``
+    basis rows needs."""
+    return 8 + 2 * MAX_BASIS + 1216 * ((rows + 7) // 8 * 8)
+
+
+CGS2_SCRATCH = cgs2_scratch(64)   # PBTE_CGS2_SCRATCH
 ERRORS = {-1: "bad argument", -2: "CUDA runtime error", -3: "sweep graph has a cycle",
           -4: "configuration not supported", -5: "device wait timed out",
           -6: "singular element operator", -7: "device allocation failed"}
@@ -103,6 +112,17 @@ class GmresCycleF32(ctypes.Structure):
                 ("tol_abs", _vp), ("state", _vp), ("hist", _vp)]
 
 
+class GsisOps(ctypes.Structure):
+    """Mirror of ``pbte_gsis_ops`` (the field-major static-condensation
+    operators of the GSIS step)."""
+    _fields_ = [("n_tris", ctypes.c_int32), ("n_faces", ctypes.c_int32), ("ndof", ctypes.c_int32),
+                ("ndof_fc", ctypes.c_int32), ("variant", ctypes.c_int32), ("n2", ctypes.c_int32),
+                ("n_walls", ctypes.c_int32), ("pad", ctypes.c_int32), ("cv", ctypes.c_double),
+                ("inv_t", _vp), ("ba1_t", _vp), ("tri1", _vp), ("ba2_t", _vp), ("slot2", _vp), ("tri2", _vp),
+                ("mirror2", _vp), ("wall_slot", _vp), ("wall_kind", _vp), ("wall_nx", _vp), ("wall_ny", _vp),
+                ("aa_trace_t", _vp), ("tri_faces", _vp)]
+
+
 _SIGS = {
     "pbte_ctx_create": ([ctypes.POINTER(CaseDesc), ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
     "pbte_ctx_destroy": ([_vp], ctypes.c_int),
@@ -139,6 +159,11 @@ _SIGS = {
                                  ctypes.c_int64, _vp, _vp], ctypes.c_int),
     "pbte_gmres_givens": ([ctypes.c_int32, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
                           ctypes.c_int),
+    "pbte_gmres_givens_bounded": ([ctypes.c_int32, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+                                  ctypes.c_int),
+    "pbte_arnoldi_column_givens": ([_vp, ctypes.c_int64, ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, _vp,
+                                    ctypes.c_int64, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp,
+                                    ctypes.c_int32, _vp], ctypes.c_int),
     "pbte_gmres_next_basis": ([ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp, _vp],
                               ctypes.c_int),
     "pbte_gmres_next_basis_f32": ([ctypes.c_int32, _vp, _vp, _vp, ctypes.c_int64, _vp, ctypes.c_int64, _vp, _vp],
@@ -150,9 +175,16 @@ _SIGS = {
     "pbte_correct": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int] + [_vp] * 6 + [_vp],
                      ctypes.c_int),
     "pbte_batched_inverse": ([_vp, _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp], ctypes.c_int),
-    "pbte_nd_forward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp],
+    "pbte_nd_forward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp, _vp],
                         ctypes.c_int),
-    "pbte_nd_backward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp], ctypes.c_int),
+    "pbte_nd_backward": ([_vp, ctypes.c_int32, _vp, _vp, _vp, _vp, _vp, ctypes.c_int32, _vp, _vp], ctypes.c_int),
+    "pbte_gsis_hot_apply": ([_vp, ctypes.POINTER(GsisOps), _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
+    "pbte_gsis_apply_inverse": ([ctypes.POINTER(GsisOps), _vp, ctypes.c_int32, ctypes.c_int32, _vp, _vp, _vp],
+                                ctypes.c_int),
+    "pbte_gsis_trace_rhs": ([ctypes.POINTER(GsisOps), _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_gsis_local_recover": ([ctypes.POINTER(GsisOps), _vp, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_singular_count": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int], ctypes.c_int),
+    "pbte_device_bytes_live": ([ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_factorise_f32": ([_vp, _vp], ctypes.c_int),
     "pbte_periodic_count": ([_vp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_periodic_gather": ([_vp, _vp, _vp, _vp], ctypes.c_int),

@@ -27,36 +27,63 @@ class BoundaryData:
     has_periodic: bool
 
 
+def _wall_table(boundaries):
+    """Per boundary condition: code, wall temperature and periodic offset."""
+    code = np.fromiter((b.code for b in boundaries), dtype=np.int32, count=len(boundaries))
+    temp = np.fromiter((float(b.temp) for b in boundaries), dtype=np.float64, count=len(boundaries))
+    shift = np.array([[float(b.xoff), float(b.yoff)] for b in boundaries], dtype=np.float64).reshape(-1, 2)
+    return code, temp, shift
+
+
+def _periodic_links(mesh, code, shift):
+    """For every face of a periodic pair: the element behind its partner face,
+    and whether the partner's 1-D trace runs the opposite way (its first node
+    matches this face's first node only after the pair's shift when the two
+    faces are walked in the same sense; otherwise their DOFs are mirrored).
+
+    All periodic faces are treated at once: each face's first node, shifted
+    by its boundary's offset, is compared with both end nodes of the partner,
+    with the tolerance of ``numpy.allclose`` per coordinate pair."""
+    n = mesh.n_faces
+    behind = np.full(n, -1, dtype=np.int32)
+    mirrored = np.zeros(n, dtype=bool)
+    fb = mesh.face_bc
+    wall = fb >= 0
+    is_pair = np.zeros(n, dtype=bool)
+    is_pair[wall] = code[fb[wall]] == BC_PERIODIC
+    faces = np.flatnonzero(is_pair)
+    if faces.size == 0:
+        return behind, mirrored
+    partner = mesh.face_pair[faces]
+    lonely = faces[partner < 0]
+    if lonely.size:
+        raise ValueError(f"periodic face {int(lonely[0])} has no partner face "
+                         f"({lonely.size} periodic faces without one)")
+    tri_of_face, _ = mesh.adjacent_all()
+    behind[faces] = tri_of_face[partner]
+    first = mesh.nodes[mesh.face_nodes[faces, 0]] + shift[fb[faces]]
+    ends = mesh.nodes[mesh.face_nodes[partner]]                  # (k, 2 ends, 2 coords)
+    same_sense = np.isclose(first, ends[:, 0]).all(axis=1)
+    reversed_sense = np.isclose(first, ends[:, 1]).all(axis=1)
+    misfit = ~(same_sense | reversed_sense)
+    if misfit.any():
+        f = int(faces[misfit][0])
+        raise ValueError(f"periodic face {f} and its partner {int(mesh.face_pair[f])} do not meet "
+                         f"under the boundary's offset {tuple(shift[fb[f]])}")
+    mirrored[faces] = reversed_sense & ~same_sense
+    return behind, mirrored
+
+
 def build_boundary_data(mesh, boundaries, ndof_tri: int) -> BoundaryData:
-    bc_type = np.array([b.code for b in boundaries], dtype=np.int32)
-    bc_temp = np.array([float(b.temp) for b in boundaries], dtype=np.float64)
-    bc_xoff = np.array([float(b.xoff) for b in boundaries], dtype=np.float64)
-    bc_yoff = np.array([float(b.yoff) for b in boundaries], dtype=np.float64)
-    if np.any(bc_type == BC_SYMMETRY):
-        raise NotImplementedError("symmetry walls (type 4) are not implemented; "
-                                  "use a periodic pair instead")
-    n_faces = mesh.n_faces
-    periodic_tri = np.full(n_faces, -1, dtype=np.int32)
-    periodic_flip = np.zeros(n_faces, dtype=bool)
-    has_periodic = bool(np.any(bc_type == BC_PERIODIC))
-    if has_periodic:
-        for f in np.flatnonzero(mesh.face_bc >= 0):
-            bc = int(mesh.face_bc[f])
-            if bc_type[bc] != BC_PERIODIC:
-                continue
-            pair = int(mesh.face_pair[f])
-            if pair < 0:
-                raise ValueError(f"periodic face {f} has no partner")
-            periodic_tri[f] = mesh.adjacent(pair)[0]
-            a = mesh.nodes[mesh.face_nodes[f, 0]] + np.array([bc_xoff[bc], bc_yoff[bc]])
-            b1 = mesh.nodes[mesh.face_nodes[pair, 0]]
-            b2 = mesh.nodes[mesh.face_nodes[pair, 1]]
-            if np.allclose(a, b2) and not np.allclose(a, b1):
-                periodic_flip[f] = True
-            elif not np.allclose(a, b1):
-                raise ValueError(f"periodic faces {f} and {pair} do not line up")
-    return BoundaryData(bc_type=bc_type, bc_temp=bc_temp, periodic_tri=periodic_tri,
-                        periodic_flip=periodic_flip,
-                        flux_wall=np.zeros((n_faces, ndof_tri)),
-                        has_nonthermalising=bool(np.any(bc_type == BC_NONTHERMALISING)),
-                        has_periodic=has_periodic)
+    """Wall tables and periodic links for the sweep (``pybte/bc.py:120-170``):
+    symmetry walls are refused, as pybte does, since its transport solve never
+    implements them."""
+    code, temp, shift = _wall_table(boundaries)
+    if (code == BC_SYMMETRY).any():
+        raise NotImplementedError("symmetry walls (type 4) have no transport treatment; "
+                                  "describe the domain with a periodic pair instead")
+    behind, mirrored = _periodic_links(mesh, code, shift)
+    return BoundaryData(bc_type=code, bc_temp=temp, periodic_tri=behind, periodic_flip=mirrored,
+                        flux_wall=np.zeros((mesh.n_faces, ndof_tri)),
+                        has_nonthermalising=bool((code == BC_NONTHERMALISING).any()),
+                        has_periodic=bool((code == BC_PERIODIC).any()))

@@ -3,15 +3,24 @@
 Per outer iteration, after the sweep (``acceleration/__init__.py:95-115``):
 
 1. hot source: third-order angular moments of the kinetic solution contracted
-   with the gradient tensors (device kernel), premultiplied by the element
-   inverses ``inv_aa_sol`` (batched product);
+   with the gradient tensors and premultiplied by the element inverses
+   ``inv_aa_sol`` (``pbte_gsis_hot_apply``: one angular-sum launch, then one
+   launch that forms each element's source in shared memory and applies the
+   inverse);
 2. trace right-hand side: ``BA_SOL @ AA_SRC`` from the one or two elements of
-   each face, wall rows imposed from the kinetic wall traces (device);
+   each face, wall rows imposed from the kinetic wall traces
+   (``pbte_wall_trace``, ``pbte_gsis_trace_rhs``);
 3. trace solve with the once-factorised global matrix: on the device from
    nested-dissection multifrontal factors (:mod:`pbte_gb300.trace_nd`,
    default), or SuperLU on the host (``performance.trace_solver = "host"``);
-4. local recovery ``UQ = AA_SRC + sum AA_TRACE @ U_TRACE`` (batched product);
-5. damped correction of the distribution and the moments (device kernel).
+4. local recovery ``UQ = AA_SRC + sum AA_TRACE @ U_TRACE``
+   (``pbte_gsis_local_recover``);
+5. damped correction of the distribution and the moments (``pbte_correct``).
+
+Every per-iteration launch is the library's own kernel; the element and face
+operators are stored field-major (``pbte_gsis_ops``) so that each of those
+kernels reads them coalesced.  With the device trace solve, a GSIS step is
+graph-captured and every launch honours the run's device stop flag.
 
 Setup (``assembly.py:44-269``) builds the 7x7-block element matrices on the
 host, inverts them with the library's batched Gauss-Jordan kernel, forms
@@ -147,10 +156,14 @@ class GSIS:
         if int(bad.item()):
             raise np.linalg.LinAlgError(f"{int(bad.item())} singular HDG element matrices")
         del A_d
-        self.inv_aa_sol = inv                                           # (n, 7nd, 7nd)
         T_d = torch.from_numpy(T).to(dev)
-        self.aa_trace = torch.einsum("ipq,ilqr->ilpr", inv, T_d).contiguous()   # (n, 3, 7nd, 3nf)
+        aa_trace = torch.einsum("ipq,ilqr->ilpr", inv, T_d).contiguous()   # (n, 3, 7nd, 3nf)
         del T_d
+        # field-major copies for the per-iteration kernels (pbte_gsis_ops)
+        self.inv_t = inv.permute(2, 0, 1).contiguous()                   # [q][i][p] = inv[i][p][q]
+        self.aa_trace_t = aa_trace.permute(1, 3, 0, 2).contiguous()      # [il][r][i][p]
+        self.aa_trace = aa_trace
+        del inv
         B = ba_sol_blocks(disc, st, self.variant)
         self.ba_sol = torch.from_numpy(B).to(dev)                        # (n, 3, 3nf, 7nd)
 
@@ -218,37 +231,61 @@ class GSIS:
         else:
             self.solver = TraceSolver(K, dev)
 
-        # per-iteration bookkeeping (global_solve.py:88-117)
-        self.p1 = (torch.from_numpy(p1_tri).to(dev), torch.from_numpy(p1_lfc).to(dev))
+        # per-iteration operators (global_solve.py:88-117), field-major
+        i32 = dict(dtype=torch.int32, device=dev)
         sel2 = np.flatnonzero(has_p2)
-        self.sel2 = torch.from_numpy(sel2).to(dev)
-        self.p2 = (torch.from_numpy(p2_tri[sel2]).to(dev), torch.from_numpy(p2_lfc[sel2]).to(dev))
-        self.ba1 = self.ba_sol[self.p1].contiguous()
-        self.ba2 = self.ba_sol[self.p2].contiguous()
-        self.flip2 = torch.from_numpy(mirror2[sel2]).to(dev)
-        # rows of the second side that are mirrored periodic faces, as indices
-        # (no data-dependent shapes per iteration, so the step can be captured)
-        self.flip2_rows = torch.from_numpy(np.flatnonzero(mirror2[sel2])).to(dev)
-        self.perm = permt
+        ba1 = self.ba_sol[torch.from_numpy(p1_tri).to(dev), torch.from_numpy(p1_lfc).to(dev)]   # (n_faces, nf3, 7nd)
+        self.ba1_t = ba1.permute(2, 0, 1).contiguous()                                          # [p][f][r]
+        del ba1
+        self.n2 = int(sel2.size)
+        if self.n2:
+            ba2 = self.ba_sol[torch.from_numpy(p2_tri[sel2]).to(dev), torch.from_numpy(p2_lfc[sel2]).to(dev)]
+            self.ba2_t = ba2.permute(2, 0, 1).contiguous()
+            del ba2
+        else:
+            self.ba2_t = torch.zeros(1, **f64)
+        del self.ba_sol, self.aa_trace
+        slot2 = np.full(m.n_faces, -1, dtype=np.int32)
+        slot2[sel2] = np.arange(self.n2, dtype=np.int32)
+        self.tri1 = torch.from_numpy(p1_tri.astype(np.int32)).to(dev)
+        self.slot2 = torch.from_numpy(slot2).to(dev)
+        self.tri2 = torch.from_numpy(p2_tri[sel2].astype(np.int32)).to(dev) if self.n2 else torch.zeros(1, **i32)
+        self.mirror2 = (torch.from_numpy(mirror2[sel2].astype(np.int32)).to(dev) if self.n2
+                        else torch.zeros(1, **i32))
         wall_th = np.flatnonzero((fbc >= 0) & (code == BC_THERMALISING))
         wall_ad = np.flatnonzero((fbc >= 0) & (code == BC_NONTHERMALISING))
         self.wall_all = np.concatenate([wall_th, wall_ad])
         self.n_th = wall_th.size
-        self.wall_idx = torch.from_numpy(self.wall_all).to(dev)
+        wall_slot = np.full(m.n_faces, -1, dtype=np.int32)
+        wall_slot[self.wall_all] = np.arange(self.wall_all.size, dtype=np.int32)
+        wall_kind = np.zeros(m.n_faces, dtype=np.int32)
+        wall_kind[wall_th] = 1
+        wall_kind[wall_ad] = 2
+        self.wall_slot = torch.from_numpy(wall_slot).to(dev)
+        self.wall_kind = torch.from_numpy(wall_kind).to(dev)
+        self.wall_nx = torch.from_numpy(np.ascontiguousarray(m.tri_normal[p1_tri, p1_lfc, 0])).to(dev)
+        self.wall_ny = torch.from_numpy(np.ascontiguousarray(m.tri_normal[p1_tri, p1_lfc, 1])).to(dev)
         self.wall_tri = torch.from_numpy(p1_tri[self.wall_all].astype(np.int32)).to(dev)
         self.wall_lfc = torch.from_numpy(p1_lfc[self.wall_all].astype(np.int32)).to(dev)
-        wnx = m.tri_normal[p1_tri[wall_ad], p1_lfc[wall_ad], 0]
-        wny = m.tri_normal[p1_tri[wall_ad], p1_lfc[wall_ad], 1]
-        self.ad_nx = torch.from_numpy(wnx).to(dev)
-        self.ad_ny = torch.from_numpy(wny).to(dev)
         self.tri_fc_fc = torch.from_numpy(np.ascontiguousarray(it.int_tri_fc_fc)).to(dev)
-        self.tri_faces = torch.from_numpy(m.tri_faces.astype(np.int64)).to(dev)
+        self.tri_faces = torch.from_numpy(m.tri_faces.astype(np.int32)).to(dev)
         self.tri_hmin = torch.from_numpy(np.ascontiguousarray(m.tri_hmin)).to(dev)
         self.use_hmin = self.variant == "A"
-        self.work = torch.zeros((n, 7 * nd), **f64)
+        self.ops = _lib.GsisOps(
+            n, m.n_faces, nd, nf, 1 if self.variant == "B" else 0, self.n2, int(self.wall_all.size), 0, c.flow.cv,
+            self.inv_t.data_ptr(), self.ba1_t.data_ptr(), self.tri1.data_ptr(), self.ba2_t.data_ptr(),
+            self.slot2.data_ptr(), self.tri2.data_ptr(), self.mirror2.data_ptr(), self.wall_slot.data_ptr(),
+            self.wall_kind.data_ptr(), self.wall_nx.data_ptr(), self.wall_ny.data_ptr(),
+            self.aa_trace_t.data_ptr(), self.tri_faces.data_ptr())
+        self.aa_src = torch.zeros((n, 7 * nd), **f64)
         self.wall_mom = torch.zeros((max(1, self.wall_all.size), nf3), **f64)
-        self.ffa = torch.zeros((nf3, m.n_faces), **f64)
+        self.ffa = torch.zeros((m.n_faces, nf3), **f64)
+        self.u_trace = torch.zeros(m.n_faces * nf3, **f64)
         self.uq = torch.zeros((7 * nd, n), **f64)
+        #: the run's device stop flag (int32 tensor) while a device-stopped
+        #: loop is captured: every launch of the step then returns at once
+        #: once it is set
+        self.done = None
         self.solve_count = 0
 
     def diagnostics(self) -> dict:
@@ -260,56 +297,51 @@ class GSIS:
                 "stabilisation": [float(v) for v in self.st], "defect_omega": 0.0, "defect_every": 1,
                 "defect_anderson": 0, "defect_outer": 0, "defect_norm": 0.0}
 
+    def _done_ptr(self):
+        return None if self.done is None else self.done.data_ptr()
+
     def rhs(self, aa_src: torch.Tensor, vdf: torch.Tensor, stream=None) -> torch.Tensor:
-        """``GlobalSolver.rhs`` (``global_solve.py:131-187``)."""
-        nf = self.nf
-        src_t = aa_src.T                                   # (n, 7nd)
-        ffa = torch.bmm(self.ba1, src_t[self.p1[0]].unsqueeze(-1)).squeeze(-1)   # (n_faces, nf3)
-        if self.sel2.numel():
-            c2 = torch.bmm(self.ba2, src_t[self.p2[0]].unsqueeze(-1)).squeeze(-1)
-            if self.flip2_rows.numel():
-                c2[self.flip2_rows] = c2[self.flip2_rows][:, self.perm]
-            ffa.index_add_(0, self.sel2, c2)
+        """``GlobalSolver.rhs`` (``global_solve.py:131-187``) into ``self.ffa``
+        (n_faces, 3nf): ``aa_src`` is (n_tris, 7nd), element-major."""
+        L = _lib.lib()
+        s = (stream or torch.cuda.current_stream()).cuda_stream
         if self.wall_all.size:
-            s = (stream or torch.cuda.current_stream()).cuda_stream
-            _lib.check(_lib.lib().pbte_wall_trace(self.s.ctx.handle, vdf.data_ptr(), self.tri_fc_fc.data_ptr(),
-                                                  int(self.wall_all.size), self.wall_tri.data_ptr(),
-                                                  self.wall_lfc.data_ptr(), self.wall_mom.data_ptr(), s),
-                       "wall_trace")
-            mom = self.wall_mom
-            cv = self.s.case.flow.cv
-            th = self.wall_idx[:self.n_th]
-            ad = self.wall_idx[self.n_th:]
-            if self.n_th:
-                ffa[th, 0:nf] = mom[:self.n_th, 0:nf] / cv
-                if self.variant == "B":
-                    ffa[th, nf:3 * nf] = mom[:self.n_th, nf:3 * nf]
-            if ad.numel():
-                ffa[ad, 0:nf] = mom[self.n_th:, 0:nf] / cv
-                qxb = mom[self.n_th:, nf:2 * nf]
-                qyb = mom[self.n_th:, 2 * nf:3 * nf]
-                nx = self.ad_nx[:, None]
-                ny = self.ad_ny[:, None]
-                ffa[ad, nf:2 * nf] = qxb * (ny * ny) - qyb * (nx * ny)
-                ffa[ad, 2 * nf:3 * nf] = -qxb * (nx * ny) + qyb * (nx * nx)
-        return ffa                                          # (n_faces, nf3): Fortran-flattened order
+            _lib.check(L.pbte_wall_trace(self.s.ctx.handle, vdf.data_ptr(), self.tri_fc_fc.data_ptr(),
+                                         int(self.wall_all.size), self.wall_tri.data_ptr(),
+                                         self.wall_lfc.data_ptr(), self.wall_mom.data_ptr(), s), "wall_trace")
+        _lib.check(L.pbte_gsis_trace_rhs(ctypes.byref(self.ops), aa_src.data_ptr(), self.wall_mom.data_ptr(),
+                                         self.ffa.data_ptr(), self._done_ptr(), s), "gsis_trace_rhs")
+        return self.ffa
+
+    def trace_solve(self, stream=None) -> torch.Tensor:
+        """The trace unknowns from ``self.ffa`` into ``self.u_trace``."""
+        if isinstance(self.solver, NestedDissectionSolver):
+            self.solver.solve(self.ffa.view(-1), out=self.u_trace, stream=stream, done=self.done)
+        else:
+            self.u_trace.copy_(self.solver.solve(self.ffa.view(-1)))
+        return self.u_trace
+
+    def recover(self, aa_src: torch.Tensor, out: torch.Tensor, stream=None) -> torch.Tensor:
+        """``local_solve`` (``local_solve.py:16-26``): ``out`` (7nd, n_tris)
+        from ``aa_src`` and the current trace unknowns."""
+        s = (stream or torch.cuda.current_stream()).cuda_stream
+        _lib.check(_lib.lib().pbte_gsis_local_recover(ctypes.byref(self.ops), aa_src.data_ptr(),
+                                                      self.u_trace.data_ptr(), out.data_ptr(), self._done_ptr(), s),
+                   "gsis_local_recover")
+        return out
 
     def apply(self, stream=None) -> None:
         s = self.s
         L = _lib.lib()
         st = (stream or torch.cuda.current_stream()).cuda_stream
-        _lib.check(L.pbte_hot_source(s.ctx.handle, s.vdf.data_ptr(), float(self.tc5), self.work.data_ptr(), st),
-                   "hot_source")
-        aa_src = torch.bmm(self.inv_aa_sol, self.work.unsqueeze(-1)).squeeze(-1).T.contiguous()   # (7nd, n)
-        ffa = self.rhs(aa_src, s.vdf, stream)
-        u_trace = self.solver.solve(ffa.reshape(-1)).reshape(-1, 3 * self.nf)                  # (n_faces, nf3)
+        _lib.check(L.pbte_gsis_hot_apply(s.ctx.handle, ctypes.byref(self.ops), s.vdf.data_ptr(), float(self.tc5),
+                                         self.aa_src.data_ptr(), st), "gsis_hot_apply")
+        self.rhs(self.aa_src, s.vdf, stream)
+        self.trace_solve(stream)
         self.solve_count += 1
-        traces = u_trace[self.tri_faces]                                                       # (n, 3, nf3)
-        uq = aa_src.T + torch.einsum("ilpr,ilr->ip", self.aa_trace, traces)
-        self.uq = uq.T.contiguous()
+        self.recover(self.aa_src, self.uq, stream)
         m = s.mom
         _lib.check(L.pbte_correct(s.ctx.handle, s.vdf.data_ptr(), self.uq.data_ptr(), self.tri_hmin.data_ptr(),
                                   float(s.case.flow.tau_thr), int(self.use_hmin), m.ts.data_ptr(),
                                   m.qxs.data_ptr(), m.qys.data_ptr(), m.temp.data_ptr(), m.qx.data_ptr(),
                                   m.qy.data_ptr(), st), "correct")
-        _ = ctypes

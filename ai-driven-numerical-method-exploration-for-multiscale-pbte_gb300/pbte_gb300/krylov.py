@@ -3,16 +3,19 @@
 One outer step is the affine map ``u -> F(u) = T u + g`` on the state ``u``
 (moments, plus the wall emission when there are adiabatic walls); GMRES
 solves ``(I - T) u = g`` with one sweep per product.  The Krylov basis, the
-state and the products live on the device; the map ``F`` (sweep + moments +
-emission) is captured once as a CUDA graph on fixed input/output buffers.
-The Hessenberg column (``j + 2`` numbers) comes to the host each step for the
-Givens rotations, as in the reference.
+state and the products live on the device.
 
-Orthogonalisation is classical Gram-Schmidt applied twice (the reference's
-CGS2), in FP64.  Stopping follows the reference: GMRES to
-``tol * krylov_tol_factor`` (floored at 1e-14 of ``||g||``), a bounded
-extension once under ``tol * 1e-2``, a closing sweep, and convergence
-decided on the true transport residual.  ``iterations`` counts sweeps.
+Each restart cycle runs on the device: per Arnoldi column the product (sweep
++ moments + emission), classical Gram-Schmidt applied twice (the reference's
+CGS2, FP64) and the Givens rotation with the stopping tests -- the target
+residual, the reference's bounded extension once under ``tol * 1e-2``, and
+breakdown -- are launches that honour a device stop state, captured in CUDA
+graphs of ten columns.  The host sees a cycle's end only: it reads the
+triangular factor and residual estimates, updates the iterate and restarts.
+Stopping otherwise follows the reference: GMRES to ``tol *
+krylov_tol_factor`` (floored at 1e-14 of ``||g||``), a closing sweep, and
+convergence decided on the true transport residual.  ``iterations`` counts
+sweeps.
 """
 from __future__ import annotations
 
@@ -199,47 +202,30 @@ class ArnoldiGraphs:
         n = op.n
         dev = op.s.device
         f64 = dict(dtype=torch.float64, device=dev)
-        if m_cap + 1 > 64:
-            raise ValueError("graph-captured Arnoldi supports a basis of at most 63 vectors")
+        if m_cap + 1 > _lib.MAX_BASIS:
+            raise ValueError(f"device GMRES holds a basis of at most {_lib.MAX_BASIS - 1} vectors")
         self.n = n
         self.m_cap = m_cap
         self.dtype = dtype
         self.Q = torch.zeros((m_cap + 1, n), dtype=dtype, device=dev)
         self.w = torch.zeros(n, dtype=dtype, device=dev)
         self.h = torch.zeros(m_cap + 2, **f64)
-        self.scratch = torch.zeros(_lib.CGS2_SCRATCH, **f64)   # block partials and ticket
+        self.scratch = torch.zeros(_lib.cgs2_scratch(m_cap + 1), **f64)   # block partials and ticket
         self.h_host = torch.zeros(m_cap + 2, dtype=torch.float64, pin_memory=True)
         self.g = None if g is None else g.detach().clone()
-        self.graphs = {}
         self.cycle_graphs = None
         self.stream = torch.cuda.Stream(device=dev)
-        self.on_product = None   # called after every product (sweep bookkeeping)
-        #: whole restart cycles on the device when no per-column host
-        #: callback is needed (the mixed path's inner solve)
-        self.device_cycles = True
+        #: a left preconditioner M (a callable on device vectors) makes the
+        #: products M A q; its torch work cannot skip on the device stop
+        #: state, so such a cycle is issued a column at a time
+        self.precond = None
 
     def set_g(self, g: torch.Tensor) -> None:
         self.g.copy_(g)
 
-    def _record(self, j: int, done=None, fill_input: bool = True) -> None:
-        op = self.op
-        n = self.n
-        Qj = self.Q[:j + 1]
-        if fill_input:
-            op.uin[:n].copy_(self.Q[j])
-        op._launch(torch.cuda.current_stream().cuda_stream)
-        L = _lib.lib()
-        fn = L.pbte_arnoldi_column_f32 if self.dtype == torch.float32 else L.pbte_arnoldi_column
-        g = self.g.data_ptr() if self.g is not None else None
-        _lib.check(fn(Qj.data_ptr(), self.Q.stride(0), j + 1, op.uout.data_ptr(), g, self.w.data_ptr(), n,
-                      self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(),
-                      None if done is None else done.data_ptr(),
-                      torch.cuda.current_stream().cuda_stream), "pbte_arnoldi_column")
-
     def __del__(self):
-        bury(*getattr(self, "graphs", {}).values(), *(getattr(self, "cycle_graphs", None) or {}).values())
+        bury(*(getattr(self, "cycle_graphs", None) or {}).values())
 
-    # -- whole restart cycles on the device ----------------------------------
     #: columns per captured chunk of a cycle (the host checks the stop state
     #: after each chunk)
     CHUNK = 10
@@ -259,9 +245,10 @@ class ArnoldiGraphs:
         self.sn = torch.zeros(m, **f64)
         self.gam = torch.zeros(m + 1, **f64)
         self.hist = torch.zeros(m, **f64)
-        self.tol = torch.zeros(1, **f64)
+        self.tol = torch.zeros(2, **f64)             # [target, enough (< 0: no extension rule)]
         self.state = torch.zeros(4, dtype=torch.int32, device=dev)
         self.state_host = torch.zeros(4, dtype=torch.int32, pin_memory=True)
+        self.tol_host = torch.zeros(2, dtype=torch.float64, pin_memory=True)
         self.cycle_graphs = {}
 
     def _cycle_desc(self):
@@ -283,69 +270,103 @@ class ArnoldiGraphs:
             self.R.data_ptr(), self.m_cap, self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(),
             self.tol.data_ptr(), self.state.data_ptr(), self.hist.data_ptr())
 
-    def _record_cycle(self, j0: int, j1: int) -> None:
-        """Columns j0..j1-1: product, CGS2, rotation, next basis vector; all
-        of it skipped once the stop state is set."""
+    def _record_cycle(self, j0: int, j1: int, bounded: bool) -> None:
+        """Columns j0..j1-1: product, CGS2, rotation and stopping tests, next
+        basis vector; all of it skipped on the device once the stop state is
+        set (the state is the context's stop flag meanwhile)."""
         L = _lib.lib()
         s = torch.cuda.current_stream().cuda_stream
-        n, ctx = self.n, self.op.s.ctx.handle
-        if self.native_columns:
+        n, ctx, op = self.n, self.op.s.ctx.handle, self.op
+        if self.native_columns and not bounded and self.precond is None:
             if getattr(self, "_desc", None) is None:
                 self._desc = self._cycle_desc()
             if self._desc is not None:
                 _lib.check(L.pbte_gmres_columns_f32(ctx, ctypes.byref(self._desc), j0, j1, s), "gmres_columns_f32")
                 return
+        g = self.g.data_ptr() if self.g is not None else None
+        ldq = self.Q.stride(0)
         _lib.check(L.pbte_set_done_flag(ctx, self.state.data_ptr()), "set_done_flag")
         try:
             for j in range(j0, j1):
-                self._record(j, done=self.state, fill_input=False)
-                _lib.check(L.pbte_gmres_givens(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap,
-                                               self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(),
-                                               self.tol.data_ptr(), self.state.data_ptr(), self.hist.data_ptr(),
-                                               s), "gmres_givens")
+                op._launch(s)
+                if self.precond is not None:
+                    # w = M (q_j - (F(q_j) - g)), then CGS2 in place
+                    v = self.Q[j] - (op.uout[:n] - (self.g if self.g is not None else 0.0))
+                    self.w.copy_(self.precond(v))
+                    _lib.check(L.pbte_cgs2(self.Q.data_ptr(), ldq, j + 1, self.w.data_ptr(), n, self.h.data_ptr(),
+                                           self.scratch.data_ptr(), self.scratch.numel(), s), "cgs2")
+                    _lib.check(L.pbte_gmres_givens_bounded(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap,
+                                                           self.cs.data_ptr(), self.sn.data_ptr(),
+                                                           self.gam.data_ptr(), self.tol.data_ptr(),
+                                                           self.state.data_ptr(), self.hist.data_ptr(), s),
+                               "gmres_givens_bounded")
+                elif self.dtype == torch.float64:
+                    _lib.check(L.pbte_arnoldi_column_givens(
+                        self.Q.data_ptr(), ldq, j + 1, op.uout.data_ptr(), g, self.w.data_ptr(), n,
+                        self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(), self.R.data_ptr(),
+                        self.m_cap, self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(), self.tol.data_ptr(),
+                        self.state.data_ptr(), self.hist.data_ptr(), int(bounded), s), "arnoldi_column_givens")
+                else:
+                    _lib.check(L.pbte_arnoldi_column_f32(self.Q.data_ptr(), ldq, j + 1, op.uout.data_ptr(), g,
+                                                         self.w.data_ptr(), n, self.h.data_ptr(),
+                                                         self.scratch.data_ptr(), self.scratch.numel(),
+                                                         self.state.data_ptr(), s), "arnoldi_column_f32")
+                    giv = L.pbte_gmres_givens_bounded if bounded else L.pbte_gmres_givens
+                    _lib.check(giv(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap, self.cs.data_ptr(),
+                                   self.sn.data_ptr(), self.gam.data_ptr(), self.tol.data_ptr(),
+                                   self.state.data_ptr(), self.hist.data_ptr(), s), "gmres_givens")
                 nb = L.pbte_gmres_next_basis_f32 if self.dtype == torch.float32 else L.pbte_gmres_next_basis
-                _lib.check(nb(j, self.w.data_ptr(), self.h.data_ptr(), self.Q.data_ptr(), self.Q.stride(0),
-                              self.op.uin.data_ptr(), n, self.state.data_ptr(), s), "gmres_next_basis")
+                if j + 1 < self.m_cap:
+                    _lib.check(nb(j, self.w.data_ptr(), self.h.data_ptr(), self.Q.data_ptr(), ldq,
+                                  op.uin.data_ptr(), n, self.state.data_ptr(), s), "gmres_next_basis")
         finally:
             _lib.check(L.pbte_set_done_flag(ctx, None), "set_done_flag")
 
-    def _chunk(self, j0: int, j1: int):
-        key = (j0, j1)
+    def _chunk(self, j0: int, j1: int, bounded: bool):
+        key = (j0, j1, bounded)
         if key not in self.cycle_graphs:
-            if uses_graphs(self.op.s):
+            if uses_graphs(self.op.s) and self.precond is None:
                 with device_lock:
                     empty_graveyard()
                     torch.cuda.synchronize(self.op.s.device)
                     gr = torch.cuda.CUDAGraph()
                     with torch.cuda.graph(gr, stream=self.stream, capture_error_mode="thread_local"):
-                        self._record_cycle(j0, j1)
+                        self._record_cycle(j0, j1, bounded)
                 self.cycle_graphs[key] = gr
             else:
                 return None
         return self.cycle_graphs[key]
 
-    def cycle(self, r: torch.Tensor, beta: float, m: int, tol_abs: float):
+    def cycle(self, r: torch.Tensor, beta: float, m: int, tol_abs: float, rule=None):
         """One restart cycle of at most ``m`` columns from the residual ``r``
         (norm ``beta``), stopping on the device when the residual estimate
-        reaches ``tol_abs`` or on breakdown.  Returns ``(k, state, R, gam,
-        hist)`` on the host: columns done, stop state (0 none, 1 converged,
-        2 breakdown), the k x k triangular factor, the k + 1 residual
-        estimates and the k residual norms."""
+        reaches ``tol_abs``, on breakdown, or -- with ``rule = (enough,
+        products_before, reached)`` -- by pybte's bounded extension.
+        Returns ``(k, stop, R, gam, hist, reached)`` on the host: columns done,
+        stop state (0 none, 1 converged, 2 breakdown, 3 halted), the k x k
+        triangular factor, the k + 1 residual estimates, the k residual norms
+        and the extension's first product under ``enough`` (-1: none)."""
         self._cycle_buffers()
         n = self.n
+        bounded = rule is not None
         torch.div(r, beta, out=self.Q[0])
         self.op.uin[:n].copy_(self.Q[0])
         self.gam.zero_()
         self.gam[0] = beta
-        self.tol.fill_(tol_abs)
-        self.state.zero_()
-        for j0 in range(0, m, self.CHUNK):
-            j1 = min(m, j0 + self.CHUNK)
-            g = self._chunk(j0, j1)
+        self.tol_host[0] = tol_abs
+        self.tol_host[1] = rule[0] if bounded else -1.0
+        self.tol.copy_(self.tol_host, non_blocking=True)
+        self.state_host.copy_(torch.tensor([0, 0, rule[1] if bounded else 0, rule[2] if bounded else -1],
+                                           dtype=torch.int32))
+        self.state.copy_(self.state_host, non_blocking=True)
+        step = 1 if self.precond is not None else self.CHUNK
+        for j0 in range(0, m, step):
+            j1 = min(m, j0 + step)
+            g = self._chunk(j0, j1, bounded)
             if g is not None:
                 g.replay()
             else:
-                self._record_cycle(j0, j1)
+                self._record_cycle(j0, j1, bounded)
             self.state_host.copy_(self.state, non_blocking=True)
             torch.cuda.current_stream().synchronize()
             if int(self.state_host[0]) != 0:
@@ -355,45 +376,18 @@ class ArnoldiGraphs:
         gam = self.gam[:k + 1].cpu().numpy()
         hist = self.hist[:k].cpu().numpy()
         self.op.sweeps += k
-        if self.on_product is not None:
-            for _ in range(k):
-                self.on_product()
-        return k, int(self.state_host[0]), R, gam, hist
-
-    def _capture(self, j: int) -> None:
-        with device_lock:
-            empty_graveyard()
-            torch.cuda.synchronize(self.op.s.device)
-            gr = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(gr, stream=self.stream, capture_error_mode="thread_local"):
-                self._record(j)
-        self.graphs[j] = gr
+        return k, int(self.state_host[0]), R, gam, hist, int(self.state_host[3])
 
     def capture_all(self) -> None:
-        """Capture every column's graph now (capturing synchronises the
-        device, which concurrent solves should not meet mid-run): the
-        per-column graphs and the chunks of a full device cycle."""
-        for j in range(self.m_cap):
-            if j not in self.graphs:
-                self._capture(j)
-        if self.device_cycles:
-            self._cycle_buffers()
-            for j0 in range(0, self.m_cap, self.CHUNK):
-                self._chunk(j0, min(self.m_cap, j0 + self.CHUNK))
-
-    def column(self, j: int) -> np.ndarray:
-        if uses_graphs(self.op.s):
-            if j not in self.graphs:
-                self._capture(j)
-            self.graphs[j].replay()
-        else:
-            self._record(j)
-        self.h_host[:j + 2].copy_(self.h[:j + 2], non_blocking=True)
-        torch.cuda.current_stream().synchronize()
-        self.op.sweeps += 1
-        if self.on_product is not None:
-            self.on_product()
-        return self.h_host[:j + 2].numpy().copy()
+        """Capture every chunk of a full device cycle now (capturing
+        synchronises the device, which concurrent solves should not meet
+        mid-run)."""
+        self._cycle_buffers()
+        # the FP64 solver's cycles carry the bounded extension, the mixed
+        # solver's inner (FP32-product) cycles do not
+        bounded = self.op.precision == "fp64"
+        for j0 in range(0, self.m_cap, self.CHUNK):
+            self._chunk(j0, min(self.m_cap, j0 + self.CHUNK), bounded)
 
 
 class MomentPreconditioner:
@@ -403,219 +397,123 @@ class MomentPreconditioner:
     trace system is solved (with the wall traces of a zero distribution) and
     whose recovered ``T, q_x, q_y`` replace them; the rest of the vector
     passes through.  pybte notes it helps in the diffusive limit and hurts in
-    the ballistic one, and leaves it off by default."""
+    the ballistic one, and leaves it off by default.  The element solves,
+    the trace right-hand side and the recovery are the GSIS step's kernels."""
 
-    def __init__(self, solver, acc, sign: float = -1.0, blocks=(0, 1, 2)):
+    def __init__(self, solver, acc, sign: float = -1.0):
         self.s = solver
         self.acc = acc
         self.nd, self.nt = solver.ndof, solver.n_tris
         self.k = self.nd * self.nt
         self.sign = sign
-        self.blocks = blocks
         self.calls = 0
+        f64 = dict(dtype=torch.float64, device=solver.device)
         self.zero_vdf = torch.zeros_like(solver.vdf)
-        self.work = torch.zeros((self.nt, 7 * self.nd), dtype=torch.float64, device=solver.device)
+        self.work = torch.zeros((self.nt, 7 * self.nd), **f64)
+        self.src = torch.zeros((self.nt, 7 * self.nd), **f64)
+        self.uq = torch.zeros((7 * self.nd, self.nt), **f64)
 
     def __call__(self, r: torch.Tensor) -> torch.Tensor:
         a, nd, nt, k = self.acc, self.nd, self.nt, self.k
-        self.work.zero_()
-        for slot, blk in enumerate(self.blocks):
-            if blk is not None:
-                self.work[:, blk * nd:(blk + 1) * nd] = self.sign * r[slot * k:(slot + 1) * k].view(nd, nt).T
-        aa_src = torch.bmm(a.inv_aa_sol, self.work.unsqueeze(-1)).squeeze(-1).T.contiguous()   # (7nd, n)
-        ffa = a.rhs(aa_src, self.zero_vdf)
-        u_trace = a.solver.solve(ffa.reshape(-1)).reshape(-1, 3 * a.nf)
-        uq = aa_src.T + torch.einsum("ilpr,ilr->ip", a.aa_trace, u_trace[a.tri_faces])              # (n, 7nd)
+        s = torch.cuda.current_stream().cuda_stream
+        # rows 0..2 of each element's local source: T, q_x, q_y of the residual
+        self.work[:, :3 * nd].copy_((self.sign * r[:3 * k]).view(3 * nd, nt).T)
+        _lib.check(_lib.lib().pbte_gsis_apply_inverse(ctypes.byref(a.ops), self.work.data_ptr(), 0, 3 * nd,
+                                                      self.src.data_ptr(), None, s), "gsis_apply_inverse")
+        a.rhs(self.src, self.zero_vdf)
+        a.trace_solve()
+        a.recover(self.src, self.uq)
         out = r.clone()
-        out[:3 * k] = uq.T[:3 * nd].reshape(-1)
+        out[:3 * k] = self.uq[:3 * nd].reshape(-1)
         self.calls += 1
         return out
 
 
-def _back_substitute(r, y):
-    out = np.array(y, dtype=float)
-    for i in range(out.size - 1, -1, -1):
-        s = out[i] - r[i, i + 1:] @ out[i + 1:]
-        out[i] = s / r[i, i] if r[i, i] != 0.0 else 0.0
-    return out
+def _solve_upper(rmat: np.ndarray, rhs: np.ndarray) -> np.ndarray:
+    """``y`` with ``R y = rhs`` for the upper-triangular cycle factor, rows
+    from the last up; a zero diagonal gives a zero component (pybte's
+    ``_back_substitute``, ``krylov.py:142-147``, the same operation order)."""
+    y = np.array(rhs, dtype=float)
+    for i in range(y.size - 1, -1, -1):
+        t = y[i] - rmat[i, i + 1:] @ y[i + 1:]
+        y[i] = t / rmat[i, i] if rmat[i, i] != 0.0 else 0.0
+    return y
 
 
-def gmres(matvec, b: torch.Tensor, x0=None, tol_abs: float = 0.0, maxiter=None, max_basis=None,
-          callback=None, arnoldi: ArnoldiGraphs | None = None, precond=None):
-    """GMRES for ``A x = b`` with device vectors (``pybte/krylov.py:150-246``).
-    With ``arnoldi`` (graphs of ``A`` for the same operator) each product and
-    its orthogonalisation is one graph replay.  ``precond``: a left
-    preconditioner ``M`` (the residuals and products are ``M (b - A x)`` and
-    ``M A q``, as pybte's); it takes the host-driven loop.  Returns
-    ``(x, converged, n_matvec)``."""
-    n = b.numel()
+class Extension:
+    """The stopping rule ``run_krylov`` wraps around GMRES
+    (``pybte/krylov.py:332-338``): after the first product whose residual is
+    under ``enough``, at most ``max(64, reached // 4)`` more products.
+    ``count`` is the index of the latest product among the run's products;
+    the device applies the same rule inside a cycle
+    (``pbte_gmres_givens_bounded``)."""
+
+    def __init__(self, enough: float, count: int):
+        self.enough = enough
+        self.count = count
+        self.reached = -1
+
+    def observe(self, res: float) -> bool:
+        """One more product with residual ``res``; True: halt."""
+        self.count += 1
+        if self.reached < 0 and res <= self.enough:
+            self.reached = self.count
+        return self.reached >= 0 and self.count - self.reached > max(64, self.reached // 4)
+
+
+def gmres(matvec, b: torch.Tensor, arnoldi: ArnoldiGraphs, x0=None, tol_abs: float = 0.0, maxiter=None,
+          rule: Extension | None = None, on_products=None):
+    """Restarted GMRES for ``A x = b`` (``pybte/krylov.py:150-246``) with its
+    restart cycles on the device (:meth:`ArnoldiGraphs.cycle`, basis of at
+    most ``arnoldi.m_cap`` vectors).  The host forms each restart's residual
+    ``b - A x`` (one product, through ``matvec``; with ``arnoldi.precond`` M
+    its ``M (b - A x)``), runs a cycle and adds the cycle's correction
+    ``Q_k y`` with ``R y = gam``.  ``rule``: the bounded extension, applied to
+    the restart residuals here and to the cycle's columns on the device.
+    ``on_products(residuals)``: the residual norms of the products just done,
+    in order (a restart's residual, then a cycle's columns).  Returns ``(x,
+    converged, products)``."""
+    ar = arnoldi
     x = torch.zeros_like(b) if x0 is None else x0.clone()
-    maxiter = int(n if maxiter is None else maxiter)
-    m_cap = maxiter if max_basis is None else max(1, min(int(max_basis), maxiter))
-    if arnoldi is not None and m_cap <= arnoldi.m_cap and precond is None:
-        return _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, arnoldi)
-    apply_m = (lambda v: v) if precond is None else precond
-    nmv = 0
-    converged = halted = False
-    while nmv < maxiter and not converged and not halted:
-        if bool(torch.any(x != 0).item()):
-            r = apply_m(b - matvec(x))
-            nmv += 1
-            if callback is not None and callback(float(torch.linalg.vector_norm(r).item())):
-                halted = True
-                break
-        else:
-            r = apply_m(b.clone())
-        beta = float(torch.linalg.vector_norm(r).item())
-        if beta <= tol_abs:
-            converged = True
-            break
-        m = min(m_cap, maxiter - nmv)
-        if m <= 0:
-            break
-        q = torch.empty((min(m, 64), n), dtype=b.dtype, device=b.device)
-        q[0] = r / beta
-        cols, cs, sn, gam = [], [], [], [beta]
-        for j in range(m):
-            w = apply_m(matvec(q[j]))
-            nmv += 1
-            qj = q[:j + 1]
-            c1 = qj @ w
-            w -= qj.T @ c1
-            c2 = qj @ w
-            w -= qj.T @ c2
-            hcol = torch.cat([c1 + c2, torch.linalg.vector_norm(w).reshape(1)]).cpu().numpy()
-            col = np.array(hcol, dtype=float)
-            hn = float(col[j + 1])
-            for i in range(j):
-                t = cs[i] * col[i] + sn[i] * col[i + 1]
-                col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1]
-                col[i] = t
-            d = float(np.hypot(col[j], col[j + 1]))
-            c_, s_ = (1.0, 0.0) if d == 0.0 else (col[j] / d, col[j + 1] / d)
-            cs.append(c_)
-            sn.append(s_)
-            col[j] = d
-            cols.append(col[:j + 1].copy())
-            gam.append(-s_ * gam[j])
-            gam[j] = c_ * gam[j]
-            res = abs(gam[j + 1])
-            stop = bool(callback(res)) if callback is not None else False
-            if res <= tol_abs:
-                converged = True
-                break
-            if stop:
-                halted = True
-                break
-            if hn == 0.0:
-                break
-            if j + 1 < m:
-                if j + 1 >= q.shape[0]:
-                    grown = torch.empty((min(m, max(2 * q.shape[0], j + 2)), n), dtype=b.dtype, device=b.device)
-                    grown[:j + 1] = q[:j + 1]
-                    q = grown
-                q[j + 1] = w / hn
-        k = len(cols)
-        if k:
-            rmat = np.zeros((k, k))
-            for j, col in enumerate(cols):
-                rmat[:j + 1, j] = col
-            y = torch.from_numpy(_back_substitute(rmat, np.asarray(gam[:k]))).to(b.device)
-            x += q[:k].T @ y
-    return x, converged, nmv
-
-
-def _gmres_cycles(matvec, b, x, tol_abs, maxiter, m_cap, ar: ArnoldiGraphs):
-    """The loop of :func:`gmres` with whole restart cycles on the device
-    (:meth:`ArnoldiGraphs.cycle`): the rotations and the stopping test run
-    after each column on the device, the host sees the cycle's end.  Same
-    Krylov arithmetic; the rotations use the device's hypot."""
-    nmv = 0
+    budget = int(b.numel() if maxiter is None else maxiter)
+    pre = ar.precond if ar.precond is not None else (lambda v: v)
+    done = 0
     converged = False
-    while nmv < maxiter and not converged:
+    while done < budget:
         if bool(torch.any(x != 0).item()):
-            r = b - matvec(x)
-            nmv += 1
+            r = pre(b - matvec(x))
+            done += 1
+            beta = float(torch.linalg.vector_norm(r).item())
+            if on_products is not None:
+                on_products([beta])
+            if rule is not None and rule.observe(beta):
+                break
         else:
-            r = b.clone()
-        beta = float(torch.linalg.vector_norm(r).item())
+            r = pre(b.clone())
+            beta = float(torch.linalg.vector_norm(r).item())
         if beta <= tol_abs:
             converged = True
             break
-        m = min(m_cap, maxiter - nmv)
+        m = min(ar.m_cap, budget - done)
         if m <= 0:
             break
-        k, state, rmat, gam, _ = ar.cycle(r, beta, m, tol_abs)
-        nmv += k
-        converged = state == 1
+        k, stop, rmat, gam, hist, reached = ar.cycle(
+            r, beta, m, tol_abs, None if rule is None else (rule.enough, rule.count, rule.reached))
+        done += k
+        if rule is not None:
+            rule.count += k
+            rule.reached = reached
+        if on_products is not None and k:
+            on_products(list(hist))
         if k:
-            y = torch.from_numpy(_back_substitute(rmat, gam[:k])).to(device=b.device, dtype=ar.Q.dtype)
-            x += ar.Q[:k].T @ y
-    return x, converged, nmv
-
-
-def _gmres_graphs(matvec, b, x, tol_abs, maxiter, m_cap, callback, ar: ArnoldiGraphs):
-    """The loop of :func:`gmres` with the basis in ``ar.Q`` and every Arnoldi
-    column from one graph replay; same arithmetic, same stopping."""
-    if callback is None and ar.device_cycles:
-        return _gmres_cycles(matvec, b, x, tol_abs, maxiter, m_cap, ar)
-    nmv = 0
-    converged = halted = False
-    Q = ar.Q
-    while nmv < maxiter and not converged and not halted:
-        if bool(torch.any(x != 0).item()):
-            r = b - matvec(x)
-            nmv += 1
-            if callback is not None and callback(float(torch.linalg.vector_norm(r).item())):
-                halted = True
-                break
-        else:
-            r = b.clone()
-        beta = float(torch.linalg.vector_norm(r).item())
-        if beta <= tol_abs:
+            y = torch.from_numpy(_solve_upper(rmat, gam[:k])).to(device=b.device, dtype=ar.Q.dtype)
+            x += (ar.Q[:k].T @ y).to(x.dtype)
+        if stop == 1:
             converged = True
             break
-        m = min(m_cap, maxiter - nmv)
-        if m <= 0:
+        if stop == 3:
             break
-        Q[0].copy_(r / beta)
-        cols, cs, sn, gam = [], [], [], [beta]
-        for j in range(m):
-            col = ar.column(j)
-            nmv += 1
-            hn = float(col[j + 1])
-            for i in range(j):
-                t = cs[i] * col[i] + sn[i] * col[i + 1]
-                col[i + 1] = -sn[i] * col[i] + cs[i] * col[i + 1]
-                col[i] = t
-            d = float(np.hypot(col[j], col[j + 1]))
-            c_, s_ = (1.0, 0.0) if d == 0.0 else (col[j] / d, col[j + 1] / d)
-            cs.append(c_)
-            sn.append(s_)
-            col[j] = d
-            cols.append(col[:j + 1].copy())
-            gam.append(-s_ * gam[j])
-            gam[j] = c_ * gam[j]
-            res = abs(gam[j + 1])
-            stop = bool(callback(res)) if callback is not None else False
-            if res <= tol_abs:
-                converged = True
-                break
-            if stop:
-                halted = True
-                break
-            if hn == 0.0:
-                break
-            if j + 1 < m:
-                torch.div(ar.w, hn, out=Q[j + 1])
-        k = len(cols)
-        if k:
-            rmat = np.zeros((k, k))
-            for j, col in enumerate(cols):
-                rmat[:j + 1, j] = col
-            y = torch.from_numpy(_back_substitute(rmat, np.asarray(gam[:k]))).to(device=b.device, dtype=Q.dtype)
-            x += Q[:k].T @ y
-    return x, converged, nmv
+    return x, converged, done
 
 
 def cached(solver, key, make):
@@ -631,6 +529,13 @@ def cached(solver, key, make):
 
 
 def basis_cap(case, n: int) -> int:
+    """pybte's Krylov dimension (``krylov.py:249-251``: ``krylov_restart``,
+    else what ``krylov_max_bytes`` holds, at least 32 and at most ``tmax``),
+    held to the device basis limit (``PBTE_MAX_BASIS - 1`` vectors)."""
+    return min(requested_basis(case, n), _lib.MAX_BASIS - 1)
+
+
+def requested_basis(case, n: int) -> int:
     if case.scheme.krylov_restart is not None:
         return int(case.scheme.krylov_restart)
     per = max(1.0, 8.0 * float(n))
@@ -639,93 +544,73 @@ def basis_cap(case, n: int) -> int:
 
 def run_krylov(solver, callback=None, progress_every: int = 0):
     """``pybte/krylov.py:257-363`` on the device.  ``callback(step,
-    residual, solver)`` and progress lines follow every residual the host
-    sees (each product's GMRES residual, the closing true residual); a
+    residual, solver)`` and progress lines follow every residual, in order;
+    the products of a restart cycle are reported when the cycle ends.  A
     restarted solver starts GMRES from its loaded state."""
     c = solver.case
     tol, tmax = c.iteration.tol, c.iteration.tmax
     want_true = c.iteration.true_residual
     op = cached(solver, "fp64", lambda: FixedPointOperator(solver))
     op.sweeps = 0
-    residuals, masses, true_res = [], [], []
+    residuals, true_res = [], []
 
-    def sweep(u):
-        out = op.apply(u)
-        product()
-        return out
-
-    def product():
-        masses.append(np.nan)
-        residuals.append(np.nan)
-        if want_true:
-            true_res.append(np.nan)
-
-    def close(res):
-        residuals[-1] = res
-        step = len(residuals)
-        if progress_every and step % progress_every == 0:
-            print(f"  step {step:8d}  residual {res:.6e}", flush=True)
-        if callback is not None:
-            callback(step, res, solver)
+    def report(values):
+        for v in values:
+            residuals.append(v)
+            if want_true:
+                true_res.append(np.nan)
+            step = len(residuals)
+            if progress_every and step % progress_every == 0:
+                print(f"  step {step:8d}  residual {v:.6e}", flush=True)
+            if callback is not None:
+                callback(step, v, solver)
 
     sync(solver.device)
     t0 = time.perf_counter()
     restarted = bool(solver.restart_info.get("enabled")) if hasattr(solver, "restart_info") else False
     x = op.state() if restarted else torch.zeros(op.n, dtype=torch.float64, device=solver.device)
-    zero = torch.zeros(op.n, dtype=torch.float64, device=solver.device)
-    g = sweep(zero)
+    g = op.apply(torch.zeros(op.n, dtype=torch.float64, device=solver.device))
     gnorm = float(torch.linalg.vector_norm(g).item())
     scale = gnorm or 1.0
-    close(1.0)
+    report([1.0])
 
     def matvec(v):
-        return v - (sweep(v) - g)
+        return v - (op.apply(v) - g)
 
     enough = max(tol * _ENOUGH, _FLOOR) * scale
     target = max(tol * c.scheme.krylov_tol_factor, _FLOOR) * scale
     cap = basis_cap(c, op.n)
-    reached = -1
-
-    def on_residual(res):
-        nonlocal reached
-        close(res / scale)
-        n = len(residuals)
-        if reached < 0 and res <= enough:
-            reached = n
-        return reached >= 0 and n - reached > max(64, reached // 4)
-
+    ar = cached(solver, ("arnoldi64", cap), lambda: ArnoldiGraphs(op, g, cap))
+    ar.set_g(g)
     precond = None
     if c.scheme.krylov_precond and getattr(solver, "acc", None) is not None:
         precond = MomentPreconditioner(solver, solver.acc)
-    ar = (cached(solver, ("arnoldi64", cap), lambda: ArnoldiGraphs(op, g, cap))
-          if cap <= 63 and precond is None else None)
-    if ar is not None:
-        ar.set_g(g)
-        ar.on_product = product
+    ar.precond = precond
     converged = False
     final = float("nan")
     for _ in range(c.scheme.krylov_max_rounds):
         budget = tmax - len(residuals) - 1
         if budget <= 0:
             break
-        reached = -1
-        x, _, _ = gmres(matvec, g, x0=x, tol_abs=target, maxiter=budget, max_basis=cap, callback=on_residual,
-                        arnoldi=ar, precond=precond)
-        sweep(x)
+        x, _, _ = gmres(matvec, g, ar, x0=x, tol_abs=target, maxiter=budget,
+                        rule=Extension(enough, len(residuals)), on_products=lambda v: report([e / scale for e in v]))
+        op.apply(x)                                       # closing sweep
         op.publish()
         final = solver.ctx.true_residual(solver.mom, solver.vdf)
+        report([final])
         if want_true:
             true_res[-1] = final
-        close(final)
         converged = bool(final < tol) if np.isfinite(final) else gnorm == 0.0
         if converged or len(residuals) >= tmax:
             break
         target = max(target * 1.0e-3, _FLOOR * scale)
+    ar.precond = None
     sync(solver.device)
     wall = time.perf_counter() - t0
     solver.ctx.sweep_count += op.sweeps
     masses = [solver.mom.mass] * len(residuals)
     return solver._record(len(residuals), converged, residuals, masses, wall, "KRYLOV",
                           extra={"krylov_size": op.n, "krylov_periodic_state": op.nper, "krylov_basis_cap": cap,
+                                 "krylov_basis_requested": requested_basis(c, op.n),
                                  "krylov_precond": precond is not None, "transport_residual": final},
                           true_res=true_res if want_true else None)

@@ -222,6 +222,49 @@ def _geometry(nodes, tri_nodes):
     return area, normal, hl.min(axis=1), min(1.0, float(hl.min()))
 
 
+def _edge_key(p: np.ndarray) -> list:
+    """Orientation-free keys of edges given by their end points ``p`` (k, 2, 2):
+    the two ends ordered lexicographically, as a tuple of four floats (equal
+    coordinates compare equal, -0.0 included)."""
+    x0, y0, x1, y1 = p[:, 0, 0], p[:, 0, 1], p[:, 1, 0], p[:, 1, 1]
+    keep = (x0 < x1) | ((x0 == x1) & (y0 <= y1))
+    lo = np.where(keep[:, None], p[:, 0], p[:, 1])
+    hi = np.where(keep[:, None], p[:, 1], p[:, 0])
+    return list(map(tuple, np.concatenate([lo, hi], axis=1).tolist()))
+
+
+def _pair_master_slave(nodes, face_nodes, face_bc, bc_names, bc_xoff, bc_yoff) -> np.ndarray:
+    """Periodic partners of the boundaries named ``Master`` and ``Slave``
+    (``pybte/mesh/topology.py:186-209``): a Master face, moved by the Master
+    boundary's offset, pairs with the Slave face that has exactly the same two
+    end points, in either order; the lowest-numbered such Slave face wins.
+    A hash join over orientation-free edge keys, linear in the face count."""
+    n_faces = face_nodes.shape[0]
+    face_pair = np.full(n_faces, -1, dtype=np.int32)
+    names = [str(s).strip() for s in bc_names]
+    if "Master" not in names:
+        return face_pair
+    if "Slave" not in names:
+        raise ValueError("a 'Master' boundary needs a matching 'Slave'")
+    bm, bs = names.index("Master"), names.index("Slave")
+    masters = np.flatnonzero(face_bc == bm)
+    slaves = np.flatnonzero(face_bc == bs)
+    shift = np.array([bc_xoff[bm], bc_yoff[bm]])
+    by_key = {}
+    for s, key in zip(slaves[::-1].tolist(), _edge_key(nodes[face_nodes[slaves[::-1]]])):
+        by_key[key] = s
+    for m, key in zip(masters.tolist(), _edge_key(nodes[face_nodes[masters]] + shift)):
+        s = by_key.get(key)
+        if s is not None:
+            face_pair[m] = s
+            face_pair[s] = m
+    lonely = np.concatenate([masters, slaves])
+    lonely = lonely[face_pair[lonely] < 0]
+    if lonely.size:
+        raise ValueError(f"periodic faces without a partner: {lonely[:8].tolist()}")
+    return face_pair
+
+
 def build_mesh(raw: RawMesh, bc_phyid, bc_codes, bc_names=None,
                bc_xoff=None, bc_yoff=None) -> Mesh:
     """Faces, connectivity, periodic pairing and geometry from a raw mesh."""
@@ -276,29 +319,7 @@ def build_mesh(raw: RawMesh, bc_phyid, bc_codes, bc_names=None,
     other = np.where(face_tri[tri_faces, 0] == ti, face_tri[tri_faces, 1], face_tri[tri_faces, 0])
     tri_neighbour = other.astype(np.int32)
 
-    face_pair = np.full(n_faces, -1, dtype=np.int32)
-    id_master = next((i for i, s in enumerate(bc_names) if str(s).strip() == "Master"), -1)
-    id_slave = next((i for i, s in enumerate(bc_names) if str(s).strip() == "Slave"), -1)
-    if id_master >= 0:
-        if id_slave < 0:
-            raise ValueError("a 'Master' boundary needs a matching 'Slave'")
-        masters = np.flatnonzero(face_bc == id_master)
-        slaves = np.flatnonzero(face_bc == id_slave)
-        off = np.array([bc_xoff[id_master], bc_yoff[id_master]])
-        for m in masters:
-            pa = nodes[face_nodes[m, 0]] + off
-            pb = nodes[face_nodes[m, 1]] + off
-            for s in slaves:
-                pc = nodes[face_nodes[s, 0]]
-                pd = nodes[face_nodes[s, 1]]
-                if (np.array_equal(pa, pc) and np.array_equal(pb, pd)) or \
-                        (np.array_equal(pa, pd) and np.array_equal(pb, pc)):
-                    face_pair[m] = s
-                    face_pair[s] = m
-                    break
-        unpaired = [int(i) for i in np.concatenate([masters, slaves]) if face_pair[i] < 0]
-        if unpaired:
-            raise ValueError(f"unpaired periodic faces: {unpaired[:8]}")
+    face_pair = _pair_master_slave(nodes, face_nodes, face_bc, bc_names, bc_xoff, bc_yoff)
     counter = 0
     for k in np.flatnonzero(face_bc >= 0):
         if bc_codes[face_bc[k]] in (BC_THERMALISING, BC_SYMMETRY):

@@ -84,14 +84,13 @@ def run_mixed(solver, opts: MixedOptions | None = None):
                     break
         else:
             cap = basis_cap(c, n)
-            if ar32 is None and cap <= 63:
+            if ar32 is None:
                 bdt = torch.float32 if c.performance.inner_basis == "fp32" else torch.float64
                 ar32 = cached(solver, ("arnoldi_inner", cap, bdt),
                               lambda: ArnoldiGraphs(op32, None, cap, dtype=bdt))
             before = op32.sweeps
-            d, _, _ = gmres(lambda v: v - op32.apply(v), r, tol_abs=opts.inner_rtol * rn,
-                            maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap), max_basis=cap,
-                            arnoldi=ar32)
+            d, _, _ = gmres(lambda v: v - op32.apply(v), r, ar32, tol_abs=opts.inner_rtol * rn,
+                            maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap))
             inner_sweeps += op32.sweeps - before
         u = u + d
         fu = op64.apply(u)

@@ -39,7 +39,7 @@ from . import _lib
 from .config import Case
 from .device import bury, device_lock, empty_graveyard, sync
 from .discretisation import Discretisation
-from .sweep import Moments, SweepContext
+from .sweep import HostReadable, Moments, SweepContext
 
 __all__ = ["Solver", "RunRecord"]
 
@@ -186,7 +186,7 @@ class Solver:
         self.precision = case.performance.precision
         self.ctx = SweepContext(self.disc, device=device)
         f64 = dict(dtype=torch.float64, device=self.device)
-        self.vdf = torch.zeros((self.ndir, self.n_tris, self.ndof), **f64)
+        self.vdf = torch.zeros((self.ndir, self.n_tris, self.ndof), **f64).as_subclass(HostReadable)
         self.mom = Moments.zeros(self.ndof, self.n_tris, device=self.device)
         self.t_old = torch.zeros(self.n_tris, **f64)
         self._res = torch.zeros(2, **f64)
@@ -316,6 +316,15 @@ class Solver:
             self.acc.apply(stream=stream)
 
     def run(self, callback=None, progress_every: int = 0) -> RunRecord:
+        rec = self._run(callback, progress_every)
+        bad = self.ctx.singular_count(reset=True)
+        if bad:
+            # pybte's on-the-fly sweep would carry the inf/NaN on silently
+            raise np.linalg.LinAlgError(f"{bad} zero pivots in the element operators during the run; "
+                                        "check TAU_C and the mesh")
+        return rec
+
+    def _run(self, callback=None, progress_every: int = 0) -> RunRecord:
         """Solve to ``iteration.tol``.  ``callback(step, residual, solver)``
         after every outer step and ``progress_every`` progress lines, as
         pybte's (``driver.py:164-215``); either one, or
@@ -328,11 +337,18 @@ class Solver:
         if c.scheme.method == "krylov":
             from .krylov import run_krylov
             return run_krylov(self, callback, progress_every)
-        if self.acc is not None or callback is not None or progress_every or c.iteration.true_residual:
-            return self._run_stepwise("GSIS" if self.acc is not None else "CIS", callback, progress_every)
+        stepwise = callback is not None or progress_every or c.iteration.true_residual
+        if self.acc is not None:
+            device_loop = (getattr(self, "use_graphs", True) and c.performance.trace_solver == "device"
+                           and not stepwise)
+            if device_loop:
+                return self._run_source("GSIS")
+            return self._run_stepwise("GSIS", callback, progress_every)
+        if stepwise:
+            return self._run_stepwise("CIS", callback, progress_every)
         return self._run_source()
 
-    # -- CIS, graph-captured ------------------------------------------------
+    # -- CIS and GSIS, graph-captured with a device stop flag ---------------
     def _iteration(self, s: int, tol: float, tmax: int, done, count, hist, cap) -> None:
         L = _lib.lib()
         ctx = self.ctx.handle
@@ -341,14 +357,24 @@ class Solver:
         m = self.mom
         _lib.check(L.pbte_sweep(ctx, m.ts.data_ptr(), m.qxs.data_ptr(), m.qys.data_ptr(), self.vdf.data_ptr(),
                                 self.ctx.flux_wall.data_ptr(), self.ctx.pbuf.data_ptr(), 0, s), "sweep")
-        _lib.check(L.pbte_moments(ctx, self.vdf.data_ptr(), m.ts.data_ptr(), m.qxs.data_ptr(), m.qys.data_ptr(),
-                                  m.temp.data_ptr(), m.qx.data_ptr(), m.qy.data_ptr(), s), "moments")
+        if self.acc is None:
+            _lib.check(L.pbte_moments(ctx, self.vdf.data_ptr(), m.ts.data_ptr(), m.qxs.data_ptr(),
+                                      m.qys.data_ptr(), m.temp.data_ptr(), m.qx.data_ptr(), m.qy.data_ptr(), s),
+                       "moments")
+        else:
+            self.acc.apply()   # on the current (capturing) stream, whose handle is s
         _lib.check(L.pbte_residual_iterate(ctx, m.temp.data_ptr(), self.t_old.data_ptr(),
                                            self._res.data_ptr(), s), "residual")
         _lib.check(L.pbte_residual_check(ctx, self._res.data_ptr(), float(tol), int(tmax), done.data_ptr(),
                                          count.data_ptr(), hist.data_ptr(), int(cap), s), "check")
 
-    def _run_source(self) -> RunRecord:
+    def _run_source(self, scheme: str = "CIS") -> RunRecord:
+        """Blocks of ``graph_block`` iterations (CIS: sweep + moments; GSIS:
+        sweep + the acceleration step) captured as one CUDA graph and replayed
+        until the device stopping rule (pybte's step residual, ``driver.py:
+        187-199``) sets the stop flag: every launch after it returns at once,
+        so the state is the one of the converged iteration.  The host reads
+        the flag once per block."""
         c = self.case
         tol, tmax = c.iteration.tol, c.iteration.tmax
         dev = self.device
@@ -358,7 +384,9 @@ class Solver:
         hist = torch.zeros(2 * cap, dtype=torch.float64, device=dev)
         L = _lib.lib()
         _lib.check(L.pbte_set_done_flag(self.ctx.handle, done.data_ptr()), "set_done_flag")
-        K = max(1, min(self.graph_block, int(tmax)))
+        if self.acc is not None:
+            self.acc.done = done
+        K = max(1, min(self.graph_block if self.acc is None else max(1, self.graph_block // 2), int(tmax)))
         stream = torch.cuda.Stream(device=dev)
         sync(dev)
         t0 = time.perf_counter()
@@ -377,14 +405,19 @@ class Solver:
                     break
         finally:
             _lib.check(L.pbte_set_done_flag(self.ctx.handle, None), "set_done_flag")
+            if self.acc is not None:
+                self.acc.done = None
             bury(g)
         sync(dev)
         wall = time.perf_counter() - t0
         n = int(count.item())
         flag = int(done.item())
         self.ctx.sweep_count += n
+        if self.acc is not None:
+            # counted once per captured step at capture time, where nothing ran
+            self.acc.solve_count += n - K
         h = hist[:2 * min(n, cap)].cpu().numpy().reshape(-1, 2)
-        return self._record(n, flag == 1, h[:, 0], h[:, 1], wall, "CIS")
+        return self._record(n, flag == 1, h[:, 0], h[:, 1], wall, scheme)
 
     # -- host-driven loop (GSIS and debugging) -------------------------------
     def _run_stepwise(self, scheme: str, callback=None, progress_every: int = 0) -> RunRecord:

@@ -23,7 +23,34 @@ from . import _lib
 from .device import device_lock, empty_graveyard
 from .discretisation import Discretisation
 
-__all__ = ["SweepContext", "Moments", "device_ptr"]
+__all__ = ["SweepContext", "Moments", "device_ptr", "SweepCycleError", "HostReadable"]
+
+
+class SweepCycleError(RuntimeError):
+    """A direction's element dependency graph contains a cycle
+    (``pybte/ordering.py:35``); raised where pybte's default
+    ``on_cycle='raise'`` raises it."""
+
+
+class HostReadable(torch.Tensor):
+    """A device tensor that numpy reads by copying it to the host, so that
+    ``np.asarray(solver.vdf)`` works as it does on pybte's host array (the
+    reference task's verifier saves the distribution that way)."""
+
+    def __array__(self, dtype=None, copy=None):
+        a = torch.Tensor.cpu(self).detach().numpy()
+        return a if dtype is None else a.astype(dtype, copy=False)
+
+
+def _create_status(rc: int, what: str) -> None:
+    """pybte's exceptions for the context's failures: singular element
+    operators raise LinAlgError (``sweep.py:122-128``), a cyclic direction
+    SweepCycleError (``ordering.py:169``)."""
+    if rc == -6:
+        raise np.linalg.LinAlgError("element operators are singular; check TAU_C and the mesh")
+    if rc == -3:
+        raise SweepCycleError("a direction has a cyclic element dependency; the mesh is not sweepable for it")
+    _lib.check(rc, what)
 
 # contexts whose destruction waits for a moment outside graph captures
 _deferred: list = []
@@ -130,8 +157,8 @@ def direction_levels(disc: Discretisation, d: int) -> np.ndarray:
     desc, keep = case_desc(disc)
     out = np.zeros(disc.mesh.n_tris, dtype=np.int32)
     n = ctypes.c_int32()
-    _lib.check(_lib.lib().pbte_direction_levels(ctypes.byref(desc), int(d), out.ctypes.data, ctypes.byref(n)),
-               "pbte_direction_levels")
+    _create_status(_lib.lib().pbte_direction_levels(ctypes.byref(desc), int(d), out.ctypes.data, ctypes.byref(n)),
+                   "pbte_direction_levels")
     del keep
     return out
 
@@ -171,8 +198,8 @@ class SweepContext:
         with device_lock, torch.cuda.device(self.device):
             empty_graveyard()
             _destroy_deferred()
-            _lib.check(_lib.lib().pbte_ctx_create(ctypes.byref(desc), int(precompute),
-                                                  ctypes.byref(handle)), "pbte_ctx_create")
+            _create_status(_lib.lib().pbte_ctx_create(ctypes.byref(desc), int(precompute),
+                                                      ctypes.byref(handle)), "pbte_ctx_create")
         self._ctx = handle
         nlev, ncls, nbytes = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         _lib.check(_lib.lib().pbte_ctx_info(self._ctx, ctypes.byref(nlev), ctypes.byref(ncls),
@@ -235,6 +262,13 @@ class SweepContext:
                                             ctypes.byref(nbytes)), "pbte_ctx_info")
         self.device_bytes = nbytes.value
         self.fp32_factors = True
+
+    def singular_count(self, reset: bool = False) -> int:
+        """Zero pivots met by the element factorisations so far (setup and
+        every sweep that factors on the fly); synchronises the device."""
+        v = ctypes.c_int64()
+        _lib.check(_lib.lib().pbte_singular_count(self._ctx, ctypes.byref(v), int(reset)), "pbte_singular_count")
+        return int(v.value)
 
     def schedule(self) -> dict:
         w, r, u = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()

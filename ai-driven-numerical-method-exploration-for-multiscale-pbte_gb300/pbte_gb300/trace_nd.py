@@ -293,9 +293,10 @@ class NestedDissectionSolver:
             del F
 
     # -- solve -----------------------------------------------------------------
-    def solve(self, b: torch.Tensor, out: torch.Tensor | None = None, stream=None) -> torch.Tensor:
+    def solve(self, b: torch.Tensor, out: torch.Tensor | None = None, stream=None, done=None) -> torch.Tensor:
         """``K^-1 b`` on the device (``b``: float64, n entries); into ``out``
-        when given, else a new tensor."""
+        when given, else a new tensor.  ``done``: an int32 device flag that
+        makes every launch return at once while it is nonzero."""
         if self.device.type != "cuda":
             raise RuntimeError("the trace solve runs on the GPU; there is no CPU fallback")
         L = _lib.lib()
@@ -306,12 +307,14 @@ class NestedDissectionSolver:
             if n_items:
                 _lib.check(L.pbte_nd_forward(items.data_ptr(), n_items, self.meta.data_ptr(), self.idx.data_ptr(),
                                              self.cptr.data_ptr(), self.csrc.data_ptr(), self.Gd.data_ptr(),
-                                             b.data_ptr(), self.z.data_ptr(), self.delta.data_ptr(), fo, s),
+                                             b.data_ptr(), self.z.data_ptr(), self.delta.data_ptr(), fo,
+                                             None if done is None else done.data_ptr(), s),
                            "nd_forward")
         for _, _, _, items, n_items, bm in reversed(self.levels):
             if n_items:
                 _lib.check(L.pbte_nd_backward(items.data_ptr(), n_items, self.meta.data_ptr(), self.idx.data_ptr(),
-                                              self.Hd.data_ptr(), self.z.data_ptr(), x.data_ptr(), bm, s),
+                                              self.Hd.data_ptr(), self.z.data_ptr(), x.data_ptr(), bm,
+                                              None if done is None else done.data_ptr(), s),
                            "nd_backward")
         return x
 

@@ -37,8 +37,13 @@ extern "C" {
 #define PBTE_ERR_SINGULAR (-6)     /* singular element operator(s)           */
 #define PBTE_ERR_NOMEM (-7)        /* device allocation failed               */
 
-/* doubles of scratch a pbte_cgs2 / pbte_arnoldi_column call needs */
-#define PBTE_CGS2_SCRATCH (1220 * 64)
+/* Krylov bases of the device GMRES hold at most PBTE_MAX_BASIS rows; a
+ * pbte_cgs2 / pbte_arnoldi_column call over `rows` basis rows needs
+ * PBTE_CGS2_SCRATCH_ROWS(rows) doubles of scratch (PBTE_CGS2_SCRATCH: up to
+ * 64 rows). */
+#define PBTE_MAX_BASIS 1024
+#define PBTE_CGS2_SCRATCH_ROWS(rows) (8 + 2 * PBTE_MAX_BASIS + 1216 * ((((rows) + 7) / 8) * 8))
+#define PBTE_CGS2_SCRATCH PBTE_CGS2_SCRATCH_ROWS(64)
 
 /* precision of the sweep arithmetic */
 #define PBTE_FP64 0
@@ -122,6 +127,19 @@ int pbte_ctx_schedule(const pbte_ctx *ctx, int64_t *ring_w, int64_t *ring_r,
 int pbte_ctx_info(const pbte_ctx *ctx, int64_t *n_levels_max, int64_t *n_classes,
                   int64_t *device_bytes);
 
+/* Zero pivots met by the context's element factorisations so far (setup and
+ * every on-the-fly sweep); reset != 0 sets the count back to zero.  pybte's
+ * precomputed mode raises LinAlgError for these at setup (sweep.py:122-128);
+ * in its on-the-fly mode a singular operator yields inf/NaN silently.
+ * Synchronises with the device. */
+int pbte_singular_count(pbte_ctx *ctx, int64_t *count, int reset);
+
+/* Device bytes held by all live contexts of this process (the sum of their
+ * pbte_ctx_info device_bytes).  No reference counterpart: a serving loop's
+ * admission check, and evidence that failed context creation frees what it
+ * allocated. */
+int pbte_device_bytes_live(int64_t *bytes);
+
 /* One FP64 transport sweep, in place on vdf.  Replaces SweepContext.sweep
  * (pybte/sweep.py:132-158 -> _kernels.sweep_precomputed/_onthefly,
  * pybte/_kernels.py:218-269).  `pbuf`/`use_pbuf` as in the reference
@@ -203,18 +221,20 @@ int pbte_transport_residual(pbte_ctx *ctx, const double *ts, const double *qxs,
                             const double *pbuf, double *num, double *den, void *stream);
 
 /* The same transport residual for callers that cannot allocate device memory
- * where they call from (code running while a CUDA graph is captured in global
- * capture mode, where cudaMalloc is illegal; hosts whose device memory belongs
- * to their own pool) or that must leave the context's scratch to a sweep in
+ * where they call from (hosts whose device memory is handed out by their own
+ * pool, where a cudaMalloc behind the pool's back fails or breaks its
+ * accounting) or that must leave the context's scratch to a sweep in
  * flight.  It allocates nothing: the moment sources go to a static 4 MiB
  * device array (524288 doubles) held by every GPU that loads the library
  * until exit, so 3 * ndof * n_tris must be <= 524288 (else PBTE_ERR_ARG).
  * The first call on a device looks the array up (cudaGetSymbolAddress, with
  * that device current), which under lazy module loading is also when the
  * runtime commits the array's memory: make that first call before any
- * stream capture starts; later calls change no device memory.  All calls
+ * stream capture starts.  All calls
  * share the array, so calls that overlap on the GPU race; no state carries
- * from one call to the next.  Periodic faces: PBTE_ERR_UNSUPPORTED.
+ * from one call to the next.  Periodic faces: PBTE_ERR_UNSUPPORTED.  Call
+ * it with the context's device current (the device current at
+ * pbte_ctx_create): another device gives PBTE_ERR_ARG.
  * No counterpart in the reference. */
 int pbte_transport_residual_noalloc(pbte_ctx *ctx, const double *ts, const double *qxs,
                                     const double *qys, const double *vdf,
@@ -238,10 +258,10 @@ int pbte_residual_check(pbte_ctx *ctx, const double *res, double tol, int64_t tm
  * (row stride ldq elements), in place on w, as in gmres_full
  * (pybte/krylov.py:201-210): h[0..rows-1] = c1 + c2 and h[rows] = ||w||.
  * Deterministic (block partial sums added in a fixed order).  `scratch`
- * holds scratch_len >= PBTE_CGS2_SCRATCH doubles (PBTE_ERR_ARG otherwise),
- * all zero before its first use; a call leaves it ready for the next one,
- * and concurrent calls need separate scratch.
- * rows <= 64.  pbte_cgs2 keeps the basis and w in FP64; pbte_cgs2_f32 keeps
+ * holds scratch_len >= PBTE_CGS2_SCRATCH_ROWS(rows) doubles (PBTE_ERR_ARG
+ * otherwise), all zero before its first use; a call leaves it ready for the
+ * next one (for any row count), and concurrent calls need separate scratch.
+ * rows <= PBTE_MAX_BASIS.  pbte_cgs2 keeps the basis and w in FP64; pbte_cgs2_f32 keeps
  * them in FP32 (FP32 products and warp sums, FP64 block and cross-block
  * sums; no reference counterpart: the inner solve of the mixed-precision
  * mode, whose operator is an FP32 sweep). */
@@ -273,9 +293,27 @@ int pbte_arnoldi_column_f32(const float *Q, int64_t ldq, int32_t rows, const dou
  * any tolerance), 2 on breakdown (h[j+1] == 0); state[1] =
  * columns done.  pbte_gmres_next_basis(_f32) stores q_{j+1} = w / h[j+1] in
  * row j+1 of Q and widened into the operator input uin[0..n).  Both do
- * nothing while state[0] != 0; j + 1 < 64. */
+ * nothing while state[0] != 0; j + 1 < PBTE_MAX_BASIS.
+ *
+ * pbte_gmres_givens_bounded adds the stopping rule run_krylov wraps around
+ * gmres_full (pybte/krylov.py:332-338): tol2 = [tol_abs, enough] and state
+ * = [stop, columns, products before this cycle, reached (-1: none)].  The
+ * first product (index n = state[2] + j + 1 among the run's products) whose
+ * residual is <= enough sets state[3] = n; once n - state[3] > max(64,
+ * state[3] / 4) the solve halts with state[0] = 3.  Precedence as
+ * gmres_full: converged (1), halted (3), breakdown (2).
+ * pbte_arnoldi_column_givens is pbte_arnoldi_column (FP64, done = state)
+ * with that rotation (bounded != 0: the bounded form) run by the last block
+ * of its norm pass. */
 int pbte_gmres_givens(int32_t j, const double *h, double *R, int32_t ldr, double *cs, double *sn,
                       double *gam, const double *tol_abs, int32_t *state, double *hist, void *stream);
+int pbte_gmres_givens_bounded(int32_t j, const double *h, double *R, int32_t ldr, double *cs, double *sn,
+                              double *gam, const double *tol2, int32_t *state, double *hist, void *stream);
+int pbte_arnoldi_column_givens(const double *Q, int64_t ldq, int32_t rows, const double *uout,
+                               const double *g, double *w, int64_t n, double *h, double *scratch,
+                               int64_t scratch_len, double *R, int32_t ldr, double *cs, double *sn,
+                               double *gam, const double *tol2, int32_t *state, double *hist,
+                               int32_t bounded, void *stream);
 int pbte_gmres_next_basis(int32_t j, const double *w, const double *h, double *Q, int64_t ldq,
                           double *uin, int64_t n, const int32_t *state, void *stream);
 int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float *Q, int64_t ldq,
@@ -297,7 +335,7 @@ int pbte_gmres_next_basis_f32(int32_t j, const float *w, const double *h, float 
  * first 3 * ndof * n_tris entries of uin in that order (the Krylov state),
  * the basis update of column j also forms column j+1's moment sources
  * (the same FP64 arithmetic), so only the call's first product launches
- * them.  0 <= j0 < j1, j1 + 1 <= rows of Q, j1 < 64. */
+ * them.  0 <= j0 < j1, j1 + 1 <= rows of Q, j1 < PBTE_MAX_BASIS. */
 typedef struct {
     const double *ts, *qxs, *qys, *flux_wall_in;   /* operator input: views of uin */
     double wall_scale;
@@ -332,6 +370,58 @@ int pbte_correct(pbte_ctx *ctx, double *vdf, const double *uq, const double *tri
                  double tau_thr, int use_hmin, double *ts, double *qxs, double *qys,
                  double *temp, double *qx, double *qy, void *stream);
 
+/* GSIS static condensation per iteration, on operator layouts made once at
+ * setup (pbte_gb300/gsis.py), field-major so that consecutive threads read
+ * consecutive addresses.  M = 7*ndof local unknowns per element, NF3 =
+ * 3*ndof_fc trace unknowns per face.
+ *   inv_t[(q*n_tris + i)*M + p]           = inv(AA_SOL_i)[p][q]
+ *                                           (assembly.py:100, build_local_operators)
+ *   ba1_t[(p*n_faces + f)*NF3 + r]        = BA_SOL[tri1[f], lfc][r][p] (assembly.py:128-184)
+ *   ba2_t[(p*n2 + k)*NF3 + r]             = the same for the second element of the
+ *                                           faces with slot2[f] = k >= 0 (tri2[k];
+ *                                           mirror2[k] != 0: a periodic pair walked the
+ *                                           same way, rows reversed within each block of
+ *                                           ndof_fc, global_solve.py:151-157)
+ *   aa_trace_t[((il*NF3 + r)*n_tris + i)*M + p] = AA_TRACE_i[il][p][r]
+ *   wall_slot[f]: row of the kinetic wall moments (pbte_wall_trace output) or -1;
+ *   wall_kind[f]: 1 thermalising, 2 diffuse adiabatic; wall_nx/ny: the wall
+ *   element's outward normal on the face.  variant: 0 = A, 1 = B. */
+typedef struct pbte_gsis_ops {
+    int32_t n_tris, n_faces, ndof, ndof_fc, variant, n2, n_walls, pad;
+    double cv;
+    const double *inv_t;
+    const double *ba1_t;
+    const int32_t *tri1;
+    const double *ba2_t;
+    const int32_t *slot2;
+    const int32_t *tri2;
+    const int32_t *mirror2;
+    const int32_t *wall_slot;
+    const int32_t *wall_kind;
+    const double *wall_nx, *wall_ny;
+    const double *aa_trace_t;
+    const int32_t *tri_faces;
+} pbte_gsis_ops;
+
+/* hot_source (acceleration/hot_source.py:29-75) including its inv_aa_sol @ work:
+ * aa_src[i][p] (n_tris x 7*ndof) from the distribution.  The context's
+ * stop flag (pbte_set_done_flag) makes it return at once. */
+int pbte_gsis_hot_apply(pbte_ctx *ctx, const pbte_gsis_ops *ops, const double *vdf, double tc5,
+                        double *aa_src, void *stream);
+/* aa_src[i][p] = sum_{q=c0}^{c1-1} inv(AA_SOL_i)[p][q] work[i][q]: the element
+ * solve of any local source (the moment preconditioner, krylov.py:369-414). */
+int pbte_gsis_apply_inverse(const pbte_gsis_ops *ops, const double *work, int32_t c0, int32_t c1,
+                            double *aa_src, const int32_t *done, void *stream);
+/* GlobalSolver.rhs (acceleration/global_solve.py:131-187): ffa[f][r]
+ * (n_faces x NF3, the solve's unknown order) from aa_src and the kinetic wall
+ * moments.  done (optional device flag): return at once while *done != 0. */
+int pbte_gsis_trace_rhs(const pbte_gsis_ops *ops, const double *aa_src, const double *wall_mom, double *ffa,
+                        const int32_t *done, void *stream);
+/* local_solve (acceleration/local_solve.py:16-26): uq[p][i] (7*ndof x n_tris) =
+ * aa_src[i][p] + sum_il AA_TRACE_i[il] u_trace[face(i, il)]. */
+int pbte_gsis_local_recover(const pbte_gsis_ops *ops, const double *aa_src, const double *u_trace, double *uq,
+                            const int32_t *done, void *stream);
+
 /* Batched dense inverse of n matrices of order m (FP64, Gauss-Jordan with
  * partial pivoting), a[n][m][m] -> inv[n][m][m].  Replaces the
  * np.linalg.inv of build_local_operators (acceleration/assembly.py:100).
@@ -348,12 +438,14 @@ int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int
  * the global unknowns of each front, own first; G: per node m x o,
  * H: o x m, row-major; cptr/csrc: per front position, the delta slots of
  * the children's updates to add.  max_own / max_front: the largest o / m of
- * the items (shared memory, at most 25 600 doubles). */
+ * the items (shared memory, at most 25 600 doubles).  done (optional device
+ * flag): every block returns at once while *done != 0. */
 int pbte_nd_forward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
                     const int64_t *cptr, const int64_t *csrc, const double *G, const double *b, double *z,
-                    double *delta, int32_t max_own, void *stream);
+                    double *delta, int32_t max_own, const int32_t *done, void *stream);
 int pbte_nd_backward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
-                     const double *H, const double *z, double *x, int32_t max_front, void *stream);
+                     const double *H, const double *z, double *x, int32_t max_front, const int32_t *done,
+                     void *stream);
 
 /* ---- field output (pybte/io_output.py:187-276) ---------------------------
  * No context: these take the mesh, basis and state as plain device arrays,

@@ -4,10 +4,12 @@ Runs the reference solver (dingtao-shen/...-PBTE, ``solver-python/pybte``) in
 its pure-Python/LAPACK mode (numba absent) and records its outputs on small
 cases, plus the certified solutions shipped with the reference's benchmark
 task (``tasks/t01-square/reference/*.npz``).  Needs the reference checkout,
-so it runs only where that is mounted:
+so it runs only where that checkout exists.  Its location comes from the first
+argument or from the environment variable ``PBTE_REFERENCE_ROOT``:
 
-    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py /root/reference
-    (sections alone: --config-only, --precond-only, --periodic-only, --field-only)
+    PYTHONDONTWRITEBYTECODE=1 python tests/golden/make_golden.py <reference checkout>
+    (sections alone: --config-only, --precond-only, --periodic-only, --field-only,
+    --c1-only)
 
 The fixtures are plain arrays; nothing at test time reads the reference.
 """
@@ -15,6 +17,7 @@ from __future__ import annotations
 
 import atexit
 import json
+import os
 import shutil
 import sys
 import tempfile
@@ -403,19 +406,60 @@ def config_errors(ref: Path) -> None:
     (OUT / "config_errors.json").write_text(json.dumps(out, indent=1, sort_keys=True))
 
 
+def c1_square(ref: Path) -> dict:
+    """The 800-triangle square of the CIS benchmark: uniform 20 x 20 grid, P1,
+    64 ordinates (npole 4 x nazim 16), tau_R = 1, tau_N = 0.1, west/east
+    isothermal at +0.5/-0.5, north/south diffuse adiabatic, CIS to 1e-8.
+    About six minutes in pybte's pure-Python mode."""
+    sys.path[:0] = [str(ref / "solver-python"), str(ref / "solver-python" / "tools")]
+    from make_meshes import build
+    from pybte import Case, Solver
+
+    tmp = _scratch()
+    (tmp / "U_20.msh").write_text(build(20, "cavity", "uniform"))
+    c = Case.from_dict({
+        "iteration": {"tol": 1e-8, "tmax": 5000}, "scheme": {"accflag": 0},
+        "velmesh": {"npole": 4, "nazim": 16}, "dg": {"deg": 1},
+        "flow": {"cv": 1.0, "vg": 1.0, "tau_r": 1.0, "tau_n": 0.1, "tau_thr": 1.0},
+        "mesh": {"file": str(tmp / "U_20.msh")},
+        "boundaries": [{"name": "SWall", "phyid": 11, "type": "nonthermalising", "temp": 0.0},
+                       {"name": "NWall", "phyid": 12, "type": "nonthermalising", "temp": 0.0},
+                       {"name": "EWall", "phyid": 13, "type": "thermalising", "temp": -0.5},
+                       {"name": "WWall", "phyid": 14, "type": "thermalising", "temp": 0.5}],
+        "output": {"field": False, "runtime_log": False, "run_record": False}}, basedir=str(tmp))
+    s = Solver(c)
+    rec = s.run()
+    tr = s.ctx.true_residual(s.mom, s.vdf)
+    np.savez_compressed(OUT / "c1_square20_cis.npz", iterations=rec.iterations, converged=rec.converged,
+                        residuals=rec.residual_history, temp=rec.temp, qx=rec.qx, qy=rec.qy,
+                        ts=rec.temp_dofs, qxs=rec.qx_dofs, qys=rec.qy_dofs, true_residual=tr)
+    print("c1", rec.iterations, rec.converged, float(np.sum(rec.qx)), tr, flush=True)
+    return {"c1_square20_cis": {"n": 20, "deg": 1, "npole": 4, "nazim": 16, "tau_r": 1.0, "tau_n": 0.1,
+                                "iterations": int(rec.iterations), "true_residual": float(tr),
+                                "sum_qx": float(np.sum(rec.qx))}}
+
+
 if __name__ == "__main__":
-    ref_root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    if "--config-only" in sys.argv[2:]:
+    ref_root = sys.argv[1] if len(sys.argv) > 1 and not sys.argv[1].startswith("--") else \
+        os.environ.get("PBTE_REFERENCE_ROOT")
+    if not ref_root:
+        sys.exit("usage: make_golden.py <reference checkout> [--section-only]  "
+                 "(or set PBTE_REFERENCE_ROOT)")
+    if "--c1-only" in sys.argv[1:]:
+        m = json.loads((OUT / "golden_meta.json").read_text())
+        m.update(c1_square(Path(ref_root)))
+        (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
+    elif "--config-only" in sys.argv[1:]:
         config_errors(Path(ref_root))
-    elif "--precond-only" in sys.argv[2:]:
+    elif "--precond-only" in sys.argv[1:]:
         m = json.loads((OUT / "golden_meta.json").read_text())
         m.update(krylov_precond(Path(ref_root)))
         (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
-    elif "--periodic-only" in sys.argv[2:]:
+    elif "--periodic-only" in sys.argv[1:]:
         m = json.loads((OUT / "golden_meta.json").read_text())
         m.update(periodic(Path(ref_root)))
         (OUT / "golden_meta.json").write_text(json.dumps(m, indent=1, sort_keys=True))
-    elif "--field-only" in sys.argv[2:]:
+    elif "--field-only" in sys.argv[1:]:
         sys.path[:0] = [str(Path(ref_root) / "solver-python"), str(Path(ref_root) / "solver-python" / "tools")]
         from make_meshes import build as _build
         from pybte import Case as _Case

@@ -51,12 +51,18 @@ def test_cgs2_rejects_short_scratch_on_the_host():
     L = _lib.lib()
     buf = (ctypes.c_double * 16)()
     p = ctypes.cast(buf, ctypes.c_void_p)
-    short = _lib.CGS2_SCRATCH - 1
-    assert f"PBTE_CGS2_SCRATCH ({_lib.CGS2_SCRATCH // 64} * 64)" in HEADER.read_text()
-    for fn in (L.pbte_cgs2, L.pbte_cgs2_f32):
-        assert fn(p, 4, 1, p, 4, p, p, short, None) == -1
-    for fn in (L.pbte_arnoldi_column, L.pbte_arnoldi_column_f32):
-        assert fn(p, 4, 1, p, None, p, 4, p, p, short, None, None) == -1
+    text = HEADER.read_text()
+    assert f"#define PBTE_MAX_BASIS {_lib.MAX_BASIS}" in text
+    assert "#define PBTE_CGS2_SCRATCH PBTE_CGS2_SCRATCH_ROWS(64)" in text
+    assert "(8 + 2 * PBTE_MAX_BASIS + 1216 * ((((rows) + 7) / 8) * 8))" in text
+    for rows in (1, 64, 200):
+        short = _lib.cgs2_scratch(rows) - 1
+        for fn in (L.pbte_cgs2, L.pbte_cgs2_f32):
+            assert fn(p, 4, rows, p, 4, p, p, short, None) == -1
+        for fn in (L.pbte_arnoldi_column, L.pbte_arnoldi_column_f32):
+            assert fn(p, 4, rows, p, p, p, 4, p, p, short, None, None) == -1
+    # a basis beyond PBTE_MAX_BASIS rows is refused whatever the scratch
+    assert L.pbte_cgs2(p, 4, _lib.MAX_BASIS + 1, p, 4, p, p, 1 << 30, None) == -1
 
 
 def test_gmres_cycle_struct_matches_header():

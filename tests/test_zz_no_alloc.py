@@ -1,19 +1,22 @@
 """The allocation-free transport residual (``pbte_transport_residual_noalloc``).
 
 It serves callers that cannot allocate device memory where they call from --
-code running while a CUDA graph is captured in global mode, hosts whose device
-memory belongs to their own pool -- by keeping its scratch in a static device
-array instead of the context's buffers.  Checked here through the C ABI
+hosts whose device memory is handed out by their own pool, so that a
+cudaMalloc behind their back fails or breaks their accounting -- by keeping its
+scratch in a static device array instead of the context's buffers.  Checked here through the C ABI
 against ``pbte_transport_residual`` on the same state, on two calls in a row
-with different states (so stale scratch would show), and for the size limit.
+with different states (so stale scratch would show), and for the size and
+periodic-face limits.
 This file is collected last so that a failure here leaves every other test
 already run.
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
 
-from cases import small_case
+from cases import periodic_case, small_case
 from pbte_gb300 import Solver, _lib
 
 pytestmark = pytest.mark.gpu
@@ -25,6 +28,12 @@ def _seed(s, seed):
         getattr(s.mom, k).copy_(torch.randn(getattr(s.mom, k).shape, generator=g, dtype=torch.float64))
     s.vdf.copy_(torch.randn(s.vdf.shape, generator=g, dtype=torch.float64))
     s.ctx.wall_flux(s.vdf)
+
+
+def _live_bytes() -> int:
+    v = ctypes.c_int64(-1)
+    _lib.check(_lib.lib().pbte_device_bytes_live(ctypes.byref(v)), "device_bytes_live")
+    return int(v.value)
 
 
 def _call(fn, s, num, den, *extra):
@@ -45,18 +54,23 @@ def test_noalloc_matches_context_scratch_version(cuda):
         num1, den1 = torch.full((s.ndir,), np.nan, **f64), torch.full((s.ndir,), np.nan, **f64)
         _lib.check(_call(L.pbte_transport_residual, s, num0, den0, s.ctx.pbuf.data_ptr()), "reference call")
         torch.cuda.synchronize()
-        free_before = torch.cuda.mem_get_info()[0]
+        # this process's own device memory: torch's pool and the library's
+        # contexts (not the device-wide free bytes, which other processes move)
+        held = (torch.cuda.memory_reserved(), _live_bytes())
         _lib.check(_call(L.pbte_transport_residual_noalloc, s, num1, den1), f"no-alloc call {call}")
         torch.cuda.synchronize()
-        if call > 0:
-            # the first call on a device resolves the static array, which with
-            # lazy module loading is when the runtime commits its 4 MiB; every
-            # later call leaves device memory exactly as it was
-            assert torch.cuda.mem_get_info()[0] == free_before
+        assert (torch.cuda.memory_reserved(), _live_bytes()) == held
         a, b = num1.cpu().numpy(), num0.cpu().numpy()
         assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
         a, b = den1.cpu().numpy(), den0.cpu().numpy()
         assert np.abs(a - b).max() <= 1e-12 * np.abs(b).max()
+
+
+def test_noalloc_refuses_periodic_faces(cuda):
+    s = Solver(periodic_case(1, 4, 8, 0.5, 0.05))
+    f64 = dict(dtype=torch.float64, device=s.device)
+    num, den = torch.zeros(s.ndir, **f64), torch.zeros(s.ndir, **f64)
+    assert _call(_lib.lib().pbte_transport_residual_noalloc, s, num, den) == -4
 
 
 def test_noalloc_rejects_cases_beyond_its_scratch(cuda):
