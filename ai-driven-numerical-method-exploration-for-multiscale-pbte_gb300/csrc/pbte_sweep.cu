@@ -144,9 +144,22 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
             const int k = nbeg + t + c * TPG;
             ncell[c] = k < nend ? __ldg(ri + kICell * M + k) : -1;
         }
+        const int rbase = (L % Rr) * W;
+        // a level wider than the group's TPG * CPT cells runs in chunks of
+        // that many; only the first waits for level L-1 and only the last
+        // hands level L on, so registers do not grow with the level width
+        for (int cb = beg; cb < end; cb += CPT * TPG) {
+        const bool first = cb == beg, last = cb + CPT * TPG >= end;
+        if (!first) {
+#pragma unroll
+            for (int c = 0; c < CPT; ++c) {
+                const int k = cb + t + c * TPG;
+                cell[c] = k < end ? __ldg(ri + kICell * M + k) : 0;
+            }
+        }
         bool valid[CPT];
 #pragma unroll
-        for (int c = 0; c < CPT; ++c) valid[c] = beg + t + c * TPG < end;
+        for (int c = 0; c < CPT; ++c) valid[c] = cb + t + c * TPG < end;
         T A[CPT][NP][NP];
         T b[CPT][NP];
         int piv[CPT][NP];
@@ -158,7 +171,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
-            const int64_t k = beg + t + c * TPG;
+            const int64_t k = cb + t + c * TPG;
             const int i = cell[c];
             {
                 // the source first, so its values are dead before the factorisation
@@ -296,8 +309,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
             }
         }
         // ---- wait for level L-1, then the upwind inflow and the solves ------
-        if (G > 1 && L > 0) bar_sync(1 + (L - 1) % G, 2 * TPG);
-        const int rbase = (L % Rr) * W;
+        if (first && G > 1 && L > 0) bar_sync(1 + (L - 1) % G, 2 * TPG);
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
             if (!valid[c]) continue;
@@ -338,7 +350,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
 #pragma unroll
                 for (int j = 0; j < kk; ++j) b[c][j] -= b[c][kk] * A[c][j][kk];
             }
-            T *rs = ring + (size_t)(rbase + t + c * TPG) * NP;
+            T *rs = ring + (size_t)(rbase + (cb - beg) + t + c * TPG) * NP;
 #pragma unroll
             for (int m = 0; m < NP; ++m) rs[m] = b[c][m];
             if (fo[c] >= 0) {
@@ -347,10 +359,12 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
                 for (int m = 0; m < NP; ++m) fs[m] = b[c][m];
             }
         }
-        if (G > 1) {
-            if (L + 1 < nlev) bar_arrive(1 + L % G, 2 * TPG);
-        } else {
-            __syncthreads();
+        if (last) {
+            if (G > 1) {
+                if (L + 1 < nlev) bar_arrive(1 + L % G, 2 * TPG);
+            } else {
+                __syncthreads();
+            }
         }
         // the distribution itself is not read back inside the sweep: store it
         // after the hand-over so the barrier does not wait on global stores
@@ -360,6 +374,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
             store_row<T, NP>(f1 + (size_t)cell[c] * NP, b[c]);
             if (f2) store_row<T, NP>(f2 + (size_t)cell[c] * NP, b[c]);
         }
+        }   // chunks of the level
         // the next level's source rows into L1
 #pragma unroll
         for (int c = 0; c < CPT; ++c) {
@@ -401,12 +416,15 @@ static int ring_launch_cpt(pbte_ctx *c, const SweepParams<T> &P, const RingParam
 }
 
 // Returns PBTE_ERR_UNSUPPORTED when the ring form does not fit (the caller
-// then uses the level-serial kernel).  Block shapes compiled: groups of 64
-// with up to four groups (1, 2 or 4 elements per thread); for DEG <= 2 also
-// up to eight groups of 64 (1 or 2 elements per thread) and up to four groups
-// of 128 (1 element per thread), the 512-thread shapes whose operators fit
-// the 128 registers such a block allows.  A requested shape that is not
-// compiled for the mesh falls back to four groups of 64.
+// then uses the level-serial kernel): degree above 3, or a ring that does not
+// fit in shared memory.  Block shapes compiled: groups of 64 with up to four
+// groups (1, 2 or 4 elements per thread in registers); for DEG <= 2 also up
+// to eight groups of 64 (1 or 2 elements per thread) and up to four groups of
+// 128 (1 element per thread), the 512-thread shapes whose operators fit the
+// 128 registers such a block allows.  A level wider than a group's elements
+// in registers runs in chunks (sweep_ring_kernel), so any level width is
+// served.  A requested shape that is not compiled for the mesh falls back to
+// four groups of 64.
 template <typename T, bool PRE>
 int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     if (c->deg > 3 || c->ring_W <= 0) return PBTE_ERR_UNSUPPORTED;
@@ -417,18 +435,21 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     int width = c->ring_width == 128 ? 128 : 64;
     int groups = c->ring_groups > 0 ? std::min(c->ring_groups, kMaxGroups) : 4;
     if (c->ring_groups == 0 && c->ring_width == 0 && c->deg <= 2) {
-        // measured defaults (C2/C3 square cavities, P1/P2, 256 ordinates):
+        // measured defaults (square cavities, P1/P2, 256-512 ordinates):
         // levels up to 64 wide take eight groups of 64 in FP32 (four in FP64,
-        // whose operators need twice the registers), levels up to 128 wide
-        // four groups of 128
+        // whose operators need twice the registers), wider levels four groups
+        // of 128 (in chunks beyond 128)
         if (c->ring_W <= 64) groups = sizeof(T) == 4 ? 8 : 4;
-        else if (c->ring_W <= 128) width = 128;
+        else width = 128;
     }
-    if (width == 128 && (cpt_for(128) > 1 || c->deg > 2 || groups > 4)) width = 64;
-    const int cpt = cpt_for(width);
-    if (groups > 4 && (cpt > 2 || c->deg > 2)) groups = 4;
-    if (cpt > 4 || (cpt == 4 && (sizeof(T) != 4 || c->deg > 2)) || (c->deg == 3 && cpt > 1))
-        return PBTE_ERR_UNSUPPORTED;
+    if (width == 128 && (c->deg > 2 || groups > 4)) width = 64;
+    if (groups > 4 && c->deg > 2) groups = 4;
+    // elements per thread held in registers: what the level needs, up to what
+    // the shape is compiled for (chunks cover the rest)
+    int cpt = cpt_for(width);
+    int cpt_max = 1;
+    if (width == 64 && c->deg <= 2) cpt_max = (sizeof(T) == 4 && groups <= 4) ? 4 : 2;
+    cpt = std::min(cpt, cpt_max);
     const size_t ring_vals = (size_t)c->ring_R * c->ring_W * c->nd;
     const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + ring_vals + (size_t)c->far_max * c->nd);
     if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;

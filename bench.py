@@ -180,12 +180,15 @@ def run_reference(args, world, rank):
     from oracle import oracle as orc
     orc.build()
     cores = os.cpu_count() or 1
+    # warm-up: untimed solves of the cheapest case (the oracle has no caches
+    # to fill; this loads the library and pages the code in)
+    for _ in range(args.warmup):
+        cpu_solve(KN[0], cores)
+    # the timed steps solve exactly the GPU arm's timed sequence of cases
     times = []
-    for k in range(args.warmup + args.steps):
-        kn = KN[k % len(KN)] if args.steps >= len(KN) else 1.0
-        t, r = cpu_solve(kn, cores)
-        if k >= args.warmup:
-            times.append(t)
+    for k in range(args.steps):
+        t, r = cpu_solve(KN[k % len(KN)], cores)
+        times.append(t)
     total = float(sum(times))
     v = len(times) / total
     line = {"metric": METRIC, "value": round(v, 4), "unit": "solves/s", "n_gpus": world, "steps": args.steps,
@@ -194,7 +197,8 @@ def run_reference(args, world, rank):
             "data": "synthetic (structured square mesh, seedless)", "impl": "reference",
             "config": {**workload_config(), "method": "GMRES(30) FP64 (C oracle)"},
             "cpu_baseline": {"value": round(v, 4), "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"{len(times)} complete solves"},
+                             "sample": f"{len(times)} complete solves, Kn_R sequence "
+                                       f"{[KN[k % len(KN)] for k in range(args.steps)]}"},
             "e2e": {"value": round(v, 4), "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
@@ -258,10 +262,12 @@ def main():
         timed(solvers, k)
     launches = 0
     times = []
+    mixed_fields = []
     with ClockSampler(local) as clk:
         for k in range(args.steps):
             ms, rec = timed(solvers, k)
             times.append(ms)
+            mixed_fields.append((KN[k % len(KN)], rec.temp, rec.qx))
             # per FP32 Arnoldi column: sweep, epilogue (moments, integrals,
             # wall emission), CGS2 (3, the rotation in the last one's tail),
             # next basis vector with the next column's moment sources; one
@@ -282,9 +288,20 @@ def main():
     for k in range(len(KN)):
         timed(fp64, k)
     t64 = []
+    fp64_fields = {}
     for k in range(min(args.steps, len(KN))):
-        ms, _ = timed(fp64, k)
+        ms, rec64 = timed(fp64, k)
         t64.append(ms)
+        fp64_fields[KN[k % len(KN)]] = (rec64.temp, rec64.qx)
+
+    def rel_l2(a, b):
+        return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+    # every timed mixed solve against the FP64 drop-in's solve of the same
+    # case (relative L2 on temperature and heat flux); the bar is 1e-8
+    err = max(max(rel_l2(t, fp64_fields[kn][0]), rel_l2(q, fp64_fields[kn][1])) for kn, t, q in mixed_fields)
+    if not err <= 1e-8:
+        raise RuntimeError(f"mixed-precision solves are {err:.2e} from the FP64 drop-in (bar 1e-8)")
     fp64_rate = len(t64) / (sum(t64) * 1e-3)
 
     # batched: two copies of each Kn case solved concurrently (one stream and
@@ -374,6 +391,9 @@ def main():
                 "config": {**workload_config(), "parallelism": f"replicas x{world}"},
                 "latency_ms": {"p50": round(float(np.percentile(lat, 50)), 3),
                                "p99": round(float(np.percentile(lat, 99)), 3)},
+                "err_vs_fp64": {"max_rel_l2": float(f"{err:.3e}"), "fields": ["temp", "qx"],
+                                "against": "FP64 GPU drop-in solve of the same case (GMRES(30), tol 1e-8)",
+                                "bar": 1e-8},
                 "fp64": {"value": round(fp64_rate, 4), "unit": "solves/s",
                          "speedup_mixed_over_fp64": round(value / world / fp64_rate, 3),
                          "speedup_batched_mixed_over_fp64": round(batched["value"] / fp64_rate, 3)},

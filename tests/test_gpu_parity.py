@@ -64,6 +64,34 @@ def test_sweep_moments_flux_match_oracle(cuda, deg, mode, south):
 
 
 @pytest.mark.parametrize("deg", [1, 2, 3])
+def test_ring_sweep_chunks_levels_wider_than_its_registers(cuda, deg):
+    """Levels wider than a thread group holds in registers run in chunks (only
+    the first waits for the level before, only the last hands the level on):
+    a 72 x 72 square (levels ~144 wide) swept with block shapes whose groups
+    hold 64 or 128 elements, FP64 and FP32, against the oracle."""
+    s = Solver(small_case(deg, 4, 8, 0.3, 0.03, mesh="cavity:72", sweep_mode="onthefly"))
+    assert s.ctx.schedule()["ring_W"] > 128
+    o = Oracle(s.disc, nthreads=4)
+    _seed_state(s, o, 23)
+    o.wall_flux()
+    s.ctx.wall_flux(s.vdf)
+    o.sweep()
+    s.ctx.set_variant(2)
+    shapes = [(1, 64), (2, 64), (4, 64), (8, 64), (2, 128), (4, 128)]
+    for g, w in shapes:
+        s.ctx.set_groups(g, w)
+        v = s.vdf.clone()
+        s.ctx.sweep(s.mom, v)
+        u = torch.zeros(s.vdf.shape, dtype=torch.float32, device=s.device)
+        s.ctx.sweep_f32((s.mom.ts, s.mom.qxs, s.mom.qys), u, s.ctx.flux_wall)
+        torch.cuda.synchronize()
+        assert _rel(v.cpu().numpy(), o.vdf) < 1e-11, (g, w)
+        assert _rel(u.double().cpu().numpy(), o.vdf) < 2e-5, (g, w)
+    s.ctx.set_groups(0, 0)
+    s.ctx.set_variant(0)
+
+
+@pytest.mark.parametrize("deg", [1, 2, 3])
 @pytest.mark.parametrize("mode", ["precomputed", "onthefly"])
 def test_ring_and_level_serial_sweeps_agree(cuda, deg, mode):
     """The ring-pipelined kernel (one block per in-plane velocity, twins
