@@ -98,8 +98,8 @@ __device__ __forceinline__ void store_row(T *o, const T (&v)[NP]) {
 }
 
 // TPG: threads per group; GMAX: the most groups the kernel is compiled for
-// (its launch bound)
-template <typename T, int DEG, bool PRECOMP, int CPT, int TPG, int GMAX>
+// (its launch bound); CH: levels may be wider than TPG * CPT (run in chunks)
+template <typename T, int DEG, bool PRECOMP, int CPT, int TPG, int GMAX, bool CH>
 __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P, RingParams Q) {
     constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -149,7 +149,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
         // that many; only the first waits for level L-1 and only the last
         // hands level L on, so registers do not grow with the level width
         for (int cb = beg; cb < end; cb += CPT * TPG) {
-        const bool first = cb == beg, last = cb + CPT * TPG >= end;
+        const bool first = !CH || cb == beg, last = !CH || cb + CPT * TPG >= end;
         if (!first) {
 #pragma unroll
             for (int c = 0; c < CPT; ++c) {
@@ -374,6 +374,7 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
             store_row<T, NP>(f1 + (size_t)cell[c] * NP, b[c]);
             if (f2) store_row<T, NP>(f2 + (size_t)cell[c] * NP, b[c]);
         }
+        if (!CH) break;
         }   // chunks of the level
         // the next level's source rows into L1
 #pragma unroll
@@ -395,6 +396,7 @@ template <typename T, int DEG, bool PRE, int TPG, int GMAX>
 static int ring_launch_cpt(pbte_ctx *c, const SweepParams<T> &P, const RingParams &Q, int cpt, size_t shm,
                            cudaStream_t s) {
     const int threads = Q.groups * TPG;
+    const bool chunked = c->ring_W > cpt * TPG;
     auto go = [&](auto kern) {
         if (shm > 48 * 1024 &&
             cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) != cudaSuccess)
@@ -403,13 +405,19 @@ static int ring_launch_cpt(pbte_ctx *c, const SweepParams<T> &P, const RingParam
         return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
     };
     switch (cpt) {
-        case 1: return go(sweep_ring_kernel<T, DEG, PRE, 1, TPG, GMAX>);
+        case 1:
+            if (chunked) return go(sweep_ring_kernel<T, DEG, PRE, 1, TPG, GMAX, true>);
+            return go(sweep_ring_kernel<T, DEG, PRE, 1, TPG, GMAX, false>);
         case 2:
-            if constexpr (DEG <= 2 && TPG == 64) return go(sweep_ring_kernel<T, DEG, PRE, 2, TPG, GMAX>);
+            if constexpr (DEG <= 2 && TPG == 64) {
+                if (chunked) return go(sweep_ring_kernel<T, DEG, PRE, 2, TPG, GMAX, true>);
+                return go(sweep_ring_kernel<T, DEG, PRE, 2, TPG, GMAX, false>);
+            }
             return PBTE_ERR_UNSUPPORTED;
         case 4:
+            // four elements per thread cover levels up to 256 wide: never chunked
             if constexpr (sizeof(T) == 4 && DEG <= 2 && TPG == 64 && GMAX <= 4)
-                return go(sweep_ring_kernel<T, DEG, PRE, 4, TPG, GMAX>);
+                if (!chunked) return go(sweep_ring_kernel<T, DEG, PRE, 4, TPG, GMAX, false>);
             return PBTE_ERR_UNSUPPORTED;
         default: return PBTE_ERR_UNSUPPORTED;
     }
@@ -437,10 +445,14 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     if (c->ring_groups == 0 && c->ring_width == 0 && c->deg <= 2) {
         // measured defaults (square cavities, P1/P2, 256-512 ordinates):
         // levels up to 64 wide take eight groups of 64 in FP32 (four in FP64,
-        // whose operators need twice the registers), wider levels four groups
-        // of 128 (in chunks beyond 128)
+        // whose operators need twice the registers), levels up to 128 wide
+        // four groups of 128, wider levels two groups of 128 in chunks (two
+        // 256-thread blocks fit an SM, so all the 256 velocities of a
+        // 512-ordinate case run at once: 3.3 ms against 4.9 with four groups
+        // on the 256 x 256 square)
         if (c->ring_W <= 64) groups = sizeof(T) == 4 ? 8 : 4;
-        else width = 128;
+        else if (c->ring_W <= 128) width = 128;
+        else { width = 128; groups = 2; }
     }
     if (width == 128 && (c->deg > 2 || groups > 4)) width = 64;
     if (groups > 4 && c->deg > 2) groups = 4;
@@ -448,7 +460,7 @@ int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s) {
     // the shape is compiled for (chunks cover the rest)
     int cpt = cpt_for(width);
     int cpt_max = 1;
-    if (width == 64 && c->deg <= 2) cpt_max = (sizeof(T) == 4 && groups <= 4) ? 4 : 2;
+    if (width == 64 && c->deg <= 2) cpt_max = (sizeof(T) == 4 && groups <= 4 && cpt == 4) ? 4 : 2;
     cpt = std::min(cpt, cpt_max);
     const size_t ring_vals = (size_t)c->ring_R * c->ring_W * c->nd;
     const size_t shm = sizeof(T) * ((size_t)6 * c->nd * c->nd + ring_vals + (size_t)c->far_max * c->nd);

@@ -123,6 +123,12 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# DRAM bytes of one launch of the FP32 ring sweep (dram__bytes_read.sum +
+# dram__bytes_write.sum), by workload (n_tris, ndof, ndir), from the ncu
+# captures summarised under profiles/ (sweep_ring_fp32_*); None elsewhere
+SWEEP_TRAFFIC = {(8192, 6, 256): 7028480 + 1436672}
+
+
 def sweep_roofline(solver, peak, peak_kind, reps=20):
     """Average duration of the FP32 sweep kernel on this case (CUDA events on
     its stream) and its algorithmic bytes per launch."""
@@ -152,14 +158,15 @@ def sweep_roofline(solver, peak, peak_kind, reps=20):
             + 116.0 * s.ctx.n_classes * nt       # field-major element records, once per direction class
             + 8.0 * s.mesh.n_faces_b * nd)       # wall emission (FP64)
     ach = algo / (ms * 1e-3) / 1e9
-    # DRAM bytes of one launch of this kernel on this workload, from ncu
-    # (dram__bytes_read.sum + dram__bytes_write.sum): the distribution stays
-    # in the 126 MB L2, so DRAM traffic is below the algorithmic bytes
-    traffic = 7028480 + 1436672 if (nt, nd, ndir) == (8192, 6, 256) else None
+    sch = s.ctx.schedule()
+    traffic = SWEEP_TRAFFIC.get((nt, nd, ndir))
     return {"bound": "hbm", "achieved": round(ach, 1), "peak": peak, "unit": "GB/s",
-            "frac": round(ach / peak, 4), "traffic": traffic, "kernel": "sweep_ring_kernel<float,2,false,1,64,8>",
+            "frac": round(ach / peak, 4), "traffic": traffic,
+            "kernel": f"sweep_ring_kernel<float, P{s.case.dg.deg}> (widest level {sch['ring_W']}, "
+                      f"{sch['levels']} levels, {sch['unique_dirs']} blocks)",
             "kernel_ms": round(ms, 4), "algorithmic_bytes": int(algo), "peak_source": f"{peak_kind} hbm_gbs",
-            "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same workload"}
+            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same workload"
+                               if traffic is not None else "not captured for this workload")}
 
 
 def cpu_solve(kn, nthreads, max_seconds=30.0):
@@ -374,6 +381,18 @@ def main():
 
     peak, kind = read_peaks()
     roof = sweep_roofline(solvers[1.0], peak, kind)
+    # the FP32 sweep on the large diffusive square (256 x 256, 131 072
+    # triangles, P2, 512 ordinates), where the roofline target is set
+    c3 = None
+    if rank == 0:
+        from pbte_gb300.config import square_case
+        t0 = time.perf_counter()
+        big = Solver(square_case(256, 2, 8, 64, tau_r=1e-3, tau_n=1e-4, precision="mixed", sweep_mode="onthefly"),
+                     device=str(dev))
+        c3 = {"workload": "square 256x256 grid (131072 tri), DG P2, 512 ordinates (8 polar x 64 azimuth)",
+              "setup_s": round(time.perf_counter() - t0, 2), "roofline": sweep_roofline(big, peak, kind, reps=10)}
+        del big
+        torch.cuda.empty_cache()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
@@ -400,7 +419,8 @@ def main():
                 "batched": batched, "gsis": gsis,
                 "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                         "d2h_bytes_per_step": int(d2h)},
-                "roofline": roof, "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": int(launches)}
+                "roofline": roof, "c3_sweep": c3, "cpu_baseline": cpu, "clocks": clocks,
+                "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     if dist is not None:
         dist.barrier()

@@ -67,17 +67,19 @@ def test_sweep_moments_flux_match_oracle(cuda, deg, mode, south):
 def test_ring_sweep_chunks_levels_wider_than_its_registers(cuda, deg):
     """Levels wider than a thread group holds in registers run in chunks (only
     the first waits for the level before, only the last hands the level on):
-    a 72 x 72 square (levels ~144 wide) swept with block shapes whose groups
+    a 136 x 136 square (levels 136 wide; P3: 72 x 72, levels 72 wide, whose
+    groups hold one element per thread) swept with block shapes whose groups
     hold 64 or 128 elements, FP64 and FP32, against the oracle."""
-    s = Solver(small_case(deg, 4, 8, 0.3, 0.03, mesh="cavity:72", sweep_mode="onthefly"))
-    assert s.ctx.schedule()["ring_W"] > 128
+    n = 72 if deg == 3 else 136
+    s = Solver(small_case(deg, 2, 8, 0.3, 0.03, mesh=f"cavity:{n}", sweep_mode="onthefly"))
+    assert s.ctx.schedule()["ring_W"] > (64 if deg == 3 else 128)
     o = Oracle(s.disc, nthreads=4)
     _seed_state(s, o, 23)
     o.wall_flux()
     s.ctx.wall_flux(s.vdf)
     o.sweep()
     s.ctx.set_variant(2)
-    shapes = [(1, 64), (2, 64), (4, 64), (8, 64), (2, 128), (4, 128)]
+    shapes = [(1, 64), (2, 64), (4, 64), (8, 64), (1, 128), (2, 128), (4, 128)]
     for g, w in shapes:
         s.ctx.set_groups(g, w)
         v = s.vdf.clone()
