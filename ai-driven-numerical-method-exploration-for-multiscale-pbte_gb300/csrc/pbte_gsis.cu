@@ -11,6 +11,8 @@
 // of 32 consecutive (element, DOF) entries: coalesced.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "pbte_device.cuh"
 
 namespace pbte {
@@ -437,6 +439,166 @@ int launch_gsis_hot_apply(pbte_ctx *c, const pbte_gsis_ops *o, const double *vdf
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
 }
 
+// ---------------------------------------------------------------------------
+// The FP32 GSIS product of the mixed-precision GSIS solve (its inner
+// operator, whose accuracy the FP64 defect correction around it sets): the
+// same steps on the folded FP32 distribution (one row per distinct in-plane
+// velocity u; z-mirror twins are equal, so a pair's weights are summed: the
+// d_u*64 arrays), FP32 products and sums, FP64 outputs.
+namespace {
+
+__global__ void __launch_bounds__(kLanes *kChunks) hot_moments32_kernel(const float *vdf, const double *cx,
+                                                                        const double *cy, const double *w, int nu,
+                                                                        int total, double *mk, const int32_t *done) {
+    if (stopped(done)) return;
+    extern __shared__ float ws32[];   // [4][nu]
+    const int tid = threadIdx.y * kLanes + threadIdx.x;
+    for (int u = tid; u < nu; u += kLanes * kChunks) {
+        double a[4];
+        weights<true>(cx[u], cy[u], w[u], a);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) ws32[k * nu + u] = (float)a[k];
+    }
+    __syncthreads();
+    const int t = blockIdx.x * kLanes + threadIdx.x;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (t < total)
+        for (int u = threadIdx.y; u < nu; u += kChunks) {
+            const float f = vdf[(size_t)u * total + t];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[k] += ws32[k * nu + u] * f;
+        }
+    double accd[4] = {acc[0], acc[1], acc[2], acc[3]};
+    reduce_chunks(accd, 4);
+    if (threadIdx.y == 0 && t < total)
+#pragma unroll
+        for (int k = 0; k < 4; ++k) mk[(size_t)k * total + t] = accd[k];
+}
+
+__global__ void __launch_bounds__(kTraceThreads) wall_trace32_kernel(const float *vdf, const double *tri_fc_fc,
+                                                                     const double *cx, const double *cy,
+                                                                     const double *w, int nu, int nt, int NP, int NF,
+                                                                     const int32_t *tri_list, const int32_t *lfc_list,
+                                                                     double *out, const int32_t *done) {
+    if (stopped(done)) return;
+    __shared__ float c[16 * kMaxNf];
+    __shared__ float red[3 * kMaxNf][kTraceThreads];
+    const int k = blockIdx.x;
+    const int tri = tri_list[k], lfc = lfc_list[k];
+    for (int e = threadIdx.x; e < NP * NF; e += blockDim.x) {
+        const int l = e / NF, m = e % NF;
+        c[e] = (float)tri_fc_fc[(((size_t)l * NF + m) * nt + tri) * 3 + lfc];
+    }
+    __syncthreads();
+    float acc[3 * kMaxNf];
+    for (int q = 0; q < 3 * NF; ++q) acc[q] = 0.f;
+    for (int u = threadIdx.x; u < nu; u += blockDim.x) {
+        const float *f = vdf + ((size_t)u * nt + tri) * NP;
+        const float wu = (float)w[u], cxu = (float)cx[u], cyu = (float)cy[u];
+        for (int m = 0; m < NF; ++m) {
+            float tt = 0.f;
+            for (int l = 0; l < NP; ++l) tt += f[l] * c[l * NF + m];
+            acc[m] += tt * wu;
+            acc[NF + m] += cxu * tt * wu;
+            acc[2 * NF + m] += cyu * tt * wu;
+        }
+    }
+    for (int q = 0; q < 3 * NF; ++q) red[q][threadIdx.x] = acc[q];
+    __syncthreads();
+    for (int h = kTraceThreads / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h)
+            for (int q = 0; q < 3 * NF; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+        __syncthreads();
+    }
+    if (threadIdx.x < 3 * NF) out[(size_t)k * 3 * NF + threadIdx.x] = red[threadIdx.x][0];
+}
+
+// the correction's coefficients (correct_moments_kernel's arithmetic after
+// FP32 angular sums); the moments themselves come from the corrected
+// distribution afterwards
+__global__ void __launch_bounds__(kLanes *kChunks) correct_coef32_kernel(
+    const float *vdf, const double *uq, const double *cx, const double *cy, const double *w, const double *tri_hmin,
+    int nu, int nt, int NP, double cv, double tau_r, double tau_thr, int use_hmin, double *coef,
+    const int32_t *done) {
+    if (stopped(done)) return;
+    const int total = nt * NP;
+    const int t = blockIdx.x * kLanes + threadIdx.x;
+    float acc[3] = {0.f, 0.f, 0.f};
+    if (t < total)
+        for (int u = threadIdx.y; u < nu; u += kChunks) {
+            const float f = vdf[(size_t)u * total + t];
+            const float fw = f * (float)w[u];
+            acc[0] += fw;
+            acc[1] += (float)cx[u] * fw;
+            acc[2] += (float)cy[u] * fw;
+        }
+    double accd[4] = {acc[0], acc[1], acc[2], 0.0};
+    reduce_chunks(accd, 3);
+    if (threadIdx.y != 0 || t >= total) return;
+    const int i = t / NP, m = t % NP;
+    const double tau_loc = use_hmin ? tau_r / tri_hmin[i] : tau_r;
+    const double beta = fmin(tau_loc, tau_thr) / tau_loc;
+    const double tv = accd[0] / cv, qxv = accd[1], qyv = accd[2];
+    coef[t] = (uq[(size_t)m * nt + i] - tv) * beta * cv / 4.0 / kPi;
+    coef[total + t] = (uq[(size_t)(NP + m) * nt + i] - qxv) * beta;
+    coef[2 * total + t] = (uq[(size_t)(2 * NP + m) * nt + i] - qyv) * beta;
+}
+
+__global__ void correct_update32_kernel(float *vdf, const double *coef, const double *cx, const double *cy, int nu,
+                                        int total, double drift, const int32_t *done) {
+    if (stopped(done)) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= total) return;
+    const float eq = (float)coef[t], lqx = (float)(coef[total + t] * drift), lqy = (float)(coef[2 * total + t] * drift);
+    for (int u = blockIdx.y; u < nu; u += gridDim.y) {
+        float *f = vdf + (size_t)u * total + t;
+        *f = *f + eq + ((float)cx[u] * lqx + (float)cy[u] * lqy);
+    }
+}
+
+}  // namespace
+
+int launch_gsis_product32(pbte_ctx *c, const pbte_gsis_ops *o, int step, float *vdf32, double tc5,
+                          const double *tri_fc_fc, int nk, const int32_t *tri_list, const int32_t *lfc_list,
+                          double *aa_src_or_wall, const double *uq, const double *tri_hmin, double tau_thr,
+                          int use_hmin, cudaStream_t s) {
+    const int total = c->n_tris * c->nd;
+    const int nu = c->n_udir;
+    if (step == 0) {   // hot source with the element inverses -> aa_src
+        if (!ops_ok(o) || o->n_tris != c->n_tris || o->ndof != c->nd) return PBTE_ERR_ARG;
+        const size_t shm = (size_t)4 * nu * sizeof(float);
+        if (shm > 48 * 1024) {
+            if (shm > 200 * 1024) return PBTE_ERR_UNSUPPORTED;
+            if (cudaFuncSetAttribute(hot_moments32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm) !=
+                cudaSuccess)
+                return PBTE_ERR_CUDA;
+        }
+        hot_moments32_kernel<<<(total + kLanes - 1) / kLanes, dim3(kLanes, kChunks), shm, s>>>(
+            vdf32, c->d_ucx64, c->d_ucy64, c->d_uw64, nu, total, c->d_gsis, c->done);
+        const int M = 7 * c->nd;
+        int th = 0;
+        const int bl = elements_grid(c->n_tris, M, &th);
+        const size_t hshm = (size_t)(th / M) * 4 * c->nd * sizeof(double);
+        hot_apply_kernel<<<bl, th, hshm, s>>>(c->d_gsis, c->d_cells64, c->d_ref64, c->n_tris, c->nd, tc5, o->inv_t,
+                                              aa_src_or_wall, c->done);
+    } else if (step == 1) {   // kinetic wall traces -> wall moments
+        if (nk <= 0) return PBTE_OK;
+        if (c->nd > 16 || c->nf > kMaxNf) return PBTE_ERR_UNSUPPORTED;
+        wall_trace32_kernel<<<nk, kTraceThreads, 0, s>>>(vdf32, tri_fc_fc, c->d_ucx64, c->d_ucy64, c->d_uw64, nu,
+                                                         c->n_tris, c->nd, c->nf, tri_list, lfc_list, aa_src_or_wall,
+                                                         c->done);
+    } else {   // the damped correction of the distribution
+        correct_coef32_kernel<<<(total + kLanes - 1) / kLanes, dim3(kLanes, kChunks), 0, s>>>(
+            vdf32, uq, c->d_ucx64, c->d_ucy64, c->d_uw64, tri_hmin, nu, c->n_tris, c->nd, c->cv, c->tau_r, tau_thr,
+            use_hmin, c->d_gsis, c->done);
+        const double drift = c->tau_c / c->tau_n * 3.0 / 4.0 / kPi / c->vg / c->vg;
+        const int th = 256;
+        correct_update32_kernel<<<dim3((total + th - 1) / th, std::min(nu, 16)), th, 0, s>>>(
+            vdf32, c->d_gsis, c->d_ucx64, c->d_ucy64, nu, total, drift, c->done);
+    }
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
 }  // namespace pbte
 
 extern "C" int pbte_gsis_hot_apply(pbte_ctx *c, const pbte_gsis_ops *o, const double *vdf, double tc5,
@@ -474,4 +636,51 @@ extern "C" int pbte_gsis_local_recover(const pbte_gsis_ops *o, const double *aa_
     pbte::local_recover_kernel<<<bl, th, 0, reinterpret_cast<cudaStream_t>(stream)>>>(*o, aa_src, u_trace, uq,
                                                                                       done);
     return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+// ---- the FP32 GSIS product of the mixed-precision GSIS solve ---------------
+static bool fold_ok(pbte_ctx *c) { return c && !c->has_periodic && (c->nd == 3 || c->nd == 6 || c->nd == 10); }
+
+extern "C" int pbte_sweep_fold_f32(pbte_ctx *c, const double *ts, const double *qxs, const double *qys,
+                                   const double *flux_wall, double wall_scale, float *vdf32, void *stream) {
+    if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
+    if (!ts || !qxs || !qys || !vdf32 || (c->n_wall_ad && !flux_wall)) return PBTE_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    int rc = pbte::launch_sources(c, ts, qxs, qys, true, s);
+    if (rc == PBTE_OK) rc = pbte::launch_sweep32(c, vdf32, flux_wall, wall_scale, s, false, true);
+    return rc;
+}
+
+extern "C" int pbte_fold_epilogue_f32(pbte_ctx *c, const float *vdf32, double *ts, double *qxs, double *qys,
+                                      double *flux_wall, double *temp, double *qx, double *qy, void *stream) {
+    if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
+    if (!vdf32 || !ts || !qxs || !qys) return PBTE_ERR_ARG;
+    if ((temp == nullptr) != (qx == nullptr) || (temp == nullptr) != (qy == nullptr)) return PBTE_ERR_ARG;
+    return pbte::launch_fold_epilogue32(c, vdf32, ts, qxs, qys, flux_wall, temp, qx, qy,
+                                        reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int pbte_gsis_hot_apply_f32(pbte_ctx *c, const pbte_gsis_ops *o, const float *vdf32, double tc5,
+                                       double *aa_src, void *stream) {
+    if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
+    if (!vdf32 || !aa_src) return PBTE_ERR_ARG;
+    return pbte::launch_gsis_product32(c, o, 0, const_cast<float *>(vdf32), tc5, nullptr, 0, nullptr, nullptr,
+                                       aa_src, nullptr, nullptr, 0.0, 0, reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int pbte_wall_trace_f32(pbte_ctx *c, const float *vdf32, const double *tri_fc_fc, int32_t nk,
+                                   const int32_t *tri_list, const int32_t *lfc_list, double *out, void *stream) {
+    if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
+    if (!vdf32 || nk < 0 || (nk && (!tri_fc_fc || !tri_list || !lfc_list || !out))) return PBTE_ERR_ARG;
+    return pbte::launch_gsis_product32(c, nullptr, 1, const_cast<float *>(vdf32), 0.0, tri_fc_fc, nk, tri_list,
+                                       lfc_list, out, nullptr, nullptr, 0.0, 0,
+                                       reinterpret_cast<cudaStream_t>(stream));
+}
+
+extern "C" int pbte_correct_f32(pbte_ctx *c, float *vdf32, const double *uq, const double *tri_hmin,
+                                double tau_thr, int use_hmin, void *stream) {
+    if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
+    if (!vdf32 || !uq || !tri_hmin) return PBTE_ERR_ARG;
+    return pbte::launch_gsis_product32(c, nullptr, 2, vdf32, 0.0, nullptr, 0, nullptr, nullptr, nullptr, uq,
+                                       tri_hmin, tau_thr, use_hmin, reinterpret_cast<cudaStream_t>(stream));
 }

@@ -162,6 +162,9 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
                          const double *fw_in, double wall_scale, float *vdf32, double *ts_out,
                          double *qxs_out, double *qys_out, double *fw_out, double *temp, double *qx,
                          double *qy, cudaStream_t s, bool with_sources = true);
+// moments, element integrals and wall emission of a folded FP32 distribution
+int launch_fold_epilogue32(pbte_ctx *c, const float *vdf32, double *ts_out, double *qxs_out, double *qys_out,
+                           double *fw_out, double *temp, double *qx, double *qy, cudaStream_t s);
 // pbte_arnoldi_column_f32 + pbte_gmres_givens for column rows - 1, the
 // rotation run by the last block of the CGS2 norm pass (pbte_krylov.cu)
 int arnoldi_column_givens_f32(const float *Q, int64_t ldq, int32_t rows, const double *uout, const double *g,
@@ -192,6 +195,12 @@ int launch_transport_residual_scratch(pbte_ctx *c, const double *ts, const doubl
 int launch_hot_source(pbte_ctx *c, const double *vdf, double tc5, double *work, cudaStream_t s);
 int launch_gsis_hot_apply(pbte_ctx *c, const pbte_gsis_ops *o, const double *vdf, double tc5, double *aa_src,
                           cudaStream_t s);
+// one step of the FP32 GSIS product on the folded FP32 distribution: 0 hot
+// source with the inverses, 1 kinetic wall traces, 2 damped correction
+int launch_gsis_product32(pbte_ctx *c, const pbte_gsis_ops *o, int step, float *vdf32, double tc5,
+                          const double *tri_fc_fc, int nk, const int32_t *tri_list, const int32_t *lfc_list,
+                          double *aa_src_or_wall, const double *uq, const double *tri_hmin, double tau_thr,
+                          int use_hmin, cudaStream_t s);
 int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk,
                       const int32_t *tri_list, const int32_t *lfc_list, double *out,
                       cudaStream_t s);

@@ -923,7 +923,14 @@ int launch_fixed_point32(pbte_ctx *c, const double *ts, const double *qxs, const
         if (rc == PBTE_OK && fw_out) rc = wall_flux_impl<float>(c, vdf32, fw_out, s);
         return rc;
     }
-    // moments, element integrals and wall emission in one launch
+    return launch_fold_epilogue32(c, vdf32, ts_out, qxs_out, qys_out, fw_out, temp, qx, qy, s);
+}
+
+// moments, element integrals and wall emission of a folded FP32 distribution
+// (one row per distinct in-plane velocity) in one launch
+int launch_fold_epilogue32(pbte_ctx *c, const float *vdf32, double *ts_out, double *qxs_out, double *qys_out,
+                           double *fw_out, double *temp, double *qx, double *qy, cudaStream_t s) {
+    if (!(c->nd == 3 || c->nd == 6 || c->nd == 10)) return PBTE_ERR_UNSUPPORTED;
     const int nch = (c->n_udir + kMomChunk - 1) / kMomChunk;
     const int ntiles = (c->n_tris + 31) / 32;
     const int nwall = fw_out ? c->n_wall_ad : 0;

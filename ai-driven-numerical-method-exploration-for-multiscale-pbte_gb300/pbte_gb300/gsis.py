@@ -36,11 +36,12 @@ import numpy as np
 import torch
 
 from . import _lib
+from .device import bury, device_lock, empty_graveyard
 from .constants import BC_NONTHERMALISING, BC_PERIODIC, BC_THERMALISING
 from .trace_nd import NestedDissectionSolver
 from .trace_solver import TraceSolver
 
-__all__ = ["GSIS", "local_blocks"]
+__all__ = ["GSIS", "GsisFixedPoint", "local_blocks"]
 
 
 def _mirror_perm(nf):
@@ -345,3 +346,165 @@ class GSIS:
                                   float(s.case.flow.tau_thr), int(self.use_hmin), m.ts.data_ptr(),
                                   m.qxs.data_ptr(), m.qys.data_ptr(), m.temp.data_ptr(), m.qx.data_ptr(),
                                   m.qy.data_ptr(), st), "correct")
+
+
+class GsisFixedPoint:
+    """One GSIS iteration as an affine map ``u -> G(u)`` on the sweep's inputs
+    ``u = [ts, qxs, qys, flux_wall]`` (the moment sources, then the adiabatic
+    wall emission when there are adiabatic walls): sweep, then the whole
+    acceleration step (``acceleration/__init__.py:95-115``), then the new
+    moments and the emission of the corrected distribution.  Its fixed point
+    is the GSIS solver's (``Solver.step`` iterates exactly this map), so the
+    mixed-precision solve can refine it in FP64 around FP32 products.
+
+    ``precision="fp64"``: the FP64 drop-in's kernels on the solver's
+    distribution.  ``precision="fp32"`` (homogeneous only: the walls' fixed
+    temperatures dropped, the map's linear part): the folded FP32 sweep and
+    the FP32 GSIS kernels on an FP32 distribution with FP32 angular sums; the
+    trace right-hand side, the trace solve and the local recovery stay FP64.
+    The interface is :class:`pbte_gb300.krylov.FixedPointOperator`'s."""
+
+    native_product = False   # no fused native GMRES chunks for this product
+
+    def __init__(self, solver, precision: str = "fp64", homogeneous: bool = False):
+        s = solver
+        if s.acc is None:
+            raise ValueError("GsisFixedPoint needs a solver with the GSIS acceleration")
+        if s.bcdata.has_periodic:
+            raise NotImplementedError("mixed-precision GSIS with periodic faces")
+        if precision == "fp32" and not homogeneous:
+            raise ValueError("the FP32 GSIS product is the homogeneous map only")
+        self.s = s
+        self.acc = s.acc
+        self.nd, self.nt = s.ndof, s.n_tris
+        self.k = self.nd * self.nt
+        self.nmom = 3 * self.k
+        self.wall = bool(s.bcdata.has_nonthermalising)
+        self.nwall = s.mesh.n_faces * self.nd if self.wall else 0
+        self.per = False
+        self.nper = 0
+        self.n = self.nmom + self.nwall
+        self.precision = precision
+        self.homogeneous = homogeneous
+        self.integrals = True
+        dev = s.device
+        f64 = dict(dtype=torch.float64, device=dev)
+        self.uin = torch.zeros(self.n, **f64)
+        self.uout = torch.zeros_like(self.uin)
+        self.temp = torch.zeros(self.nt, **f64)
+        self.qx = torch.zeros(self.nt, **f64)
+        self.qy = torch.zeros(self.nt, **f64)
+        if precision == "fp64":
+            self.vdf = s.vdf
+        else:
+            self.vdf = torch.zeros((s.ctx.schedule()["unique_dirs"], self.nt, self.nd), dtype=torch.float32,
+                                   device=dev)
+            self.uq = torch.zeros_like(self.acc.uq)
+        self.sweeps = 0
+        self.graph = None
+        self.stream = torch.cuda.Stream(device=dev)
+
+    def _views(self, u):
+        k, m = self.k, self.nmom
+        fw = u[m:m + self.nwall].view(-1, self.nd) if self.wall else None
+        return (u[:k].view(self.nd, self.nt), u[k:2 * k].view(self.nd, self.nt),
+                u[2 * k:3 * k].view(self.nd, self.nt), fw, None)
+
+    @staticmethod
+    def _ptr(t):
+        return t.data_ptr() if t is not None else None
+
+    def _launch(self, st: int, done=None) -> None:
+        L = _lib.lib()
+        s, a = self.s, self.acc
+        ctx = s.ctx.handle
+        ts, qxs, qys, fw, _ = self._views(self.uin)
+        ots, oqxs, oqys, ofw, _ = self._views(self.uout)
+        fw_in = fw if fw is not None else s.ctx.flux_wall
+        stream = torch.cuda.ExternalStream(st, device=s.device)
+        keep, a.done = a.done, done
+        try:
+            if self.precision == "fp64":
+                _lib.check(L.pbte_sweep(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), self.vdf.data_ptr(),
+                                        fw_in.data_ptr(), s.ctx.pbuf.data_ptr(), 0, st), "sweep")
+                _lib.check(L.pbte_gsis_hot_apply(ctx, ctypes.byref(a.ops), self.vdf.data_ptr(), float(a.tc5),
+                                                 a.aa_src.data_ptr(), st), "gsis_hot_apply")
+                a.rhs(a.aa_src, self.vdf, stream)
+                a.trace_solve(stream)
+                a.recover(a.aa_src, a.uq, stream)
+                _lib.check(L.pbte_correct(ctx, self.vdf.data_ptr(), a.uq.data_ptr(), a.tri_hmin.data_ptr(),
+                                          float(s.case.flow.tau_thr), int(a.use_hmin), ots.data_ptr(),
+                                          oqxs.data_ptr(), oqys.data_ptr(), self.temp.data_ptr(), self.qx.data_ptr(),
+                                          self.qy.data_ptr(), st), "correct")
+                if self.wall:
+                    _lib.check(L.pbte_wall_flux(ctx, self.vdf.data_ptr(), ofw.data_ptr(), st), "wall_flux")
+                return
+            v = self.vdf.data_ptr()
+            _lib.check(L.pbte_sweep_fold_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), fw_in.data_ptr(),
+                                             0.0 if self.homogeneous else 1.0, v, st), "sweep_fold_f32")
+            _lib.check(L.pbte_gsis_hot_apply_f32(ctx, ctypes.byref(a.ops), v, float(a.tc5), a.aa_src.data_ptr(), st),
+                       "gsis_hot_apply_f32")
+            if a.wall_all.size:
+                _lib.check(L.pbte_wall_trace_f32(ctx, v, a.tri_fc_fc.data_ptr(), int(a.wall_all.size),
+                                                 a.wall_tri.data_ptr(), a.wall_lfc.data_ptr(), a.wall_mom.data_ptr(),
+                                                 st), "wall_trace_f32")
+            _lib.check(L.pbte_gsis_trace_rhs(ctypes.byref(a.ops), a.aa_src.data_ptr(), a.wall_mom.data_ptr(),
+                                             a.ffa.data_ptr(), a._done_ptr(), st), "gsis_trace_rhs")
+            a.trace_solve(stream)
+            a.recover(a.aa_src, self.uq, stream)
+            _lib.check(L.pbte_correct_f32(ctx, v, self.uq.data_ptr(), a.tri_hmin.data_ptr(),
+                                          float(s.case.flow.tau_thr), int(a.use_hmin), st), "correct_f32")
+            _lib.check(L.pbte_fold_epilogue_f32(ctx, v, ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(),
+                                                self._ptr(ofw), None, None, None, st), "fold_epilogue_f32")
+        finally:
+            a.done = keep
+
+    def _capture(self):
+        with device_lock:
+            empty_graveyard()
+            torch.cuda.synchronize(self.s.device)
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+                self._launch(torch.cuda.current_stream().cuda_stream)
+        self.graph = g
+
+    def __del__(self):
+        bury(getattr(self, "graph", None))
+
+    def apply(self, u: torch.Tensor) -> torch.Tensor:
+        """G(u), stream-ordered on the current stream."""
+        self.uin.copy_(u)
+        if getattr(self.s, "use_graphs", True) and self.s.case.performance.trace_solver == "device":
+            if self.graph is None:
+                self._capture()
+            self.graph.replay()
+        else:
+            self._launch(torch.cuda.current_stream().cuda_stream)
+        self.sweeps += 1
+        return self.uout.clone()
+
+    def state(self) -> torch.Tensor:
+        """The state of the solver's current distribution and moments (a
+        restart's start): the moments, and the wall emission of ``vdf``."""
+        s = self.s
+        u = torch.zeros_like(self.uin)
+        ts, qxs, qys, fw, _ = self._views(u)
+        ts.copy_(s.mom.ts)
+        qxs.copy_(s.mom.qxs)
+        qys.copy_(s.mom.qys)
+        if self.wall:
+            s.ctx.wall_flux(s.vdf, out=fw)
+        return u
+
+    def publish(self) -> None:
+        """The last product's moments and emission into the solver's state."""
+        s = self.s
+        ts, qxs, qys, fw, _ = self._views(self.uout)
+        s.mom.ts.copy_(ts)
+        s.mom.qxs.copy_(qxs)
+        s.mom.qys.copy_(qys)
+        s.mom.temp.copy_(self.temp)
+        s.mom.qx.copy_(self.qx)
+        s.mom.qy.copy_(self.qy)
+        if self.wall:
+            s.ctx.flux_wall.copy_(fw)

@@ -92,7 +92,9 @@ class FixedPointOperator:
     def _ptr(t):
         return t.data_ptr() if t is not None else None
 
-    def _launch(self, s: int) -> None:
+    def _launch(self, s: int, done=None) -> None:
+        """The product's launches on stream ``s``; they honour the context's
+        stop flag (``done`` is for products with context-free launches)."""
         L = _lib.lib()
         ctx = self.s.ctx.handle
         p = self._ptr
@@ -256,7 +258,8 @@ class ArnoldiGraphs:
         ``pbte_gmres_columns_f32`` (which issues a chunk's launches from
         native code); None for the other forms."""
         op = self.op
-        if op.precision == "fp64" or self.dtype != torch.float32 or op.per:
+        if (op.precision == "fp64" or self.dtype != torch.float32 or op.per
+                or not getattr(op, "native_product", True)):
             return None
         p = op._ptr
         ts, qxs, qys, fw, _ = op._views(op.uin)
@@ -288,7 +291,7 @@ class ArnoldiGraphs:
         _lib.check(L.pbte_set_done_flag(ctx, self.state.data_ptr()), "set_done_flag")
         try:
             for j in range(j0, j1):
-                op._launch(s)
+                op._launch(s, done=self.state)
                 if self.precond is not None:
                     # w = M (q_j - (F(q_j) - g)), then CGS2 in place
                     v = self.Q[j] - (op.uout[:n] - (self.g if self.g is not None else 0.0))

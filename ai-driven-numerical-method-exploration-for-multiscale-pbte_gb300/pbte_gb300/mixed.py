@@ -1,11 +1,13 @@
 """Mixed precision: FP32 sweeps inside an FP64 defect-correction loop.
 
 The outer problem is the fixed point ``u = F(u) = T u + g`` of source
-iteration (``u``: the moments, plus the wall emission with adiabatic walls).
-Each outer step
+iteration (``u``: the moments, plus the wall emission with adiabatic walls),
+or, for a case with the GSIS acceleration, of the GSIS iteration (``F``: a
+sweep followed by the acceleration step, :class:`pbte_gb300.gsis.GsisFixedPoint`;
+the HDG trace solve stays FP64 in both of its forms).  Each outer step
 
 1. evaluates the FP64 defect ``r = F64(u) - u`` with one FP64 sweep, moments
-   and emission (exactly one CIS step of the FP64 solver);
+   and emission (exactly one CIS or GSIS step of the FP64 solver);
 2. solves the correction equation ``(I - T) d = r`` approximately with
    FP32 sweeps of the homogeneous problem (no wall sources): either source
    iteration (``method = "source"``) or GMRES (``method = "krylov"``), both
@@ -46,11 +48,21 @@ class MixedOptions:
 def run_mixed(solver, opts: MixedOptions | None = None):
     opts = opts or MixedOptions()
     c = solver.case
-    if solver.acc is not None:
-        raise NotImplementedError("mixed precision GSIS is not implemented; use precision='fp64'")
-    method = "krylov" if c.scheme.method == "krylov" else "source"
-    op64 = cached(solver, "fp64", lambda: FixedPointOperator(solver, "fp64"))
-    op32 = cached(solver, "fp32h", lambda: FixedPointOperator(solver, "fp32", homogeneous=True, integrals=False))
+    gsis = solver.acc is not None
+    if gsis:
+        # the fixed point of the GSIS iteration (not CIS's: GSIS converges to
+        # its own discrete fixed point), refined around FP32 GSIS products;
+        # the inner solve is GMRES, which does not stall on the slow wall
+        # modes that plain GSIS iteration meets with adiabatic walls
+        from .gsis import GsisFixedPoint
+        method = "krylov"
+        op64 = cached(solver, "gsis64", lambda: GsisFixedPoint(solver, "fp64"))
+        op32 = cached(solver, "gsis32h", lambda: GsisFixedPoint(solver, "fp32", homogeneous=True))
+    else:
+        method = "krylov" if c.scheme.method == "krylov" else "source"
+        op64 = cached(solver, "fp64", lambda: FixedPointOperator(solver, "fp64"))
+        op32 = cached(solver, "fp32h",
+                      lambda: FixedPointOperator(solver, "fp32", homogeneous=True, integrals=False))
     op64.sweeps = op32.sweeps = 0
     n = op64.n
     dev = solver.device
@@ -101,7 +113,7 @@ def run_mixed(solver, opts: MixedOptions | None = None):
     solver.ctx.sweep_count += sweeps64 + inner_sweeps
     rec = solver._record(sweeps64 + inner_sweeps, converged, np.array(history),
                          np.full(len(history), solver.mom.mass), wall,
-                         "KRYLOV" if method == "krylov" else "CIS",
+                         "GSIS" if gsis else ("KRYLOV" if method == "krylov" else "CIS"),
                          extra={"fp64_sweeps": sweeps64, "fp32_sweeps": inner_sweeps,
                                 "outer_steps": len(history), "final_defect": history[-1]})
     return rec

@@ -422,6 +422,33 @@ int pbte_gsis_trace_rhs(const pbte_gsis_ops *ops, const double *aa_src, const do
 int pbte_gsis_local_recover(const pbte_gsis_ops *ops, const double *aa_src, const double *u_trace, double *uq,
                             const int32_t *done, void *stream);
 
+/* The FP32 GSIS product of the mixed-precision GSIS solve (no reference
+ * counterpart: the inner operator of an FP64 defect correction around
+ * Acceleration.apply, acceleration/__init__.py:95-115).  The distribution
+ * is folded, vdf32[n_udir][n_tris][ndof]: one row per distinct in-plane
+ * velocity (an ordinate and its z-mirror twin see the same transport, so
+ * the pair is solved once and its weights summed).  No periodic faces; ndof
+ * 3, 6 or 10 (PBTE_ERR_UNSUPPORTED otherwise).
+ *  pbte_sweep_fold_f32: the moment sources of ts/qxs/qys and one FP32 sweep
+ *    (pbte_sweep_f32's arithmetic) into the folded rows;
+ *  pbte_fold_epilogue_f32: moments, element integrals (temp/qx/qy, all NULL
+ *    or none) and the adiabatic wall emission (flux_wall, may be NULL) of a
+ *    folded distribution;
+ *  pbte_gsis_hot_apply_f32, pbte_wall_trace_f32, pbte_correct_f32: the hot
+ *    source with the element inverses, the kinetic wall traces and the
+ *    damped update of the distribution (pbte_correct without its moment
+ *    outputs) on the folded distribution, with FP32 angular sums. */
+int pbte_sweep_fold_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
+                        const double *flux_wall, double wall_scale, float *vdf32, void *stream);
+int pbte_fold_epilogue_f32(pbte_ctx *ctx, const float *vdf32, double *ts, double *qxs, double *qys,
+                           double *flux_wall, double *temp, double *qx, double *qy, void *stream);
+int pbte_gsis_hot_apply_f32(pbte_ctx *ctx, const pbte_gsis_ops *ops, const float *vdf32, double tc5,
+                            double *aa_src, void *stream);
+int pbte_wall_trace_f32(pbte_ctx *ctx, const float *vdf32, const double *tri_fc_fc, int32_t nk,
+                        const int32_t *tri_list, const int32_t *lfc_list, double *out, void *stream);
+int pbte_correct_f32(pbte_ctx *ctx, float *vdf32, const double *uq, const double *tri_hmin, double tau_thr,
+                     int use_hmin, void *stream);
+
 /* Batched dense inverse of n matrices of order m (FP64, Gauss-Jordan with
  * partial pivoting), a[n][m][m] -> inv[n][m][m].  Replaces the
  * np.linalg.inv of build_local_operators (acceleration/assembly.py:100).

@@ -89,3 +89,16 @@ def test_c2_mixed_reaches_the_oracle_fixed_point(cuda, kn):
     # the heat flux as a vector field (q_y alone is ~1e-7 of q_x here: the
     # square is symmetric about y = 1/2)
     assert rel_l2(np.concatenate([rec.qx, rec.qy]), np.concatenate([z[f"{key}__qx"], z[f"{key}__qy"]])) <= 1e-8
+
+
+def test_c2_mixed_gsis_reaches_the_gsis_fixed_point(cuda):
+    """Kn_R = 0.01 (GSIS): the mixed solve against the FP64 GSIS drop-in
+    iterated to 1e-13 (the drop-in itself matches the oracle above): the GSIS
+    fixed point within 1e-8 relative L2."""
+    ref = Solver(square_case(*C2, tau_r=0.01, accflag=1, tol=1e-13, tmax=20000)).run()
+    assert ref.converged
+    rec = Solver(square_case(*C2, tau_r=0.01, accflag=1, tol=1e-8, tmax=20000, precision="mixed",
+                             krylov_restart=30)).run()
+    assert rec.converged
+    assert rel_l2(rec.temp, ref.temp) <= 1e-8
+    assert rel_l2(np.concatenate([rec.qx, rec.qy]), np.concatenate([ref.qx, ref.qy])) <= 1e-8

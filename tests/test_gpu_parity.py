@@ -284,6 +284,24 @@ def test_mixed_precision_reaches_fp64_fixed_point(cuda, method):
     assert rec.diagnostics["fp32_sweeps"] > rec.diagnostics["fp64_sweeps"]
 
 
+@pytest.mark.parametrize("name", ["gsis_deg2_adiabatic", "gsis_deg1_isothermal"])
+@pytest.mark.parametrize("graphs", [True, False])
+def test_mixed_gsis_reaches_the_gsis_fixed_point(cuda, name, graphs):
+    """Mixed-precision GSIS (FP64 GSIS defects, inner GMRES on FP32 GSIS
+    products with the FP64 trace solve) against the oracle's GSIS iterated to
+    1e-13: the GSIS fixed point (not CIS's) within 1e-8."""
+    o = Oracle(Solver(case_from_meta(name)).disc, nthreads=4)
+    r = o.run_source(tol=1e-13, tmax=20000, gsis=True)
+    assert r["converged"]
+    s = Solver(case_from_meta(name, precision="mixed"))
+    s.use_graphs = graphs
+    rec = s.run()
+    assert rec.converged and rec.scheme == "GSIS"
+    assert rec.diagnostics["fp32_sweeps"] > 0
+    assert _rel(rec.temp_dofs, o.ts) < 1e-8
+    assert _rel(rec.qx_dofs, o.qxs) < 1e-8
+
+
 @pytest.mark.parametrize("graphs", [True, False])
 @pytest.mark.parametrize("basis", [8, 100])
 def test_fp64_device_gmres_matches_oracle(cuda, graphs, basis):
