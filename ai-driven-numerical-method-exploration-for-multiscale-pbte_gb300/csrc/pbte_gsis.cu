@@ -513,13 +513,12 @@ __global__ void __launch_bounds__(kTraceThreads) wall_trace32_kernel(const float
     if (threadIdx.x < 3 * NF) out[(size_t)k * 3 * NF + threadIdx.x] = red[threadIdx.x][0];
 }
 
-// the correction's coefficients (correct_moments_kernel's arithmetic after
-// FP32 angular sums); the moments themselves come from the corrected
-// distribution afterwards
+// the correction's coefficients and new moments (correct_moments_kernel's
+// arithmetic after FP32 angular sums); ts/qxs/qys may be null
 __global__ void __launch_bounds__(kLanes *kChunks) correct_coef32_kernel(
     const float *vdf, const double *uq, const double *cx, const double *cy, const double *w, const double *tri_hmin,
-    int nu, int nt, int NP, double cv, double tau_r, double tau_thr, int use_hmin, double *coef,
-    const int32_t *done) {
+    int nu, int nt, int NP, double cv, double tau_r, double tau_thr, int use_hmin, double *coef, double *ts,
+    double *qxs, double *qys, const int32_t *done) {
     if (stopped(done)) return;
     const int total = nt * NP;
     const int t = blockIdx.x * kLanes + threadIdx.x;
@@ -539,9 +538,17 @@ __global__ void __launch_bounds__(kLanes *kChunks) correct_coef32_kernel(
     const double tau_loc = use_hmin ? tau_r / tri_hmin[i] : tau_r;
     const double beta = fmin(tau_loc, tau_thr) / tau_loc;
     const double tv = accd[0] / cv, qxv = accd[1], qyv = accd[2];
-    coef[t] = (uq[(size_t)m * nt + i] - tv) * beta * cv / 4.0 / kPi;
-    coef[total + t] = (uq[(size_t)(NP + m) * nt + i] - qxv) * beta;
-    coef[2 * total + t] = (uq[(size_t)(2 * NP + m) * nt + i] - qyv) * beta;
+    const double lt = (uq[(size_t)m * nt + i] - tv) * beta;
+    const double lqx = (uq[(size_t)(NP + m) * nt + i] - qxv) * beta;
+    const double lqy = (uq[(size_t)(2 * NP + m) * nt + i] - qyv) * beta;
+    coef[t] = lt * cv / 4.0 / kPi;
+    coef[total + t] = lqx;
+    coef[2 * total + t] = lqy;
+    if (ts) {
+        ts[(size_t)m * nt + i] = lt + tv;
+        qxs[(size_t)m * nt + i] = lqx + qxv;
+        qys[(size_t)m * nt + i] = lqy + qyv;
+    }
 }
 
 __global__ void correct_update32_kernel(float *vdf, const double *coef, const double *cx, const double *cy, int nu,
@@ -561,7 +568,7 @@ __global__ void correct_update32_kernel(float *vdf, const double *coef, const do
 int launch_gsis_product32(pbte_ctx *c, const pbte_gsis_ops *o, int step, float *vdf32, double tc5,
                           const double *tri_fc_fc, int nk, const int32_t *tri_list, const int32_t *lfc_list,
                           double *aa_src_or_wall, const double *uq, const double *tri_hmin, double tau_thr,
-                          int use_hmin, cudaStream_t s) {
+                          int use_hmin, double *const *mom_out, cudaStream_t s) {
     const int total = c->n_tris * c->nd;
     const int nu = c->n_udir;
     if (step == 0) {   // hot source with the element inverses -> aa_src
@@ -590,7 +597,8 @@ int launch_gsis_product32(pbte_ctx *c, const pbte_gsis_ops *o, int step, float *
     } else {   // the damped correction of the distribution
         correct_coef32_kernel<<<(total + kLanes - 1) / kLanes, dim3(kLanes, kChunks), 0, s>>>(
             vdf32, uq, c->d_ucx64, c->d_ucy64, c->d_uw64, tri_hmin, nu, c->n_tris, c->nd, c->cv, c->tau_r, tau_thr,
-            use_hmin, c->d_gsis, c->done);
+            use_hmin, c->d_gsis, mom_out ? mom_out[0] : nullptr, mom_out ? mom_out[1] : nullptr,
+            mom_out ? mom_out[2] : nullptr, c->done);
         const double drift = c->tau_c / c->tau_n * 3.0 / 4.0 / kPi / c->vg / c->vg;
         const int th = 256;
         correct_update32_kernel<<<dim3((total + th - 1) / th, std::min(nu, 16)), th, 0, s>>>(
@@ -665,7 +673,8 @@ extern "C" int pbte_gsis_hot_apply_f32(pbte_ctx *c, const pbte_gsis_ops *o, cons
     if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
     if (!vdf32 || !aa_src) return PBTE_ERR_ARG;
     return pbte::launch_gsis_product32(c, o, 0, const_cast<float *>(vdf32), tc5, nullptr, 0, nullptr, nullptr,
-                                       aa_src, nullptr, nullptr, 0.0, 0, reinterpret_cast<cudaStream_t>(stream));
+                                       aa_src, nullptr, nullptr, 0.0, 0, nullptr,
+                                       reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int pbte_wall_trace_f32(pbte_ctx *c, const float *vdf32, const double *tri_fc_fc, int32_t nk,
@@ -673,14 +682,17 @@ extern "C" int pbte_wall_trace_f32(pbte_ctx *c, const float *vdf32, const double
     if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
     if (!vdf32 || nk < 0 || (nk && (!tri_fc_fc || !tri_list || !lfc_list || !out))) return PBTE_ERR_ARG;
     return pbte::launch_gsis_product32(c, nullptr, 1, const_cast<float *>(vdf32), 0.0, tri_fc_fc, nk, tri_list,
-                                       lfc_list, out, nullptr, nullptr, 0.0, 0,
+                                       lfc_list, out, nullptr, nullptr, 0.0, 0, nullptr,
                                        reinterpret_cast<cudaStream_t>(stream));
 }
 
 extern "C" int pbte_correct_f32(pbte_ctx *c, float *vdf32, const double *uq, const double *tri_hmin,
-                                double tau_thr, int use_hmin, void *stream) {
+                                double tau_thr, int use_hmin, double *ts, double *qxs, double *qys, void *stream) {
     if (!fold_ok(c)) return c ? PBTE_ERR_UNSUPPORTED : PBTE_ERR_ARG;
     if (!vdf32 || !uq || !tri_hmin) return PBTE_ERR_ARG;
+    if ((ts == nullptr) != (qxs == nullptr) || (ts == nullptr) != (qys == nullptr)) return PBTE_ERR_ARG;
+    double *const mom[3] = {ts, qxs, qys};
     return pbte::launch_gsis_product32(c, nullptr, 2, vdf32, 0.0, nullptr, 0, nullptr, nullptr, nullptr, uq,
-                                       tri_hmin, tau_thr, use_hmin, reinterpret_cast<cudaStream_t>(stream));
+                                       tri_hmin, tau_thr, use_hmin, ts ? mom : nullptr,
+                                       reinterpret_cast<cudaStream_t>(stream));
 }

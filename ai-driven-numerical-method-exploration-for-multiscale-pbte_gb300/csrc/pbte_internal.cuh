@@ -200,7 +200,7 @@ int launch_gsis_hot_apply(pbte_ctx *c, const pbte_gsis_ops *o, const double *vdf
 int launch_gsis_product32(pbte_ctx *c, const pbte_gsis_ops *o, int step, float *vdf32, double tc5,
                           const double *tri_fc_fc, int nk, const int32_t *tri_list, const int32_t *lfc_list,
                           double *aa_src_or_wall, const double *uq, const double *tri_hmin, double tau_thr,
-                          int use_hmin, cudaStream_t s);
+                          int use_hmin, double *const *mom_out, cudaStream_t s);
 int launch_wall_trace(pbte_ctx *c, const double *vdf, const double *tri_fc_fc, int nk,
                       const int32_t *tri_list, const int32_t *lfc_list, double *out,
                       cudaStream_t s);

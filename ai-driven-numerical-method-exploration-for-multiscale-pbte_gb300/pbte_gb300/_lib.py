@@ -187,7 +187,7 @@ _SIGS = {
     "pbte_fold_epilogue_f32": ([_vp] * 9 + [_vp], ctypes.c_int),
     "pbte_gsis_hot_apply_f32": ([_vp, ctypes.POINTER(GsisOps), _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace_f32": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
-    "pbte_correct_f32": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp], ctypes.c_int),
+    "pbte_correct_f32": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_singular_count": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int], ctypes.c_int),
     "pbte_device_bytes_live": ([ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_factorise_f32": ([_vp, _vp], ctypes.c_int),

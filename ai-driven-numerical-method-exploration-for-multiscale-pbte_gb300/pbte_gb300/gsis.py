@@ -400,6 +400,7 @@ class GsisFixedPoint:
             self.vdf = torch.zeros((s.ctx.schedule()["unique_dirs"], self.nt, self.nd), dtype=torch.float32,
                                    device=dev)
             self.uq = torch.zeros_like(self.acc.uq)
+            self.scratch_mom = torch.zeros((3, self.nd, self.nt), **f64)
         self.sweeps = 0
         self.graph = None
         self.stream = torch.cuda.Stream(device=dev)
@@ -421,7 +422,12 @@ class GsisFixedPoint:
         ts, qxs, qys, fw, _ = self._views(self.uin)
         ots, oqxs, oqys, ofw, _ = self._views(self.uout)
         fw_in = fw if fw is not None else s.ctx.flux_wall
-        stream = torch.cuda.ExternalStream(st, device=s.device)
+        # the stream whose handle is st is the current one (direct launches,
+        # or the capturing stream); a stream object is not rebuilt from the
+        # handle, since torch maps a null handle to a new pool stream
+        stream = torch.cuda.current_stream(s.device)
+        if stream.cuda_stream != st:
+            raise RuntimeError("GsisFixedPoint launches on the current stream only")
         keep, a.done = a.done, done
         try:
             if self.precision == "fp64":
@@ -452,10 +458,17 @@ class GsisFixedPoint:
                                              a.ffa.data_ptr(), a._done_ptr(), st), "gsis_trace_rhs")
             a.trace_solve(stream)
             a.recover(a.aa_src, self.uq, stream)
+            # the new moments are the distribution's plus the damped corrections
+            # (correction.py: not the moments of the corrected distribution,
+            # whose flux part differs by tau_C / tau_N); the emission is the
+            # corrected distribution's
             _lib.check(L.pbte_correct_f32(ctx, v, self.uq.data_ptr(), a.tri_hmin.data_ptr(),
-                                          float(s.case.flow.tau_thr), int(a.use_hmin), st), "correct_f32")
-            _lib.check(L.pbte_fold_epilogue_f32(ctx, v, ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(),
-                                                self._ptr(ofw), None, None, None, st), "fold_epilogue_f32")
+                                          float(s.case.flow.tau_thr), int(a.use_hmin), ots.data_ptr(),
+                                          oqxs.data_ptr(), oqys.data_ptr(), st), "correct_f32")
+            if self.wall:
+                m = self.scratch_mom
+                _lib.check(L.pbte_fold_epilogue_f32(ctx, v, m[0].data_ptr(), m[1].data_ptr(), m[2].data_ptr(),
+                                                    ofw.data_ptr(), None, None, None, st), "fold_epilogue_f32")
         finally:
             a.done = keep
 

@@ -436,8 +436,10 @@ int pbte_gsis_local_recover(const pbte_gsis_ops *ops, const double *aa_src, cons
  *    folded distribution;
  *  pbte_gsis_hot_apply_f32, pbte_wall_trace_f32, pbte_correct_f32: the hot
  *    source with the element inverses, the kinetic wall traces and the
- *    damped update of the distribution (pbte_correct without its moment
- *    outputs) on the folded distribution, with FP32 angular sums. */
+ *    damped correction (pbte_correct: the distribution updated in place and
+ *    the new moments ts/qxs/qys = the distribution's plus the damped
+ *    corrections, all three NULL to skip; no element integrals) on the
+ *    folded distribution, with FP32 angular sums. */
 int pbte_sweep_fold_f32(pbte_ctx *ctx, const double *ts, const double *qxs, const double *qys,
                         const double *flux_wall, double wall_scale, float *vdf32, void *stream);
 int pbte_fold_epilogue_f32(pbte_ctx *ctx, const float *vdf32, double *ts, double *qxs, double *qys,
@@ -447,7 +449,7 @@ int pbte_gsis_hot_apply_f32(pbte_ctx *ctx, const pbte_gsis_ops *ops, const float
 int pbte_wall_trace_f32(pbte_ctx *ctx, const float *vdf32, const double *tri_fc_fc, int32_t nk,
                         const int32_t *tri_list, const int32_t *lfc_list, double *out, void *stream);
 int pbte_correct_f32(pbte_ctx *ctx, float *vdf32, const double *uq, const double *tri_hmin, double tau_thr,
-                     int use_hmin, void *stream);
+                     int use_hmin, double *ts, double *qxs, double *qys, void *stream);
 
 /* Batched dense inverse of n matrices of order m (FP64, Gauss-Jordan with
  * partial pivoting), a[n][m][m] -> inv[n][m][m].  Replaces the

@@ -285,6 +285,29 @@ def test_mixed_precision_reaches_fp64_fixed_point(cuda, method):
 
 
 @pytest.mark.parametrize("name", ["gsis_deg2_adiabatic", "gsis_deg1_isothermal"])
+def test_fp32_gsis_product_is_the_linear_part_of_the_gsis_step(cuda, name):
+    """The FP64 GSIS step as a map on the sweep inputs, G(u) = T u + g, is the
+    same captured or launched directly; and the FP32 GSIS product of the mixed
+    solve (homogeneous: walls at zero temperature) is its linear part T to
+    FP32 accuracy: G(u) - G(v) = T32 (u - v) within 1e-5."""
+    from pbte_gb300.gsis import GsisFixedPoint
+    out = {}
+    for graphs in (True, False):
+        s = Solver(case_from_meta(name, precision="mixed"))
+        s.use_graphs = graphs
+        op64, op32 = GsisFixedPoint(s, "fp64"), GsisFixedPoint(s, "fp32", homogeneous=True)
+        g = torch.Generator(device="cpu").manual_seed(3)
+        u = torch.randn(op64.n, generator=g, dtype=torch.float64).to(cuda)
+        v = torch.randn(op64.n, generator=g, dtype=torch.float64).to(cuda)
+        gu, gv = op64.apply(u), op64.apply(v)
+        t = op32.apply(u - v)
+        assert float((gu - gv - t).norm() / t.norm()) < 1e-5
+        out[graphs] = (gu, gv, t)
+    for a, b in zip(out[True], out[False]):
+        assert float((a - b).norm() / b.norm()) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["gsis_deg2_adiabatic", "gsis_deg1_isothermal"])
 @pytest.mark.parametrize("graphs", [True, False])
 def test_mixed_gsis_reaches_the_gsis_fixed_point(cuda, name, graphs):
     """Mixed-precision GSIS (FP64 GSIS defects, inner GMRES on FP32 GSIS
