@@ -43,6 +43,18 @@ class MixedOptions:
     #: 21/82/600 with four cycles): a fresh FP64 defect restarts GMRES where
     #: its early, fast convergence is, and FP32 round-off cannot stall it.
     inner_budget_restarts = 1
+    #: "fp32": the inner products are FP32 sweeps (the mixed-precision
+    #: solve); "fp64": FP64 products of the same map (T u = F64(u) - F64(0)),
+    #: the all-FP64 form of the same Krylov-accelerated defect correction, the
+    #: FP64 comparator where the plain FP64 iteration is too slow to run to
+    #: convergence (GSIS with adiabatic walls on large meshes)
+    inner_precision = "fp32"
+
+    def __init__(self, **kw):
+        for k, v in kw.items():
+            if not hasattr(type(self), k):
+                raise TypeError(f"unknown mixed-precision option {k!r}")
+            setattr(self, k, v)
 
 
 def run_mixed(solver, opts: MixedOptions | None = None):
@@ -63,6 +75,14 @@ def run_mixed(solver, opts: MixedOptions | None = None):
         op64 = cached(solver, "fp64", lambda: FixedPointOperator(solver, "fp64"))
         op32 = cached(solver, "fp32h",
                       lambda: FixedPointOperator(solver, "fp32", homogeneous=True, integrals=False))
+    inner64 = opts.inner_precision == "fp64"
+    g0 = None
+    if inner64:
+        method = "krylov"
+        if gsis:
+            op32 = cached(solver, "gsis64i", lambda: GsisFixedPoint(solver, "fp64"))
+        else:
+            op32 = cached(solver, "fp64i", lambda: FixedPointOperator(solver, "fp64"))
     op64.sweeps = op32.sweeps = 0
     n = op64.n
     dev = solver.device
@@ -74,6 +94,8 @@ def run_mixed(solver, opts: MixedOptions | None = None):
     converged = False
     sync(dev)
     t0 = time.perf_counter()
+    if inner64:
+        g0 = op32.apply(torch.zeros(n, dtype=torch.float64, device=dev))   # F64(0): the affine part
     fu = op64.apply(u)
     for outer in range(opts.max_outer):
         r = fu - u
@@ -97,11 +119,17 @@ def run_mixed(solver, opts: MixedOptions | None = None):
         else:
             cap = basis_cap(c, n)
             if ar32 is None:
-                bdt = torch.float32 if c.performance.inner_basis == "fp32" else torch.float64
-                ar32 = cached(solver, ("arnoldi_inner", cap, bdt),
-                              lambda: ArnoldiGraphs(op32, None, cap, dtype=bdt))
+                bdt = torch.float32 if c.performance.inner_basis == "fp32" and not inner64 else torch.float64
+                ar32 = cached(solver, ("arnoldi_inner", cap, bdt, inner64),
+                              lambda: ArnoldiGraphs(op32, g0, cap, dtype=bdt))
+                if inner64:
+                    ar32.set_g(g0)
             before = op32.sweeps
-            d, _, _ = gmres(lambda v: v - op32.apply(v), r, ar32, tol_abs=opts.inner_rtol * rn,
+            if inner64:
+                mv = lambda v: v - (op32.apply(v) - g0)   # noqa: E731
+            else:
+                mv = lambda v: v - op32.apply(v)          # noqa: E731
+            d, _, _ = gmres(mv, r, ar32, tol_abs=opts.inner_rtol * rn,
                             maxiter=min(opts.max_inner, opts.inner_budget_restarts * cap))
             inner_sweeps += op32.sweeps - before
         u = u + d
@@ -114,6 +142,8 @@ def run_mixed(solver, opts: MixedOptions | None = None):
     rec = solver._record(sweeps64 + inner_sweeps, converged, np.array(history),
                          np.full(len(history), solver.mom.mass), wall,
                          "GSIS" if gsis else ("KRYLOV" if method == "krylov" else "CIS"),
-                         extra={"fp64_sweeps": sweeps64, "fp32_sweeps": inner_sweeps,
+                         extra={"fp64_sweeps": sweeps64 + (inner_sweeps if inner64 else 0),
+                                "fp32_sweeps": 0 if inner64 else inner_sweeps,
+                                "inner_precision": opts.inner_precision,
                                 "outer_steps": len(history), "final_defect": history[-1]})
     return rec
