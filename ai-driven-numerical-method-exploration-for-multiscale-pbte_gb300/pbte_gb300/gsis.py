@@ -288,6 +288,9 @@ class GSIS:
         #: once it is set
         self.done = None
         self.solve_count = 0
+        #: host bytes this setup moved to the device (the element and face
+        #: blocks and the trace matrix the factorisation starts from)
+        self.h2d_bytes = int(A.nbytes + T.nbytes + B.nbytes + K.data.nbytes + K.indices.nbytes + K.indptr.nbytes)
 
     def diagnostics(self) -> dict:
         """The run-record entries of ``Acceleration.diagnostics``
