@@ -348,7 +348,7 @@ def main():
         rank_barrier(dist)
         torch.cuda.synchronize(dev)
 
-    def timed(s, k):
+    def timed(s, k, check=True):
         s.reset()
         flush.fill_(float(k))
         barrier()
@@ -357,7 +357,7 @@ def main():
         rec = s.run()
         b.record()
         barrier()
-        if not rec.converged:
+        if check and not rec.converged:
             raise RuntimeError(f"solve of {s.case.flow.tau_r} ({s.precision}) did not converge")
         return a.elapsed_time(b), rec
 
@@ -444,9 +444,10 @@ def main():
                 for prec in ("fp64", "mixed"):
                     sv = (fp64 if prec == "fp64" else solvers)[kn] if meth == method_for(kn) else \
                         Solver(make_case(kn, precision=prec, method=meth), device=str(dev))
-                    timed(sv, 0)
-                    ms, rec = timed(sv, 1)
+                    timed(sv, 0, check=False)
+                    ms, rec = timed(sv, 1, check=False)
                     row[f"{meth}_{prec}"] = {"ms": round(ms, 3), "iterations": int(rec.iterations),
+                                             "converged": bool(rec.converged),
                                              "err": float(f"{field_error(rec, ref):.3e}")}
             methods[str(kn)] = row
         torch.cuda.empty_cache()
@@ -503,6 +504,7 @@ def main():
         hc.iteration.tmax = 20
         h = Solver(hc, device=str(dev))
         hrec = h.run()
+        g.reset()
         grec = g.run()
         gsis = {"kn_r": 0.01, "iterations": int(grec.iterations),
                 "ms_per_iteration": round(1e3 * grec.wall_clock / grec.iterations, 3),
