@@ -183,5 +183,9 @@ __device__ __forceinline__ int lu_solve(T (&A)[N][N], T (&b)[N]) {
 // ring-pipelined sweep (pbte_sweep.cu); PBTE_ERR_UNSUPPORTED when it does not fit
 template <typename T, bool PRE>
 int launch_ring(pbte_ctx *c, const SweepParams<T> &P, cudaStream_t s);
+// the parameters of a folded FP32 sweep (rows by distinct velocity, factored
+// in registers) of context c, with `done` as its stop flag
+SweepParams<float> fold_params32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale,
+                                 const int32_t *done);
 
 }  // namespace pbte

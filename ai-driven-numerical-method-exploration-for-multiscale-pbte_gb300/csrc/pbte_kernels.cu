@@ -760,6 +760,18 @@ int launch_sweep64(pbte_ctx *c, double *vdf, const double *fw, const double *pbu
     return sweep_dispatch<double, false>(c, P, s);
 }
 
+SweepParams<float> fold_params32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale,
+                                 const int32_t *done) {
+    SweepParams<float> P = make_params<float>(c);
+    P.cells = c->d_cells32; P.ref = c->d_ref32; P.S = c->d_S32; P.vdf = vdf32;
+    P.flux_wall = fw; P.wall_scale = (float)wall_scale;
+    P.store_twin = 0;
+    P.by_udir = 1;
+    P.lu32 = nullptr;
+    P.done = done;
+    return P;
+}
+
 int launch_sweep32(pbte_ctx *c, float *vdf32, const double *fw, double wall_scale, cudaStream_t s,
                    bool store_twin, bool by_udir) {
     SweepParams<float> P = make_params<float>(c);

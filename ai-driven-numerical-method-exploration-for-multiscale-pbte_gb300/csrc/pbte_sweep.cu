@@ -31,6 +31,9 @@
 // passed L+R-1, and every level reads its inflow before it arrives.
 #include <algorithm>
 #include <type_traits>
+#include <vector>
+
+#include "pbte_internal.cuh"
 
 #include "pbte_device.cuh"
 
@@ -99,10 +102,12 @@ __device__ __forceinline__ void store_row(T *o, const T (&v)[NP]) {
 
 // TPG: threads per group; GMAX: the most groups the kernel is compiled for
 // (its launch bound); CH: levels may be wider than TPG * CPT (run in chunks)
+// The sweep of one velocity (block `bid` of the case's grid); the body of
+// sweep_ring_kernel (one case) and sweep_ring_batch_kernel (many cases).
 template <typename T, int DEG, bool PRECOMP, int CPT, int TPG, int GMAX, bool CH>
-__global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P, RingParams Q) {
+__device__ __forceinline__ void ring_body(const SweepParams<T> &P, const RingParams &Q, int bid,
+                                          unsigned char *smem_raw) {
     constexpr int NP = Shape<DEG>::NP, NF = Shape<DEG>::NF;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     T *sref = reinterpret_cast<T *>(smem_raw);
     T *ring = sref + 6 * NP * NP;
     T *far = ring + Q.far_offset;
@@ -110,8 +115,8 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
     const T *__restrict__ rf = reinterpret_cast<const T *>(Q.rf);
     const int32_t *__restrict__ ri = Q.ri;
     const int64_t M = Q.stride;
-    const int u = Q.unfold ? P.udir_of[blockIdx.x] : (int)blockIdx.x;
-    const int d = Q.unfold ? (int)blockIdx.x : Q.udir_rep[u];
+    const int u = Q.unfold ? P.udir_of[bid] : bid;
+    const int d = Q.unfold ? bid : Q.udir_rep[u];
     const int d2 = Q.unfold ? -1 : Q.udir_twin[u];
     for (int k = threadIdx.x; k < 6 * NP * NP; k += blockDim.x) sref[k] = P.ref[k];
     __syncthreads();
@@ -392,6 +397,40 @@ __global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P
     if (sing) atomicAdd(P.singular, sing);
 }
 
+template <typename T, int DEG, bool PRECOMP, int CPT, int TPG, int GMAX, bool CH>
+__global__ void __launch_bounds__(GMAX * TPG) sweep_ring_kernel(SweepParams<T> P, RingParams Q) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ring_body<T, DEG, PRECOMP, CPT, TPG, GMAX, CH>(P, Q, (int)blockIdx.x, smem_raw);
+}
+
+// Many cases of one degree in one launch: the blocks of case k are
+// block0[k] .. block0[k] + nblocks[k] - 1 (cases ordered by block0); each
+// block copies its case's parameters into shared memory and sweeps one of
+// its velocities.  The launch's shared memory is the largest ring of the
+// cases; each case's far slots start after its own ring.
+struct RingCase {
+    SweepParams<float> P;
+    RingParams Q;
+    int block0, nblocks;
+};
+
+template <int DEG, int CPT, int TPG, int GMAX>
+__global__ void __launch_bounds__(GMAX * TPG) sweep_ring_batch_kernel(const RingCase *cases, int ncases) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ RingCase sc;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = ncases - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (cases[mid].block0 <= (int)blockIdx.x) lo = mid;
+            else hi = mid - 1;
+        }
+        sc = cases[lo];
+    }
+    __syncthreads();
+    ring_body<float, DEG, false, CPT, TPG, GMAX, true>(sc.P, sc.Q, (int)blockIdx.x - sc.block0, smem_raw);
+}
+
 template <typename T, int DEG, bool PRE, int TPG, int GMAX>
 static int ring_launch_cpt(pbte_ctx *c, const SweepParams<T> &P, const RingParams &Q, int cpt, size_t shm,
                            cudaStream_t s) {
@@ -574,3 +613,136 @@ int launch_factorise32(pbte_ctx *c, cudaStream_t s) {
 }
 
 }  // namespace pbte
+
+// ---------------------------------------------------------------------------
+// Many cases' folded FP32 sweeps in one launch per degree (pbte_sweep_batch_*)
+struct pbte_sweep_batch {
+    struct Group {
+        int deg = 0, tpg = 64, groups = 4, nblocks = 0;
+        size_t shm = 0;
+        pbte::RingCase *d_cases = nullptr;
+        int ncases = 0;
+    };
+    std::vector<Group> groups;
+    std::vector<pbte_batch_item> items;
+};
+
+namespace pbte {
+namespace {
+
+template <int DEG, int CPT, int TPG, int GMAX>
+int batch_go(const pbte_sweep_batch::Group &g, cudaStream_t s) {
+    auto kern = sweep_ring_batch_kernel<DEG, CPT, TPG, GMAX>;
+    if (g.shm > 48 * 1024 &&
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)g.shm) != cudaSuccess)
+        return PBTE_ERR_CUDA;
+    kern<<<g.nblocks, g.groups * TPG, g.shm, s>>>(g.d_cases, g.ncases);
+    return cudaGetLastError() == cudaSuccess ? PBTE_OK : PBTE_ERR_CUDA;
+}
+
+int batch_launch(const pbte_sweep_batch::Group &g, cudaStream_t s) {
+    if (g.tpg == 128) {
+        if (g.deg == 1) return batch_go<1, 1, 128, 4>(g, s);
+        if (g.deg == 2) return batch_go<2, 1, 128, 4>(g, s);
+    } else if (g.groups > 4) {
+        if (g.deg == 1) return batch_go<1, 1, 64, 8>(g, s);
+        if (g.deg == 2) return batch_go<2, 1, 64, 8>(g, s);
+    } else {
+        if (g.deg == 1) return batch_go<1, 1, 64, 4>(g, s);
+        if (g.deg == 2) return batch_go<2, 1, 64, 4>(g, s);
+        if (g.deg == 3) return batch_go<3, 1, 64, 4>(g, s);
+    }
+    return PBTE_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+}  // namespace pbte
+
+extern "C" int pbte_sweep_batch_destroy(pbte_sweep_batch *b) {
+    if (!b) return PBTE_OK;
+    for (auto &g : b->groups)
+        if (g.d_cases) cudaFree(g.d_cases);
+    delete b;
+    return PBTE_OK;
+}
+
+static int batch_create_impl(int32_t n, const pbte_batch_item *items, int32_t groups, int32_t width,
+                             pbte_sweep_batch **out) {
+    if (!out || n <= 0 || !items || groups < 1 || groups > pbte::kMaxGroups || (width != 64 && width != 128))
+        return PBTE_ERR_ARG;
+    *out = nullptr;
+    const int dev = items[0].ctx ? items[0].ctx->device : -1;
+    for (int i = 0; i < n; ++i) {
+        const pbte_batch_item &it = items[i];
+        if (!it.ctx || !it.ts || !it.qxs || !it.qys || !it.vdf32 || (it.ctx->n_wall_ad && !it.flux_wall))
+            return PBTE_ERR_ARG;
+        if (it.ctx->device != dev) return PBTE_ERR_ARG;
+        if (it.ctx->has_periodic || it.ctx->deg > 3 || it.ctx->ring_W <= 0) return PBTE_ERR_UNSUPPORTED;
+    }
+    auto *b = new pbte_sweep_batch();
+    b->items.assign(items, items + n);
+    for (int deg = 1; deg <= 3; ++deg) {
+        pbte_sweep_batch::Group g;
+        g.deg = deg;
+        g.tpg = (deg <= 2 && width == 128) ? 128 : 64;
+        g.groups = (deg == 3 || g.tpg == 128) ? std::min(groups, 4) : groups;
+        std::vector<pbte::RingCase> cases;
+        for (int i = 0; i < n; ++i) {
+            pbte_ctx *c = items[i].ctx;
+            if (c->deg != deg) continue;
+            pbte::RingCase rc{};
+            rc.P = pbte::fold_params32(c, items[i].vdf32, items[i].flux_wall, items[i].wall_scale, items[i].done);
+            const size_t ring_vals = (size_t)c->ring_R * c->ring_W * c->nd;
+            rc.Q = pbte::RingParams{c->d_rf32, c->d_ri, (int64_t)c->nclass * c->n_tris, c->d_class_W, c->d_class_R,
+                                    c->d_udir_rep, c->d_udir_twin, g.groups, (int)ring_vals, 0};
+            rc.block0 = g.nblocks;
+            rc.nblocks = c->n_udir;
+            g.nblocks += c->n_udir;
+            g.shm = std::max(g.shm, sizeof(float) * ((size_t)6 * c->nd * c->nd + ring_vals + (size_t)c->far_max * c->nd));
+            cases.push_back(rc);
+        }
+        if (cases.empty()) continue;
+        if (g.shm > 200 * 1024) {
+            pbte_sweep_batch_destroy(b);
+            return PBTE_ERR_UNSUPPORTED;
+        }
+        g.ncases = (int)cases.size();
+        if (cudaMalloc((void **)&g.d_cases, cases.size() * sizeof(pbte::RingCase)) != cudaSuccess) {
+            pbte_sweep_batch_destroy(b);
+            return PBTE_ERR_NOMEM;
+        }
+        b->groups.push_back(g);
+        if (cudaMemcpy(g.d_cases, cases.data(), cases.size() * sizeof(pbte::RingCase), cudaMemcpyHostToDevice) !=
+            cudaSuccess) {
+            pbte_sweep_batch_destroy(b);
+            return PBTE_ERR_CUDA;
+        }
+    }
+    *out = b;
+    return PBTE_OK;
+}
+
+extern "C" int pbte_sweep_batch_create(int32_t n, const pbte_batch_item *items, int32_t groups, int32_t width,
+                                       pbte_sweep_batch **out) {
+    try {
+        return batch_create_impl(n, items, groups, width, out);
+    } catch (...) {
+        if (out) *out = nullptr;
+        return PBTE_ERR_NOMEM;
+    }
+}
+
+extern "C" int pbte_sweep_batch_run(pbte_sweep_batch *b, int with_sources, void *stream) {
+    if (!b) return PBTE_ERR_ARG;
+    const cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    if (with_sources)
+        for (const auto &it : b->items) {
+            const int rc = pbte::launch_sources(it.ctx, it.ts, it.qxs, it.qys, true, s);
+            if (rc) return rc;
+        }
+    for (const auto &g : b->groups) {
+        const int rc = pbte::batch_launch(g, s);
+        if (rc) return rc;
+    }
+    return PBTE_OK;
+}

@@ -123,6 +123,12 @@ class GsisOps(ctypes.Structure):
                 ("aa_trace_t", _vp), ("tri_faces", _vp)]
 
 
+class BatchItem(ctypes.Structure):
+    """Mirror of ``pbte_batch_item``."""
+    _fields_ = [("ctx", _vp), ("ts", _vp), ("qxs", _vp), ("qys", _vp), ("flux_wall", _vp),
+                ("wall_scale", ctypes.c_double), ("vdf32", _vp), ("done", _vp)]
+
+
 _SIGS = {
     "pbte_ctx_create": ([ctypes.POINTER(CaseDesc), ctypes.c_int, ctypes.POINTER(_vp)], ctypes.c_int),
     "pbte_ctx_destroy": ([_vp], ctypes.c_int),
@@ -188,6 +194,10 @@ _SIGS = {
     "pbte_gsis_hot_apply_f32": ([_vp, ctypes.POINTER(GsisOps), _vp, ctypes.c_double, _vp, _vp], ctypes.c_int),
     "pbte_wall_trace_f32": ([_vp, _vp, _vp, ctypes.c_int32, _vp, _vp, _vp, _vp], ctypes.c_int),
     "pbte_correct_f32": ([_vp, _vp, _vp, _vp, ctypes.c_double, ctypes.c_int, _vp, _vp, _vp, _vp], ctypes.c_int),
+    "pbte_sweep_batch_create": ([ctypes.c_int32, ctypes.POINTER(BatchItem), ctypes.c_int32, ctypes.c_int32,
+                                 ctypes.POINTER(_vp)], ctypes.c_int),
+    "pbte_sweep_batch_run": ([_vp, ctypes.c_int, _vp], ctypes.c_int),
+    "pbte_sweep_batch_destroy": ([_vp], ctypes.c_int),
     "pbte_singular_count": ([_vp, ctypes.POINTER(ctypes.c_int64), ctypes.c_int], ctypes.c_int),
     "pbte_device_bytes_live": ([ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "pbte_factorise_f32": ([_vp, _vp], ctypes.c_int),

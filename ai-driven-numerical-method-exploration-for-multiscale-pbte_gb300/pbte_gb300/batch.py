@@ -14,15 +14,18 @@ and every kernel's arithmetic is independent of what else runs.
 """
 from __future__ import annotations
 
+import ctypes
 import threading
 import time
 
+import numpy as np
 import torch
 
+from .device import bury, device_lock, empty_graveyard
 from .krylov import ArnoldiGraphs
 from .solver import RunRecord, Solver
 
-__all__ = ["BatchSolver"]
+__all__ = ["BatchSolver", "LockstepBatch", "tune_batch_shape"]
 
 
 class BatchSolver:
@@ -93,3 +96,218 @@ class BatchSolver:
             if e is not None:
                 raise e
         return results   # type: ignore[return-value]
+
+
+class LockstepBatch:
+    """Mixed-precision solves of many uneven cases advanced together, every
+    inner FP32 product of all of them swept in ONE launch per DG order.
+
+    Each case runs the defect correction of :func:`pbte_gb300.mixed.run_mixed`
+    (FP64 defects; one inner GMRES cycle per outer step on FP32 products --
+    source-iteration steps for CIS/GMRES cases, GSIS steps for GSIS cases).
+    The cases' outer steps go in lockstep: all FP64 defects, then the inner
+    cycles column by column, where column j of every case is [its moment
+    sources] + one batched sweep (``pbte_sweep_batch_run``: the blocks are
+    the distinct velocities of all cases of an order) + [its epilogue or GSIS
+    chain, CGS2, rotation, next basis vector].  A case whose cycle has stopped
+    (its device stop state) skips the rest of the cycle, and one that has
+    converged skips everything; the host checks the states once per chunk of
+    columns.  With ``use_graphs`` a chunk of all cases is one CUDA graph.
+
+    Each case's arithmetic is the one it has alone (the batched sweep gives
+    the single sweep's bits), so the results are the solo results.
+    ``shape = (groups, threads per group)`` is the batched sweep's block
+    shape, the autotuner's knob (:func:`tune_batch_shape`)."""
+
+    CHUNK = 10
+
+    def __init__(self, solvers: list[Solver], shape: tuple[int, int] = (4, 128), use_graphs: bool = True,
+                 opts=None):
+        from . import _lib
+        from .krylov import FixedPointOperator, basis_cap, cached
+        from .mixed import MixedOptions
+
+        if not solvers:
+            raise ValueError("empty batch")
+        self.solvers = list(solvers)
+        self.device = self.solvers[0].device
+        if any(s.device != self.device for s in self.solvers):
+            raise ValueError("all solves of a batch run on one device")
+        if any(s.precision != "mixed" for s in self.solvers):
+            raise ValueError("a lockstep batch runs mixed-precision solves")
+        self.opts = opts or MixedOptions()
+        self.use_graphs = use_graphs
+        self.shape = shape
+        self.cases = []
+        for s in self.solvers:
+            c = s.case
+            if s.acc is not None:
+                from .gsis import GsisFixedPoint
+                op64 = cached(s, "gsis64", lambda s=s: GsisFixedPoint(s, "fp64"))
+                op32 = cached(s, "gsis32h", lambda s=s: GsisFixedPoint(s, "fp32", homogeneous=True))
+            else:
+                op64 = cached(s, "fp64", lambda s=s: FixedPointOperator(s, "fp64"))
+                op32 = cached(s, "fp32h",
+                              lambda s=s: FixedPointOperator(s, "fp32", homogeneous=True, integrals=False))
+            cap = basis_cap(c, op64.n)
+            bdt = torch.float32 if c.performance.inner_basis == "fp32" else torch.float64
+            ar = cached(s, ("arnoldi_inner", cap, bdt, False), lambda o=op32, m=cap, d=bdt: ArnoldiGraphs(o, None, m, d))
+            ar._cycle_buffers()
+            self.cases.append({"s": s, "op64": op64, "op32": op32, "ar": ar, "cap": cap})
+        items = (_lib.BatchItem * len(self.cases))(*[k["op32"].batch_item(k["ar"].state) for k in self.cases])
+        h = ctypes.c_void_p()
+        _lib.check(_lib.lib().pbte_sweep_batch_create(len(self.cases), items, int(shape[0]), int(shape[1]),
+                                                      ctypes.byref(h)), "sweep_batch_create")
+        self._items = items
+        self.handle = h
+        self.graphs = {}
+        self.stream = torch.cuda.Stream(device=self.device)
+        self.wall_clock = 0.0
+
+    def __del__(self):
+        from . import _lib
+        bury(*getattr(self, "graphs", {}).values())
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            _lib.lib().pbte_sweep_batch_destroy(h)
+
+    # -- one chunk of columns of every case's cycle ----------------------------
+    def _record(self, j0: int, j1: int) -> None:
+        from . import _lib
+        L = _lib.lib()
+        s = torch.cuda.current_stream().cuda_stream
+        for k in self.cases:
+            _lib.check(L.pbte_set_done_flag(k["s"].ctx.handle, k["ar"].state.data_ptr()), "set_done_flag")
+        try:
+            for j in range(j0, j1):
+                _lib.check(L.pbte_sweep_batch_run(self.handle, 1, s), "sweep_batch_run")
+                for k in self.cases:
+                    if j < k["cap"]:
+                        k["op32"].after_sweep(s, done=k["ar"].state)
+                        k["ar"].column_tail(j, s)
+        finally:
+            for k in self.cases:
+                _lib.check(L.pbte_set_done_flag(k["s"].ctx.handle, None), "set_done_flag")
+
+    def _chunk(self, j0: int, j1: int) -> None:
+        if not self.use_graphs:
+            self._record(j0, j1)
+            return
+        g = self.graphs.get((j0, j1))
+        if g is None:
+            with device_lock:
+                empty_graveyard()
+                torch.cuda.synchronize(self.device)
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=self.stream, capture_error_mode="thread_local"):
+                    self._record(j0, j1)
+            self.graphs[(j0, j1)] = g
+        g.replay()
+
+    def run(self) -> list[RunRecord]:
+        """Solve every case from zero; the records in the solvers' order."""
+        from .krylov import _solve_upper
+
+        o = self.opts
+        dev = self.device
+        for k in self.cases:
+            k["s"].reset()
+            k["op64"].sweeps = k["op32"].sweeps = 0
+            k.update(u=torch.zeros(k["op64"].n, dtype=torch.float64, device=dev), history=[], inner=0,
+                     done=False, converged=False)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for k in self.cases:
+            k["fu"] = k["op64"].apply(k["u"])
+        mmax = max(k["cap"] for k in self.cases)
+        for _ in range(o.max_outer):
+            live = [k for k in self.cases if not k["done"]]
+            if not live:
+                break
+            norms = torch.stack([torch.stack([torch.linalg.vector_norm(k["fu"] - k["u"]),
+                                              torch.linalg.vector_norm(k["fu"])]) for k in live]).cpu().numpy()
+            for k, (rn, fn) in zip(live, norms):
+                fn = float(fn) or 1.0
+                k["rn"] = float(rn)
+                k["history"].append(float(rn) / fn)
+                if rn <= o.refine_tol * fn:
+                    k["done"] = k["converged"] = True
+                elif k["op64"].sweeps + k["inner"] >= k["s"].case.iteration.tmax:
+                    k["done"] = True
+            for k in self.cases:
+                if k["done"]:
+                    k["ar"].state.fill_(9)            # every launch of this case returns at once
+                else:
+                    r = k["fu"] - k["u"]
+                    k["ar"].begin_cycle(r, k["rn"], o.inner_rtol * k["rn"])
+            if all(k["done"] for k in self.cases):
+                break
+            for j0 in range(0, mmax, self.CHUNK):
+                self._chunk(j0, min(mmax, j0 + self.CHUNK))
+                states = torch.stack([k["ar"].state[0] for k in self.cases]).cpu().numpy()
+                if all(int(v) != 0 or k["done"] or j0 + self.CHUNK >= k["cap"]
+                       for v, k in zip(states, self.cases)):
+                    break
+            for k in self.cases:
+                if k["done"]:
+                    continue
+                kk, _, rmat, gam, _, _ = k["ar"].end_cycle()
+                k["inner"] += kk
+                if kk:
+                    ar = k["ar"]
+                    y = torch.from_numpy(_solve_upper(rmat, gam[:kk])).to(device=dev, dtype=ar.Q.dtype)
+                    k["u"] = k["u"] + (ar.Q[:kk].T @ y).to(torch.float64)
+                k["fu"] = k["op64"].apply(k["u"])
+        torch.cuda.synchronize(dev)
+        self.wall_clock = time.perf_counter() - t0
+        recs = []
+        for k in self.cases:
+            s = k["s"]
+            k["op64"].publish()
+            s64 = k["op64"].sweeps
+            s.ctx.sweep_count += s64 + k["inner"]
+            h = k["history"] or [float("nan")]
+            recs.append(s._record(s64 + k["inner"], k["converged"], np.array(h), np.full(len(h), s.mom.mass),
+                                  self.wall_clock, "GSIS" if s.acc is not None else
+                                  ("KRYLOV" if s.case.scheme.method == "krylov" else "CIS"),
+                                  extra={"fp64_sweeps": s64, "fp32_sweeps": k["inner"], "inner_precision": "fp32",
+                                         "outer_steps": len(h), "final_defect": h[-1], "batched": len(self.cases)}))
+        return recs
+
+
+def tune_batch_shape(solvers, shapes=((4, 64), (8, 64), (2, 128), (4, 128)), reps: int = 3) -> dict:
+    """The autotuner for a batch: times one batched sweep of every case at
+    each block shape (CUDA events, after a warm-up launch) and returns
+    ``{"choice": (groups, width), "ms": {shape: ms}}``."""
+    from . import _lib
+    from .krylov import FixedPointOperator, cached
+
+    ops = []
+    for s in solvers:
+        if s.acc is not None:
+            from .gsis import GsisFixedPoint
+            ops.append(cached(s, "gsis32h", lambda s=s: GsisFixedPoint(s, "fp32", homogeneous=True)))
+        else:
+            ops.append(cached(s, "fp32h", lambda s=s: FixedPointOperator(s, "fp32", homogeneous=True,
+                                                                             integrals=False)))
+    items = (_lib.BatchItem * len(ops))(*[op.batch_item(None) for op in ops])
+    L = _lib.lib()
+    out = {}
+    for g, w in shapes:
+        h = ctypes.c_void_p()
+        rc = L.pbte_sweep_batch_create(len(ops), items, g, w, ctypes.byref(h))
+        if rc != 0:
+            continue
+        st = torch.cuda.current_stream().cuda_stream
+        _lib.check(L.pbte_sweep_batch_run(h, 1, st), "sweep_batch_run")
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        for _ in range(reps):
+            _lib.check(L.pbte_sweep_batch_run(h, 1, st), "sweep_batch_run")
+        b.record()
+        b.synchronize()
+        out[f"{g}x{w}"] = a.elapsed_time(b) / reps
+        L.pbte_sweep_batch_destroy(h)
+    best = min(out, key=out.get)
+    g, w = (int(v) for v in best.split("x"))
+    return {"choice": (g, w), "ms": {k: round(v, 4) for k, v in out.items()}}

@@ -448,32 +448,60 @@ class GsisFixedPoint:
                 if self.wall:
                     _lib.check(L.pbte_wall_flux(ctx, self.vdf.data_ptr(), ofw.data_ptr(), st), "wall_flux")
                 return
-            v = self.vdf.data_ptr()
             _lib.check(L.pbte_sweep_fold_f32(ctx, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(), fw_in.data_ptr(),
-                                             0.0 if self.homogeneous else 1.0, v, st), "sweep_fold_f32")
-            _lib.check(L.pbte_gsis_hot_apply_f32(ctx, ctypes.byref(a.ops), v, float(a.tc5), a.aa_src.data_ptr(), st),
-                       "gsis_hot_apply_f32")
-            if a.wall_all.size:
-                _lib.check(L.pbte_wall_trace_f32(ctx, v, a.tri_fc_fc.data_ptr(), int(a.wall_all.size),
-                                                 a.wall_tri.data_ptr(), a.wall_lfc.data_ptr(), a.wall_mom.data_ptr(),
-                                                 st), "wall_trace_f32")
-            _lib.check(L.pbte_gsis_trace_rhs(ctypes.byref(a.ops), a.aa_src.data_ptr(), a.wall_mom.data_ptr(),
-                                             a.ffa.data_ptr(), a._done_ptr(), st), "gsis_trace_rhs")
-            a.trace_solve(stream)
-            a.recover(a.aa_src, self.uq, stream)
-            # the new moments are the distribution's plus the damped corrections
-            # (correction.py: not the moments of the corrected distribution,
-            # whose flux part differs by tau_C / tau_N); the emission is the
-            # corrected distribution's
-            _lib.check(L.pbte_correct_f32(ctx, v, self.uq.data_ptr(), a.tri_hmin.data_ptr(),
-                                          float(s.case.flow.tau_thr), int(a.use_hmin), ots.data_ptr(),
-                                          oqxs.data_ptr(), oqys.data_ptr(), st), "correct_f32")
-            if self.wall:
-                m = self.scratch_mom
-                _lib.check(L.pbte_fold_epilogue_f32(ctx, v, m[0].data_ptr(), m[1].data_ptr(), m[2].data_ptr(),
-                                                    ofw.data_ptr(), None, None, None, st), "fold_epilogue_f32")
+                                             0.0 if self.homogeneous else 1.0, self.vdf.data_ptr(), st),
+                       "sweep_fold_f32")
+            self._after_sweep32(st, stream)
         finally:
             a.done = keep
+
+    def batch_item(self, done=None) -> "_lib.BatchItem":
+        """The FP32 product's sweep as an item of a batched sweep
+        (``pbte_sweep_batch_*``)."""
+        if self.precision != "fp32":
+            raise ValueError("only the FP32 product sweeps in a batch")
+        ts, qxs, qys, fw, _ = self._views(self.uin)
+        fw_in = fw if fw is not None else self.s.ctx.flux_wall
+        return _lib.BatchItem(self.s.ctx.handle.value, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(),
+                              fw_in.data_ptr(), 0.0 if self.homogeneous else 1.0, self.vdf.data_ptr(),
+                              None if done is None else done.data_ptr())
+
+    def after_sweep(self, st: int, done=None) -> None:
+        """The FP32 product's launches after a batched sweep (the GSIS chain)."""
+        a = self.acc
+        keep, a.done = a.done, done
+        try:
+            self._after_sweep32(st, torch.cuda.current_stream(self.s.device))
+        finally:
+            a.done = keep
+
+    def _after_sweep32(self, st: int, stream) -> None:
+        L = _lib.lib()
+        s, a = self.s, self.acc
+        ctx = s.ctx.handle
+        ots, oqxs, oqys, ofw, _ = self._views(self.uout)
+        v = self.vdf.data_ptr()
+        _lib.check(L.pbte_gsis_hot_apply_f32(ctx, ctypes.byref(a.ops), v, float(a.tc5), a.aa_src.data_ptr(), st),
+                   "gsis_hot_apply_f32")
+        if a.wall_all.size:
+            _lib.check(L.pbte_wall_trace_f32(ctx, v, a.tri_fc_fc.data_ptr(), int(a.wall_all.size),
+                                             a.wall_tri.data_ptr(), a.wall_lfc.data_ptr(), a.wall_mom.data_ptr(),
+                                             st), "wall_trace_f32")
+        _lib.check(L.pbte_gsis_trace_rhs(ctypes.byref(a.ops), a.aa_src.data_ptr(), a.wall_mom.data_ptr(),
+                                         a.ffa.data_ptr(), a._done_ptr(), st), "gsis_trace_rhs")
+        a.trace_solve(stream)
+        a.recover(a.aa_src, self.uq, stream)
+        # the new moments are the distribution's plus the damped corrections
+        # (correction.py: not the moments of the corrected distribution,
+        # whose flux part differs by tau_C / tau_N); the emission is the
+        # corrected distribution's
+        _lib.check(L.pbte_correct_f32(ctx, v, self.uq.data_ptr(), a.tri_hmin.data_ptr(),
+                                      float(s.case.flow.tau_thr), int(a.use_hmin), ots.data_ptr(),
+                                      oqxs.data_ptr(), oqys.data_ptr(), st), "correct_f32")
+        if self.wall:
+            m = self.scratch_mom
+            _lib.check(L.pbte_fold_epilogue_f32(ctx, v, m[0].data_ptr(), m[1].data_ptr(), m[2].data_ptr(),
+                                                ofw.data_ptr(), None, None, None, st), "fold_epilogue_f32")
 
     def _capture(self):
         with device_lock:

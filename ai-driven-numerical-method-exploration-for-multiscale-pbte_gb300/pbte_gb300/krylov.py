@@ -122,6 +122,27 @@ class FixedPointOperator:
                                               ots.data_ptr(), oqxs.data_ptr(), oqys.data_ptr(), p(ofw), *ints, s),
                        "fixed_point_f32")
 
+    def batch_item(self, done=None) -> "_lib.BatchItem":
+        """This FP32 product's sweep as an item of a batched sweep
+        (``pbte_sweep_batch_*``): the inputs are the views of ``uin``, the
+        folded distribution is ``vdf``."""
+        if self.precision == "fp64" or self.per:
+            raise ValueError("only the FP32 product without periodic faces sweeps in a batch")
+        ts, qxs, qys, fw, _ = self._views(self.uin)
+        return _lib.BatchItem(self.s.ctx.handle.value, ts.data_ptr(), qxs.data_ptr(), qys.data_ptr(),
+                              self._ptr(fw), 0.0 if self.homogeneous else 1.0, self.vdf.data_ptr(),
+                              None if done is None else done.data_ptr())
+
+    def after_sweep(self, s: int, done=None) -> None:
+        """The FP32 product's launches after a batched sweep: moments,
+        element integrals and wall emission of the folded distribution."""
+        ots, oqxs, oqys, ofw, _ = self._views(self.uout)
+        ints = (self.temp.data_ptr(), self.qx.data_ptr(), self.qy.data_ptr()) if self.integrals \
+            else (None, None, None)
+        _lib.check(_lib.lib().pbte_fold_epilogue_f32(self.s.ctx.handle, self.vdf.data_ptr(), ots.data_ptr(),
+                                                     oqxs.data_ptr(), oqys.data_ptr(), self._ptr(ofw), *ints, s),
+                   "fold_epilogue_f32")
+
     def _capture(self):
         with device_lock:
             empty_graveyard()
@@ -279,51 +300,59 @@ class ArnoldiGraphs:
         set (the state is the context's stop flag meanwhile)."""
         L = _lib.lib()
         s = torch.cuda.current_stream().cuda_stream
-        n, ctx, op = self.n, self.op.s.ctx.handle, self.op
+        ctx, op = self.op.s.ctx.handle, self.op
         if self.native_columns and not bounded and self.precond is None:
             if getattr(self, "_desc", None) is None:
                 self._desc = self._cycle_desc()
             if self._desc is not None:
                 _lib.check(L.pbte_gmres_columns_f32(ctx, ctypes.byref(self._desc), j0, j1, s), "gmres_columns_f32")
                 return
-        g = self.g.data_ptr() if self.g is not None else None
-        ldq = self.Q.stride(0)
         _lib.check(L.pbte_set_done_flag(ctx, self.state.data_ptr()), "set_done_flag")
         try:
             for j in range(j0, j1):
                 op._launch(s, done=self.state)
-                if self.precond is not None:
-                    # w = M (q_j - (F(q_j) - g)), then CGS2 in place
-                    v = self.Q[j] - (op.uout[:n] - (self.g if self.g is not None else 0.0))
-                    self.w.copy_(self.precond(v))
-                    _lib.check(L.pbte_cgs2(self.Q.data_ptr(), ldq, j + 1, self.w.data_ptr(), n, self.h.data_ptr(),
-                                           self.scratch.data_ptr(), self.scratch.numel(), s), "cgs2")
-                    _lib.check(L.pbte_gmres_givens_bounded(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap,
-                                                           self.cs.data_ptr(), self.sn.data_ptr(),
-                                                           self.gam.data_ptr(), self.tol.data_ptr(),
-                                                           self.state.data_ptr(), self.hist.data_ptr(), s),
-                               "gmres_givens_bounded")
-                elif self.dtype == torch.float64:
-                    _lib.check(L.pbte_arnoldi_column_givens(
-                        self.Q.data_ptr(), ldq, j + 1, op.uout.data_ptr(), g, self.w.data_ptr(), n,
-                        self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(), self.R.data_ptr(),
-                        self.m_cap, self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(), self.tol.data_ptr(),
-                        self.state.data_ptr(), self.hist.data_ptr(), int(bounded), s), "arnoldi_column_givens")
-                else:
-                    _lib.check(L.pbte_arnoldi_column_f32(self.Q.data_ptr(), ldq, j + 1, op.uout.data_ptr(), g,
-                                                         self.w.data_ptr(), n, self.h.data_ptr(),
-                                                         self.scratch.data_ptr(), self.scratch.numel(),
-                                                         self.state.data_ptr(), s), "arnoldi_column_f32")
-                    giv = L.pbte_gmres_givens_bounded if bounded else L.pbte_gmres_givens
-                    _lib.check(giv(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap, self.cs.data_ptr(),
-                                   self.sn.data_ptr(), self.gam.data_ptr(), self.tol.data_ptr(),
-                                   self.state.data_ptr(), self.hist.data_ptr(), s), "gmres_givens")
-                nb = L.pbte_gmres_next_basis_f32 if self.dtype == torch.float32 else L.pbte_gmres_next_basis
-                if j + 1 < self.m_cap:
-                    _lib.check(nb(j, self.w.data_ptr(), self.h.data_ptr(), self.Q.data_ptr(), ldq,
-                                  op.uin.data_ptr(), n, self.state.data_ptr(), s), "gmres_next_basis")
+                self.column_tail(j, s, bounded)
         finally:
             _lib.check(L.pbte_set_done_flag(ctx, None), "set_done_flag")
+
+    def column_tail(self, j: int, s: int, bounded: bool = False) -> None:
+        """Column j after its product is in the operator's output: w (with
+        the preconditioner, if any), CGS2, the rotation with the stopping
+        tests, and the next basis vector; all skipped on the device once the
+        stop state is set."""
+        L = _lib.lib()
+        op, n = self.op, self.n
+        g = self.g.data_ptr() if self.g is not None else None
+        ldq = self.Q.stride(0)
+        if self.precond is not None:
+            # w = M (q_j - (F(q_j) - g)), then CGS2 in place
+            v = self.Q[j] - (op.uout[:n] - (self.g if self.g is not None else 0.0))
+            self.w.copy_(self.precond(v))
+            _lib.check(L.pbte_cgs2(self.Q.data_ptr(), ldq, j + 1, self.w.data_ptr(), n, self.h.data_ptr(),
+                                   self.scratch.data_ptr(), self.scratch.numel(), s), "cgs2")
+            _lib.check(L.pbte_gmres_givens_bounded(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap,
+                                                   self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(),
+                                                   self.tol.data_ptr(), self.state.data_ptr(),
+                                                   self.hist.data_ptr(), s), "gmres_givens_bounded")
+        elif self.dtype == torch.float64:
+            _lib.check(L.pbte_arnoldi_column_givens(
+                self.Q.data_ptr(), ldq, j + 1, op.uout.data_ptr(), g, self.w.data_ptr(), n,
+                self.h.data_ptr(), self.scratch.data_ptr(), self.scratch.numel(), self.R.data_ptr(),
+                self.m_cap, self.cs.data_ptr(), self.sn.data_ptr(), self.gam.data_ptr(), self.tol.data_ptr(),
+                self.state.data_ptr(), self.hist.data_ptr(), int(bounded), s), "arnoldi_column_givens")
+        else:
+            _lib.check(L.pbte_arnoldi_column_f32(self.Q.data_ptr(), ldq, j + 1, op.uout.data_ptr(), g,
+                                                 self.w.data_ptr(), n, self.h.data_ptr(),
+                                                 self.scratch.data_ptr(), self.scratch.numel(),
+                                                 self.state.data_ptr(), s), "arnoldi_column_f32")
+            giv = L.pbte_gmres_givens_bounded if bounded else L.pbte_gmres_givens
+            _lib.check(giv(j, self.h.data_ptr(), self.R.data_ptr(), self.m_cap, self.cs.data_ptr(),
+                           self.sn.data_ptr(), self.gam.data_ptr(), self.tol.data_ptr(),
+                           self.state.data_ptr(), self.hist.data_ptr(), s), "gmres_givens")
+        nb = L.pbte_gmres_next_basis_f32 if self.dtype == torch.float32 else L.pbte_gmres_next_basis
+        if j + 1 < self.m_cap:
+            _lib.check(nb(j, self.w.data_ptr(), self.h.data_ptr(), self.Q.data_ptr(), ldq,
+                          op.uin.data_ptr(), n, self.state.data_ptr(), s), "gmres_next_basis")
 
     def _chunk(self, j0: int, j1: int, bounded: bool):
         key = (j0, j1, bounded)
@@ -349,6 +378,26 @@ class ArnoldiGraphs:
         stop state (0 none, 1 converged, 2 breakdown, 3 halted), the k x k
         triangular factor, the k + 1 residual estimates, the k residual norms
         and the extension's first product under ``enough`` (-1: none)."""
+        bounded = rule is not None
+        self.begin_cycle(r, beta, tol_abs, rule)
+        step = 1 if self.precond is not None else self.CHUNK
+        for j0 in range(0, m, step):
+            j1 = min(m, j0 + step)
+            g = self._chunk(j0, j1, bounded)
+            if g is not None:
+                g.replay()
+            else:
+                self._record_cycle(j0, j1, bounded)
+            self.state_host.copy_(self.state, non_blocking=True)
+            torch.cuda.current_stream().synchronize()
+            if int(self.state_host[0]) != 0:
+                break
+        return self.end_cycle()
+
+    def begin_cycle(self, r: torch.Tensor, beta: float, tol_abs: float, rule=None) -> None:
+        """A cycle's start on the current stream: q_0 = r / beta (also the
+        operator's input), the residual estimates, the tolerances and the
+        stop state (``rule``: see :meth:`cycle`)."""
         self._cycle_buffers()
         n = self.n
         bounded = rule is not None
@@ -362,24 +411,17 @@ class ArnoldiGraphs:
         self.state_host.copy_(torch.tensor([0, 0, rule[1] if bounded else 0, rule[2] if bounded else -1],
                                            dtype=torch.int32))
         self.state.copy_(self.state_host, non_blocking=True)
-        step = 1 if self.precond is not None else self.CHUNK
-        for j0 in range(0, m, step):
-            j1 = min(m, j0 + step)
-            g = self._chunk(j0, j1, bounded)
-            if g is not None:
-                g.replay()
-            else:
-                self._record_cycle(j0, j1, bounded)
-            self.state_host.copy_(self.state, non_blocking=True)
-            torch.cuda.current_stream().synchronize()
-            if int(self.state_host[0]) != 0:
-                break
-        k = int(self.state_host[1])
+
+    def end_cycle(self):
+        """``(k, stop, R, gam, hist, reached)`` of the finished cycle (reads
+        the device state; synchronises)."""
+        st = self.state.cpu()
+        k = int(st[1])
         R = self.R[:k, :k].cpu().numpy().T.copy()
         gam = self.gam[:k + 1].cpu().numpy()
         hist = self.hist[:k].cpu().numpy()
         self.op.sweeps += k
-        return k, int(self.state_host[0]), R, gam, hist, int(self.state_host[3])
+        return k, int(st[0]), R, gam, hist, int(st[3])
 
     def capture_all(self) -> None:
         """Capture every chunk of a full device cycle now (capturing

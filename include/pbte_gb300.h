@@ -422,6 +422,33 @@ int pbte_gsis_trace_rhs(const pbte_gsis_ops *ops, const double *aa_src, const do
 int pbte_gsis_local_recover(const pbte_gsis_ops *ops, const double *aa_src, const double *u_trace, double *uq,
                             const int32_t *done, void *stream);
 
+/* ---- many cases' folded FP32 sweeps in one launch per DG order ----------
+ * (no reference counterpart: pybte solves one case at a time; the batched
+ * solves of many uneven cases).  A batch is made once for a fixed set of
+ * cases and buffers; each run launches, per case, the moment sources of its
+ * ts/qxs/qys (when with_sources != 0; the context's stop flag applies), then
+ * ONE ring-sweep kernel per DG order present, whose blocks are the distinct
+ * velocities of all that order's cases: each block sweeps one velocity of
+ * one case, exactly as pbte_sweep_fold_f32 does it alone (same arithmetic,
+ * same results).  A case whose `done` flag (device int, may be NULL) is
+ * nonzero is skipped.  groups x width is the block shape (thread groups of
+ * 64 or 128 threads, 1 to 8 groups; P3 uses groups of 64, at most 4): the
+ * autotuner's knob.  All cases on one device, no periodic faces, P1-P3.
+ * Creating a batch allocates its case table on the device; runs allocate
+ * nothing. */
+typedef struct pbte_sweep_batch pbte_sweep_batch;
+typedef struct {
+    pbte_ctx *ctx;
+    const double *ts, *qxs, *qys, *flux_wall;   /* flux_wall may be NULL without adiabatic walls */
+    double wall_scale;
+    float *vdf32;                               /* folded rows: [n_udir][n_tris][ndof] */
+    const int32_t *done;
+} pbte_batch_item;
+int pbte_sweep_batch_create(int32_t n, const pbte_batch_item *items, int32_t groups, int32_t width,
+                            pbte_sweep_batch **out);
+int pbte_sweep_batch_run(pbte_sweep_batch *batch, int with_sources, void *stream);
+int pbte_sweep_batch_destroy(pbte_sweep_batch *batch);
+
 /* The FP32 GSIS product of the mixed-precision GSIS solve (no reference
  * counterpart: the inner operator of an FP64 defect correction around
  * Acceleration.apply, acceleration/__init__.py:95-115).  The distribution
