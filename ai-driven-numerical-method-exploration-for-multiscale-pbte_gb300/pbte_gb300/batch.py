@@ -122,7 +122,7 @@ class LockstepBatch:
     CHUNK = 10
 
     def __init__(self, solvers: list[Solver], shape: tuple[int, int] = (4, 128), use_graphs: bool = True,
-                 opts=None):
+                 opts=None, lanes: int = 16):
         from . import _lib
         from .krylov import FixedPointOperator, basis_cap, cached
         from .mixed import MixedOptions
@@ -162,6 +162,7 @@ class LockstepBatch:
         self.handle = h
         self.graphs = {}
         self.stream = torch.cuda.Stream(device=self.device)
+        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(min(lanes, len(self.cases)))]
         self.wall_clock = 0.0
 
     def __del__(self):
@@ -173,18 +174,36 @@ class LockstepBatch:
 
     # -- one chunk of columns of every case's cycle ----------------------------
     def _record(self, j0: int, j1: int) -> None:
+        """Columns j0..j1-1 of every case: the batched sweep on the current
+        stream, then each case's remaining launches of the column on one of
+        ``self.lanes`` side streams (forked from and joined back to the
+        current stream: in a captured chunk they are parallel branches, so
+        the small latency-bound kernels of different cases overlap)."""
         from . import _lib
         L = _lib.lib()
-        s = torch.cuda.current_stream().cuda_stream
+        main = torch.cuda.current_stream()
+        s = main.cuda_stream
         for k in self.cases:
             _lib.check(L.pbte_set_done_flag(k["s"].ctx.handle, k["ar"].state.data_ptr()), "set_done_flag")
         try:
             for j in range(j0, j1):
                 _lib.check(L.pbte_sweep_batch_run(self.handle, 1, s), "sweep_batch_run")
-                for k in self.cases:
-                    if j < k["cap"]:
-                        k["op32"].after_sweep(s, done=k["ar"].state)
-                        k["ar"].column_tail(j, s)
+                swept = torch.cuda.Event()
+                swept.record(main)
+                used = set()
+                for i, k in enumerate(self.cases):
+                    if j >= k["cap"]:
+                        continue
+                    lane = self.lanes[i % len(self.lanes)]
+                    if id(lane) not in used:
+                        lane.wait_event(swept)
+                        used.add(id(lane))
+                    with torch.cuda.stream(lane):
+                        k["op32"].after_sweep(lane.cuda_stream, done=k["ar"].state)
+                        k["ar"].column_tail(j, lane.cuda_stream)
+                for lane in self.lanes:
+                    if id(lane) in used:
+                        main.wait_stream(lane)
         finally:
             for k in self.cases:
                 _lib.check(L.pbte_set_done_flag(k["s"].ctx.handle, None), "set_done_flag")
