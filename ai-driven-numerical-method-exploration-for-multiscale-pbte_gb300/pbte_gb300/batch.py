@@ -105,14 +105,17 @@ class LockstepBatch:
     Each case runs the defect correction of :func:`pbte_gb300.mixed.run_mixed`
     (FP64 defects; one inner GMRES cycle per outer step on FP32 products --
     source-iteration steps for CIS/GMRES cases, GSIS steps for GSIS cases).
-    The cases' outer steps go in lockstep: all FP64 defects, then the inner
-    cycles column by column, where column j of every case is [its moment
-    sources] + one batched sweep (``pbte_sweep_batch_run``: the blocks are
-    the distinct velocities of all cases of an order) + [its epilogue or GSIS
-    chain, CGS2, rotation, next basis vector].  A case whose cycle has stopped
-    (its device stop state) skips the rest of the cycle, and one that has
+    The cases' outer steps go in lockstep (:meth:`step`): all FP64 defects
+    (concurrently, on side streams), then the inner cycles column by column,
+    where column j of every case is [its moment sources] + one batched sweep
+    (``pbte_sweep_batch_run``: the blocks are the distinct velocities of all
+    cases of an order) + [its epilogue or GSIS chain, CGS2, rotation, next
+    basis vector, on a side stream].  A case whose cycle has stopped (its
+    device stop state) skips the rest of the cycle, and one that has
     converged skips everything; the host checks the states once per chunk of
     columns.  With ``use_graphs`` a chunk of all cases is one CUDA graph.
+    Cases can join between steps (:meth:`add`) and leave when done
+    (``step(remove_finished=True)``): continuous batching for a server.
 
     Each case's arithmetic is the one it has alone (the batched sweep gives
     the single sweep's bits), so the results are the solo results.
@@ -121,49 +124,73 @@ class LockstepBatch:
 
     CHUNK = 10
 
-    def __init__(self, solvers: list[Solver], shape: tuple[int, int] = (4, 128), use_graphs: bool = True,
-                 opts=None, lanes: int = 16):
-        from . import _lib
-        from .krylov import FixedPointOperator, basis_cap, cached
+    def __init__(self, solvers: list[Solver] = (), shape: tuple[int, int] = (4, 128), use_graphs: bool = True,
+                 opts=None, lanes: int = 16, device=None):
         from .mixed import MixedOptions
 
-        if not solvers:
-            raise ValueError("empty batch")
-        self.solvers = list(solvers)
-        self.device = self.solvers[0].device
-        if any(s.device != self.device for s in self.solvers):
-            raise ValueError("all solves of a batch run on one device")
-        if any(s.precision != "mixed" for s in self.solvers):
-            raise ValueError("a lockstep batch runs mixed-precision solves")
+        solvers = list(solvers)
+        self.device = solvers[0].device if solvers else torch.device(device or "cuda")
         self.opts = opts or MixedOptions()
         self.use_graphs = use_graphs
         self.shape = shape
         self.cases = []
-        for s in self.solvers:
-            c = s.case
-            if s.acc is not None:
-                from .gsis import GsisFixedPoint
-                op64 = cached(s, "gsis64", lambda s=s: GsisFixedPoint(s, "fp64"))
-                op32 = cached(s, "gsis32h", lambda s=s: GsisFixedPoint(s, "fp32", homogeneous=True))
-            else:
-                op64 = cached(s, "fp64", lambda s=s: FixedPointOperator(s, "fp64"))
-                op32 = cached(s, "fp32h",
-                              lambda s=s: FixedPointOperator(s, "fp32", homogeneous=True, integrals=False))
-            cap = basis_cap(c, op64.n)
-            bdt = torch.float32 if c.performance.inner_basis == "fp32" else torch.float64
-            ar = cached(s, ("arnoldi_inner", cap, bdt, False), lambda o=op32, m=cap, d=bdt: ArnoldiGraphs(o, None, m, d))
-            ar._cycle_buffers()
-            self.cases.append({"s": s, "op64": op64, "op32": op32, "ar": ar, "cap": cap})
-        items = (_lib.BatchItem * len(self.cases))(*[k["op32"].batch_item(k["ar"].state) for k in self.cases])
-        h = ctypes.c_void_p()
-        _lib.check(_lib.lib().pbte_sweep_batch_create(len(self.cases), items, int(shape[0]), int(shape[1]),
-                                                      ctypes.byref(h)), "sweep_batch_create")
-        self._items = items
-        self.handle = h
+        self.handle = None
+        self._dirty = True
         self.graphs = {}
         self.stream = torch.cuda.Stream(device=self.device)
-        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(min(lanes, len(self.cases)))]
+        self.lanes = [torch.cuda.Stream(device=self.device) for _ in range(max(1, lanes))]
         self.wall_clock = 0.0
+        for s in solvers:
+            self.add(s)
+
+    @property
+    def solvers(self) -> list[Solver]:
+        return [k["s"] for k in self.cases]
+
+    def add(self, s: Solver) -> dict:
+        """A mixed-precision solver joins the batch; its solve starts from
+        zero at the next :meth:`step`."""
+        from .krylov import FixedPointOperator, basis_cap, cached
+
+        if s.device != self.device:
+            raise ValueError("all solves of a batch run on one device")
+        if s.precision != "mixed":
+            raise ValueError("a lockstep batch runs mixed-precision solves")
+        c = s.case
+        if s.acc is not None:
+            from .gsis import GsisFixedPoint
+            op64 = cached(s, "gsis64", lambda: GsisFixedPoint(s, "fp64"))
+            op32 = cached(s, "gsis32h", lambda: GsisFixedPoint(s, "fp32", homogeneous=True))
+        else:
+            op64 = cached(s, "fp64", lambda: FixedPointOperator(s, "fp64"))
+            op32 = cached(s, "fp32h", lambda: FixedPointOperator(s, "fp32", homogeneous=True, integrals=False))
+        cap = basis_cap(c, op64.n)
+        bdt = torch.float32 if c.performance.inner_basis == "fp32" else torch.float64
+        ar = cached(s, ("arnoldi_inner", cap, bdt, False), lambda: ArnoldiGraphs(op32, None, cap, dtype=bdt))
+        ar._cycle_buffers()
+        k = {"s": s, "op64": op64, "op32": op32, "ar": ar, "cap": cap, "fresh": True, "done": False,
+             "converged": False}
+        self.cases.append(k)
+        self._dirty = True
+        return k
+
+    def _rebuild(self) -> None:
+        """The batched sweep's case table for the current cases (and no
+        captured chunk: they hold the old membership)."""
+        from . import _lib
+        bury(*self.graphs.values())
+        self.graphs = {}
+        if self.handle is not None and self.handle.value:
+            _lib.lib().pbte_sweep_batch_destroy(self.handle)
+            self.handle = None
+        if self.cases:
+            items = (_lib.BatchItem * len(self.cases))(*[k["op32"].batch_item(k["ar"].state) for k in self.cases])
+            h = ctypes.c_void_p()
+            _lib.check(_lib.lib().pbte_sweep_batch_create(len(self.cases), items, int(self.shape[0]),
+                                                          int(self.shape[1]), ctypes.byref(h)), "sweep_batch_create")
+            self._items = items
+            self.handle = h
+        self._dirty = False
 
     def __del__(self):
         from . import _lib
@@ -223,29 +250,37 @@ class LockstepBatch:
             self.graphs[(j0, j1)] = g
         g.replay()
 
-    def run(self) -> list[RunRecord]:
-        """Solve every case from zero; the records in the solvers' order."""
+    def _lane(self, i: int):
+        return torch.cuda.stream(self.lanes[i % len(self.lanes)])
+
+    def step(self, remove_finished: bool = False) -> list[dict]:
+        """One outer step of every unfinished case: its FP64 defect decides
+        whether it has converged (or reached tmax); the others run one inner
+        cycle in lockstep and update.  Returns the cases that finished in this
+        step (with ``remove_finished`` they also leave the batch)."""
         from .krylov import _solve_upper
 
         o = self.opts
         dev = self.device
-        for k in self.cases:
-            k["s"].reset()
-            k["op64"].sweeps = k["op32"].sweeps = 0
-            k.update(u=torch.zeros(k["op64"].n, dtype=torch.float64, device=dev), history=[], inner=0,
-                     done=False, converged=False)
+        for i, k in enumerate(self.cases):
+            if k["fresh"]:
+                s = k["s"]
+                s.reset()
+                k["op64"].sweeps = k["op32"].sweeps = 0
+                k.update(u=torch.zeros(k["op64"].n, dtype=torch.float64, device=dev), history=[], inner=0,
+                         done=False, converged=False, fresh=False, started=time.perf_counter())
+                with self._lane(i):
+                    k["fu"] = k["op64"].apply(k["u"])
+        live = [(i, k) for i, k in enumerate(self.cases) if not k["done"]]
+        for i, k in live:
+            with self._lane(i):
+                k["nrm"] = torch.stack([torch.linalg.vector_norm(k["fu"] - k["u"]),
+                                        torch.linalg.vector_norm(k["fu"])])
         torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        for k in self.cases:
-            k["fu"] = k["op64"].apply(k["u"])
-        mmax = max(k["cap"] for k in self.cases)
-        for _ in range(o.max_outer):
-            live = [k for k in self.cases if not k["done"]]
-            if not live:
-                break
-            norms = torch.stack([torch.stack([torch.linalg.vector_norm(k["fu"] - k["u"]),
-                                              torch.linalg.vector_norm(k["fu"])]) for k in live]).cpu().numpy()
-            for k, (rn, fn) in zip(live, norms):
+        finished = []
+        if live:
+            norms = torch.stack([k["nrm"] for _, k in live]).cpu().numpy()
+            for (_, k), (rn, fn) in zip(live, norms):
                 fn = float(fn) or 1.0
                 k["rn"] = float(rn)
                 k["history"].append(float(rn) / fn)
@@ -253,45 +288,74 @@ class LockstepBatch:
                     k["done"] = k["converged"] = True
                 elif k["op64"].sweeps + k["inner"] >= k["s"].case.iteration.tmax:
                     k["done"] = True
-            for k in self.cases:
+                if k["done"]:
+                    k["record"] = self._finish(k)
+                    finished.append(k)
+        if remove_finished and finished:
+            self.cases = [k for k in self.cases if not k["done"]]
+            self._dirty = True
+        if not any(not k["done"] for k in self.cases):
+            return finished
+        if self._dirty:
+            self._rebuild()
+        for i, k in enumerate(self.cases):
+            with self._lane(i):
                 if k["done"]:
                     k["ar"].state.fill_(9)            # every launch of this case returns at once
                 else:
-                    r = k["fu"] - k["u"]
-                    k["ar"].begin_cycle(r, k["rn"], o.inner_rtol * k["rn"])
-            if all(k["done"] for k in self.cases):
+                    k["ar"].begin_cycle(k["fu"] - k["u"], k["rn"], o.inner_rtol * k["rn"])
+        torch.cuda.synchronize(dev)
+        mmax = max(k["cap"] for k in self.cases)
+        for j0 in range(0, mmax, self.CHUNK):
+            self._chunk(j0, min(mmax, j0 + self.CHUNK))
+            states = torch.stack([k["ar"].state[0] for k in self.cases]).cpu().numpy()
+            if all(int(v) != 0 or k["done"] or j0 + self.CHUNK >= k["cap"] for v, k in zip(states, self.cases)):
                 break
-            for j0 in range(0, mmax, self.CHUNK):
-                self._chunk(j0, min(mmax, j0 + self.CHUNK))
-                states = torch.stack([k["ar"].state[0] for k in self.cases]).cpu().numpy()
-                if all(int(v) != 0 or k["done"] or j0 + self.CHUNK >= k["cap"]
-                       for v, k in zip(states, self.cases)):
-                    break
-            for k in self.cases:
-                if k["done"]:
-                    continue
-                kk, _, rmat, gam, _, _ = k["ar"].end_cycle()
-                k["inner"] += kk
+        for i, k in enumerate(self.cases):
+            if k["done"]:
+                continue
+            kk, _, rmat, gam, _, _ = k["ar"].end_cycle()
+            k["inner"] += kk
+            with self._lane(i):
                 if kk:
                     ar = k["ar"]
                     y = torch.from_numpy(_solve_upper(rmat, gam[:kk])).to(device=dev, dtype=ar.Q.dtype)
                     k["u"] = k["u"] + (ar.Q[:kk].T @ y).to(torch.float64)
                 k["fu"] = k["op64"].apply(k["u"])
-        torch.cuda.synchronize(dev)
-        self.wall_clock = time.perf_counter() - t0
-        recs = []
-        for k in self.cases:
-            s = k["s"]
+        return finished
+
+    def _finish(self, k) -> RunRecord:
+        s = k["s"]
+        with torch.cuda.stream(self.lanes[0]):
             k["op64"].publish()
-            s64 = k["op64"].sweeps
-            s.ctx.sweep_count += s64 + k["inner"]
-            h = k["history"] or [float("nan")]
-            recs.append(s._record(s64 + k["inner"], k["converged"], np.array(h), np.full(len(h), s.mom.mass),
-                                  self.wall_clock, "GSIS" if s.acc is not None else
-                                  ("KRYLOV" if s.case.scheme.method == "krylov" else "CIS"),
-                                  extra={"fp64_sweeps": s64, "fp32_sweeps": k["inner"], "inner_precision": "fp32",
-                                         "outer_steps": len(h), "final_defect": h[-1], "batched": len(self.cases)}))
-        return recs
+        torch.cuda.synchronize(self.device)
+        s64 = k["op64"].sweeps
+        s.ctx.sweep_count += s64 + k["inner"]
+        h = k["history"] or [float("nan")]
+        return s._record(s64 + k["inner"], k["converged"], np.array(h), np.full(len(h), s.mom.mass),
+                         time.perf_counter() - k["started"], "GSIS" if s.acc is not None else
+                         ("KRYLOV" if s.case.scheme.method == "krylov" else "CIS"),
+                         extra={"fp64_sweeps": s64, "fp32_sweeps": k["inner"], "inner_precision": "fp32",
+                                "outer_steps": len(h), "final_defect": h[-1], "batched": len(self.cases)})
+
+    def run(self) -> list[RunRecord]:
+        """Solve every case of the batch from zero; the records in the
+        solvers' order."""
+        torch.cuda.synchronize(self.device)
+        t0 = time.perf_counter()
+        for k in self.cases:
+            k["fresh"] = True
+        for _ in range(self.opts.max_outer + 1):
+            self.step()
+            if all(k["done"] for k in self.cases):
+                break
+        for k in self.cases:
+            if not k["done"]:
+                k["done"] = True
+                k["record"] = self._finish(k)
+        torch.cuda.synchronize(self.device)
+        self.wall_clock = time.perf_counter() - t0
+        return [k["record"] for k in self.cases]
 
 
 def tune_batch_shape(solvers, shapes=((4, 64), (8, 64), (2, 128), (4, 128)), reps: int = 3) -> dict:

@@ -12,6 +12,14 @@ the same time overlap on the device; each result is the one the case gives
 alone (no buffer is shared between solves, and every kernel is
 deterministic).
 
+With ``mode="lockstep"`` (mixed-precision requests) the admitted solves
+are batched continuously into one :class:`pbte_gb300.batch.LockstepBatch`:
+an engine thread advances every admitted solve by one outer step at a time,
+all their inner FP32 products swept in one launch per DG order; a request
+whose set-up (done on its own host thread) has finished joins the batch at
+the next step, and a finished one leaves it and returns its memory to the
+budget.
+
 Latency of a request = completion time - arrival time (queueing, setup on
 the host and the device, and the solve).
 """
@@ -84,7 +92,11 @@ class Server:
 
     def __init__(self, device: str = "cuda", hbm_budget: float = 150e9, slots: int = 4,
                  ring_shape: tuple[int, int] | None = (4, 64), runner=None, estimator=None,
-                 use_graphs: bool = False):
+                 use_graphs: bool = False, mode: str = "streams", batch_shape: tuple[int, int] = (2, 128)):
+        if mode not in ("streams", "lockstep"):
+            raise ValueError("mode is 'streams' or 'lockstep'")
+        self.mode = mode
+        self.batch_shape = batch_shape
         self.device = torch.device(device)
         self.budget = int(hbm_budget)
         self.slots = int(slots)
@@ -107,8 +119,13 @@ class Server:
         self.t0 = time.perf_counter()
         self.peak_used = 0
         self.peak_running = 0
+        self._ready: list = []          # (ticket, solver) set up and waiting to join the batch
         self._admitter = threading.Thread(target=self._admit_loop, daemon=True)
         self._admitter.start()
+        self._engine = None
+        if mode == "lockstep":
+            self._engine = threading.Thread(target=self._engine_loop, daemon=True)
+            self._engine.start()
 
     def now(self) -> float:
         return time.perf_counter() - self.t0
@@ -132,6 +149,9 @@ class Server:
         with self._lock:
             while self._running:
                 self._lock.wait()
+            self._lock.notify_all()
+        if self._engine is not None:
+            self._engine.join()
 
     # -- admission ---------------------------------------------------------
     def _admit_loop(self) -> None:
@@ -167,7 +187,8 @@ class Server:
                 self.peak_used = max(self.peak_used, self._used)
                 self.peak_running = max(self.peak_running, self._running)
                 t.bytes, t.admitted = need, self.now()
-            threading.Thread(target=self._solve, args=(t, disc), daemon=True).start()
+            target = self._setup if self.mode == "lockstep" else self._solve
+            threading.Thread(target=target, args=(t, disc), daemon=True).start()
 
     def _run_on_device(self, case: Case, disc: Discretisation) -> RunRecord:
         stream = torch.cuda.Stream(device=self.device)
@@ -182,6 +203,58 @@ class Server:
             finally:
                 s.release()
         return rec
+
+    # -- continuous batching ----------------------------------------------------
+    def _setup(self, t: Ticket, disc: Discretisation) -> None:
+        """Host and device set-up of an admitted request on its own thread;
+        the engine adds the solver to the batch at its next step."""
+        try:
+            s = Solver(t.case, device=str(self.device), discretisation=disc)
+            if s.precision != "mixed":
+                raise ValueError("lockstep serving batches mixed-precision solves")
+        except BaseException as e:   # reported on the ticket
+            self._complete(t, error=e)
+            return
+        with self._lock:
+            self._ready.append((t, s))
+            self._lock.notify_all()
+
+    def _complete(self, t: Ticket, record=None, error=None) -> None:
+        t.record, t.error = record, error
+        t.done = self.now()
+        with self._lock:
+            self._running -= 1
+            self._used -= t.bytes
+            self._lock.notify_all()
+        t._event.set()
+
+    def _engine_loop(self) -> None:
+        from .batch import LockstepBatch
+
+        batch = LockstepBatch(shape=self.batch_shape, use_graphs=False, device=self.device)
+        owner = {}
+        while True:
+            with self._lock:
+                while not self._ready and not batch.cases and not (self._closed and self._running == 0):
+                    self._lock.wait()
+                if not self._ready and not batch.cases and self._closed and self._running == 0:
+                    return
+                joining, self._ready = self._ready, []
+            for t, s in joining:
+                k = batch.add(s)
+                owner[id(k)] = t
+            try:
+                finished = batch.step(remove_finished=True)
+            except BaseException as e:   # every solve of the failed step reports it
+                for k in list(batch.cases):
+                    self._complete(owner.pop(id(k)), error=e)
+                    k["s"].release()
+                batch = LockstepBatch(shape=self.batch_shape, use_graphs=False, device=self.device)
+                continue
+            for k in finished:
+                t = owner.pop(id(k))
+                k["s"].release()
+                self._complete(t, record=k["record"])
 
     def _solve(self, t: Ticket, disc: Discretisation) -> None:
         try:
@@ -251,17 +324,26 @@ def main(argv=None) -> int:
     ap.add_argument("--ndirs", default="64,128,256")
     ap.add_argument("--log10-tau", default="-1,1")
     ap.add_argument("--serial-fp64", action="store_true")
+    ap.add_argument("--mode", default="streams", choices=["streams", "lockstep"])
+    ap.add_argument("--batched-draw", action="store_true",
+                    help="draw the requests as the batched workload does (GSIS; every grid, order, "
+                         "ordinate count and Kn_R in [1e-3, 10])")
     a = ap.parse_args(argv)
     ints = lambda s: tuple(int(x) for x in s.split(","))
     lo, hi = (float(x) for x in a.log10_tau.split(","))
-    cases = draw_cases(a.requests, a.seed, ints(a.grids), ints(a.degs), ints(a.ndirs), (lo, hi))
+    if a.batched_draw:
+        from .config import batched_instances
+        cases = batched_instances(a.seed, a.requests)
+    else:
+        cases = draw_cases(a.requests, a.seed, ints(a.grids), ints(a.degs), ints(a.ndirs), (lo, hi))
     gaps = np.random.default_rng(a.seed + 1000).exponential(1.0 / a.rate, size=len(cases))
-    srv = Server(hbm_budget=a.budget_gb * 1e9, slots=a.slots)
+    srv = Server(hbm_budget=a.budget_gb * 1e9, slots=a.slots, mode=a.mode)
     for c, gap in zip(cases, gaps):
         time.sleep(float(gap))
         srv.submit(c)
     srv.close()
-    out = {"requests": a.requests, "rate_per_s": a.rate, "seed": a.seed, "slots": a.slots, **srv.stats()}
+    out = {"requests": a.requests, "rate_per_s": a.rate, "seed": a.seed, "slots": a.slots, "mode": a.mode,
+           **srv.stats()}
     if a.serial_fp64:
         t0 = time.perf_counter()
         lat = []

@@ -98,3 +98,59 @@ def test_results_in_the_mix_equal_results_alone(cuda):
         assert np.array_equal(rec.temp, ref.temp) and np.array_equal(rec.qx, ref.qx)
     st = srv.stats()
     assert st["completed"] == len(cases) and st["peak_concurrent"] >= 2
+
+
+def test_oversized_request_arriving_mid_mix_fails_alone():
+    """A request over the whole budget that arrives while others run is
+    refused at once; the running and later requests complete."""
+    ref = [None]
+    runner = _FakeRunner(ref, hold=0.2)
+    srv = Server(device="cpu", hbm_budget=100, slots=3, runner=runner,
+                 estimator=lambda d, c: 1000 if c.flow.tau_r == 7.0 else 30)
+    ref[0] = srv
+    first = [srv.submit(_small(k)) for k in (10.0, 5.0)]
+    time.sleep(0.05)                            # both running now
+    big = srv.submit(_small(7.0))
+    last = srv.submit(_small(2.0))
+    srv.close()
+    with pytest.raises(MemoryError):
+        big.result(timeout=10)
+    assert big.done < first[0].done             # refused without waiting for the mix
+    assert [t.result(timeout=10) for t in first + [last]] == [10.0, 5.0, 2.0]
+
+
+@pytest.mark.gpu
+def test_continuous_batching_results_equal_results_alone(cuda):
+    """Lockstep serving: requests arriving over time join the running batch
+    between its steps (their FP32 sweeps share the batch's launches), an
+    over-budget request arriving mid-mix is refused alone, and every result
+    equals the case's solo mixed-precision solve bit for bit."""
+    from pbte_gb300 import Solver
+    from pbte_gb300.mixed import run_mixed
+
+    cases = [_small(10.0, deg=1), _small(1.0, deg=2, n=8), _small(0.5, deg=1, n=10),
+             square_case(8, 2, 4, 8, tau_r=0.05, tau_n=0.005, accflag=1, precision="mixed", tol=1e-8,
+                         tmax=4000, krylov_restart=12), _small(2.0, deg=2, n=6, dt=0.3)]
+    alone = []
+    for c in cases:
+        s = Solver(c)
+        alone.append(run_mixed(s))
+        s.release()
+    big = square_case(12, 1, 2, 4, tau_r=1.0, method="krylov", precision="mixed")
+    est = lambda d, c: int(50e9) if c is big else int(estimate_device_bytes(d, c))   # noqa: E731
+    srv = Server(hbm_budget=40e9, slots=4, mode="lockstep", estimator=est)
+    tickets = []
+    for i, c in enumerate(cases):
+        tickets.append(srv.submit(c))
+        if i == 1:
+            refused = srv.submit(big)
+        time.sleep(0.2)
+    srv.close()
+    with pytest.raises(MemoryError):
+        refused.result(timeout=600)
+    for t, ref in zip(tickets, alone):
+        rec = t.result(timeout=600)
+        assert rec.converged
+        assert rec.diagnostics["fp32_sweeps"] == ref.diagnostics["fp32_sweeps"]
+        assert np.array_equal(rec.temp_dofs, ref.temp_dofs) and np.array_equal(rec.qx_dofs, ref.qx_dofs)
+    assert srv.stats()["completed"] == len(cases)
