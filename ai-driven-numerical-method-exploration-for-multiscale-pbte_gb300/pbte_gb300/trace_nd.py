@@ -223,74 +223,127 @@ class NestedDissectionSolver:
         self.delta = torch.zeros(max(d_off, 1), **f64)
 
     # -- factorisation -----------------------------------------------------------
+    #: fronts factorised together: at most this many, and padded to at most
+    #: this factor of the smallest front of the batch
+    BATCH_FRONTS = 512
+    BATCH_PAD = 1.3
+
     def _factor(self, nodes, Kb, KT, b):
         """Fronts assembled and factorised on ``self.device`` (or on the host
         where the device's dense linear-algebra library cannot be loaded); G
-        and H written into their slices of ``Gd`` / ``Hd``."""
+        and H written into their slices of ``Gd`` / ``Hd``.
+
+        The fronts of one tree height are independent, so they are processed
+        in batches of similar size: each front is padded to the batch's
+        largest own and boundary parts (own faces first, padded with an
+        identity block; boundary faces after the batch's own part, padded
+        with zeros), so one batched LU with partial pivoting and a handful of
+        batched products do the work of a front each.  The padding neither
+        changes the pivots (a padding row is zero in every real column) nor
+        the real blocks of G, H and the update passed to the parent."""
         dst = self.device
         dev = _linalg_device(dst)
         f64 = dict(dtype=torch.float64, device=dev)
         n_faces = Kb.shape[0] // b
-        loc = np.full(n_faces, -1, dtype=np.int64)
         kb_data = torch.from_numpy(np.ascontiguousarray(Kb.data)).to(dev)
         kt_data = torch.from_numpy(np.ascontiguousarray(np.transpose(KT.data, (0, 2, 1)))).to(dev)
+        meta = {id(nd): self.meta_host[i] for i, nd in enumerate(nodes)}
         upd = {}
-        for i, nd in enumerate(nodes):
-            _, o, m, g_off, h_off, *_ = (int(v) for v in self.meta_host[i])
-            faces = np.concatenate([nd.own, nd.bnd])
-            nf, no = faces.size, nd.own.size
-            loc[faces] = np.arange(nf)
-            Fp = torch.zeros((nf, nf, b, b), **f64)          # block (front face, front face)
+        by_height = {}
+        for nd in nodes:
+            by_height.setdefault(nd.height, []).append(nd)
+        loc = np.full(n_faces, -1, dtype=np.int64)
+        for h in sorted(by_height):
+            group = sorted(by_height[h], key=lambda nd: nd.own.size + nd.bnd.size)
+            start = 0
+            while start < len(group):
+                m0 = max(1, group[start].own.size + group[start].bnd.size)
+                stop = start + 1
+                while (stop < len(group) and stop - start < self.BATCH_FRONTS
+                       and group[stop].own.size + group[stop].bnd.size <= self.BATCH_PAD * m0):
+                    stop += 1
+                self._factor_batch(group[start:stop], Kb, KT, kb_data, kt_data, b, loc, upd, meta, dev, f64)
+                start = stop
+
+    def _factor_batch(self, batch, Kb, KT, kb_data, kt_data, b, loc, upd, meta, dev, f64):
+        dst = self.device
+        B = len(batch)
+        NO = max(nd.own.size for nd in batch)          # padded own faces
+        NB = max(nd.bnd.size for nd in batch)          # padded boundary faces
+        MF = NO + NB
+        F = torch.zeros((B, MF, MF, b, b), **f64)      # block (front face, front face) of every front
+        kb_b, kb_r, kb_c, kb_e = [], [], [], []
+        kt_b, kt_r, kt_c, kt_e = [], [], [], []
+        ch_b, ch_r, ch_c, ch_v = [], [], [], []
+        for k, nd in enumerate(batch):
+            no = nd.own.size
+            loc[nd.own] = np.arange(no)
+            loc[nd.bnd] = NO + np.arange(nd.bnd.size)
             if no:
                 # blocks K[own, front] from the rows, K[bnd, own] from the columns
                 owner, ent = _ranges(Kb.indptr, nd.own)
                 c = loc[Kb.indices[ent]]
                 keep = np.flatnonzero(c >= 0)
-                Fp.index_put_((torch.from_numpy(owner[keep]).to(dev), torch.from_numpy(c[keep]).to(dev)),
-                              kb_data[torch.from_numpy(ent[keep]).to(dev)], accumulate=True)
+                kb_b.append(np.full(keep.size, k)), kb_r.append(owner[keep]), kb_c.append(c[keep])
+                kb_e.append(ent[keep])
                 owner, ent = _ranges(KT.indptr, nd.own)
                 c = loc[KT.indices[ent]]
-                keep = np.flatnonzero(c >= no)
-                Fp.index_put_((torch.from_numpy(c[keep]).to(dev), torch.from_numpy(owner[keep]).to(dev)),
-                              kt_data[torch.from_numpy(ent[keep]).to(dev)], accumulate=True)
+                keep = np.flatnonzero(c >= NO)
+                kt_b.append(np.full(keep.size, k)), kt_r.append(c[keep]), kt_c.append(owner[keep])
+                kt_e.append(ent[keep])
             for ch in nd.children:
                 S = upd.pop(id(ch))
-                kp = torch.from_numpy(loc[ch.bnd]).to(dev)
-                L = kp.numel()
-                Fp.index_put_((kp[:, None].expand(L, L), kp[None, :].expand(L, L)),
-                              S.view(L, b, L, b).permute(0, 2, 1, 3), accumulate=True)
-            loc[faces] = -1
-            F = Fp.permute(0, 2, 1, 3).reshape(nf * b, nf * b)
-            del Fp
-            F11, F12, F21, F22 = F[:o, :o], F[:o, o:], F[o:, :o], F[o:, o:]
-            Gdst = self.Gd[g_off:g_off + m * o].view(m, o)
-            Hdst = self.Hd[h_off:h_off + o * m].view(o, m)
-            G = Gdst if dev == dst else torch.empty((m, o), **f64)
-            H = Hdst if dev == dst else torch.empty((o, m), **f64)
+                L = ch.bnd.size
+                kp = loc[ch.bnd]
+                ch_b.append(np.full(L * L, k))
+                ch_r.append(np.repeat(kp, L))
+                ch_c.append(np.tile(kp, L))
+                ch_v.append(S.view(L, b, L, b).permute(0, 2, 1, 3).reshape(L * L, b, b))
+            loc[nd.own] = -1
+            loc[nd.bnd] = -1
+        T = lambda parts: torch.from_numpy(np.concatenate(parts)).to(dev)   # noqa: E731
+        if kb_b:
+            F.index_put_((T(kb_b), T(kb_r), T(kb_c)), kb_data[T(kb_e)], accumulate=True)
+            F.index_put_((T(kt_b), T(kt_r), T(kt_c)), kt_data[T(kt_e)], accumulate=True)
+        if ch_b:
+            F.index_put_((T(ch_b), T(ch_r), T(ch_c)), torch.cat(ch_v), accumulate=True)
+        eye_b = torch.eye(b, **f64)
+        for k, nd in enumerate(batch):
+            if nd.own.size < NO:
+                pad = torch.arange(nd.own.size, NO, device=dev)
+                F[k, pad, pad] = eye_b
+        Fm = F.permute(0, 1, 3, 2, 4).reshape(B, MF * b, MF * b)
+        del F
+        o_, m_ = NO * b, MF * b
+        F11, F12, F21, F22 = Fm[:, :o_, :o_], Fm[:, :o_, o_:], Fm[:, o_:, :o_], Fm[:, o_:, o_:]
+        if o_:
+            LU, piv = torch.linalg.lu_factor(F11)
+            P, Lf, Uf = torch.lu_unpack(LU, piv)
+            eye = torch.eye(o_, **f64).expand(B, o_, o_)
+            Linv = torch.linalg.solve_triangular(Lf, eye, upper=False, unitriangular=True)
+            Uinv = torch.linalg.solve_triangular(Uf, eye, upper=True)
+            Gtop = Linv @ P.transpose(-1, -2)                # L11^-1 P^T
+            U12 = Gtop @ F12
+            L21 = F21 @ Uinv
+            S = F22 - L21 @ U12
+            Gbot = -(L21 @ Gtop)
+            Hr = -(Uinv @ U12)
+        else:
+            S = F22.clone()
+        for k, nd in enumerate(batch):
+            i_off, o, m, g_off, h_off = (int(v) for v in meta[id(nd)][:5])
+            mb = m - o
             if o:
-                LU, piv = torch.linalg.lu_factor(F11)
-                perm = np.arange(o)
-                for r, p in enumerate(piv.cpu().numpy() - 1):
-                    perm[r], perm[p] = perm[p], perm[r]
-                eye = torch.eye(o, **f64)
-                Linv = torch.linalg.solve_triangular(LU, eye, upper=False, unitriangular=True)
-                Uinv = torch.linalg.solve_triangular(LU, eye, upper=True)
-                G[:o][:, torch.from_numpy(perm).to(dev)] = Linv      # L11^-1 P
-                U12 = G[:o] @ F12
-                L21 = F21 @ Uinv
-                S = F22 - L21 @ U12
-                H[:, :o] = Uinv
-                if m > o:
-                    G[o:] = -(L21 @ G[:o])
-                    H[:, o:] = -(Uinv @ U12)
-            else:
-                S = F22.clone()
-            if dev != dst:
-                Gdst.copy_(G)
-                Hdst.copy_(H)
+                G = torch.empty((m, o), **f64)
+                H = torch.empty((o, m), **f64)
+                G[:o] = Gtop[k, :o, :o]
+                G[o:] = Gbot[k, :mb, :o]
+                H[:, :o] = Uinv[k, :o, :o]
+                H[:, o:] = Hr[k, :o, :mb]
+                self.Gd[g_off:g_off + m * o].copy_(G.reshape(-1).to(dst))
+                self.Hd[h_off:h_off + o * m].copy_(H.reshape(-1).to(dst))
             if nd.parent is not None:
-                upd[id(nd)] = S.contiguous()
-            del F
+                upd[id(nd)] = S[k, :mb, :mb]
 
     # -- solve -----------------------------------------------------------------
     def solve(self, b: torch.Tensor, out: torch.Tensor | None = None, stream=None, done=None) -> torch.Tensor:
