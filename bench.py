@@ -22,7 +22,12 @@ against its all-FP64 form, and the FP32 sweep's roofline), ``cpu_baseline``
 (the C oracle on the host cores, one solve), ``e2e`` (the public API from
 host arrays: operator upload, solve, results to host), ``latency_ms``,
 ``batched`` (two copies of each case solved concurrently), ``gsis`` (the FP64
-GSIS drop-in's iteration, with the device and with the host trace solve).
+GSIS drop-in's iteration, with the device and with the host trace solve),
+``batched_c4`` (the first ``--c4`` instances of the batched workload: the
+lockstep batch, one sweep launch per DG order for all instances, against the
+same solves in sequence, mixed and FP64) and ``serving_c5`` (``--c5``
+requests of the served workload at Poisson rate ``--c5-rate``: continuous
+batching and one stream per request, against serial FP64 solves).
 
 ``--impl reference`` times the reference algorithm's CPU implementation (the
 C oracle, OpenMP over ordinates on all host cores) on the same sequence of
@@ -310,6 +315,101 @@ def run_c3(dev, peak, kind):
     return out
 
 
+def run_c4(dev, count):
+    """The batched workload's first ``count`` instances (seed 0: grids 16-128,
+    P1-P3, 64-512 ordinates, Kn_R in [1e-3, 10], GSIS, mixed to 1e-8):
+    the lockstep batch (one sweep launch per order for all instances'
+    products, autotuned block shape) against the same mixed solves one after
+    another and against the same solves in FP64 (the Krylov-accelerated GSIS
+    defect correction with FP64 products), all with operators resident."""
+    import torch
+    from pbte_gb300 import Solver
+    from pbte_gb300.batch import LockstepBatch, tune_batch_shape
+    from pbte_gb300.config import batched_instances
+    from pbte_gb300.mixed import MixedOptions, run_mixed
+
+    t0 = time.perf_counter()
+    sol = [Solver(c, device=str(dev)) for c in batched_instances(0, count)]
+    torch.cuda.synchronize(dev)
+    setup = time.perf_counter() - t0
+    tune = tune_batch_shape(sol)
+    batch = LockstepBatch(sol, shape=tune["choice"])
+    batch.run()
+    recs = batch.run()
+    t_batch = batch.wall_clock
+    del batch
+
+    def serial(opts):
+        for s in sol:
+            s.reset()
+            run_mixed(s, opts)
+        torch.cuda.synchronize(dev)
+        t = time.perf_counter()
+        out = []
+        for s in sol:
+            s.reset()
+            out.append(run_mixed(s, opts))
+        torch.cuda.synchronize(dev)
+        return time.perf_counter() - t, out
+
+    t_serial, _ = serial(MixedOptions())
+    t64, r64 = serial(MixedOptions(inner_precision="fp64", inner_rtol=1e-12, refine_tol=1e-12))
+    err = max(field_error(a, b) for a, b in zip(recs, r64))
+    out = {"instances": count, "draw": "config.batched_instances(seed=0), first instances", "setup_s": round(setup, 1),
+           "block_shape": list(tune["choice"]), "tune_ms": tune["ms"],
+           "lockstep": {"value": round(count / t_batch, 4), "unit": "solves/s", "seconds": round(t_batch, 3),
+                        "converged": int(sum(r.converged for r in recs))},
+           "serial_mixed": {"value": round(count / t_serial, 4), "unit": "solves/s", "seconds": round(t_serial, 3)},
+           "serial_fp64": {"value": round(count / t64, 4), "unit": "solves/s", "seconds": round(t64, 3),
+                           "form": "Krylov-accelerated GSIS defect correction with FP64 products"},
+           "speedup_lockstep_over_fp64": round(t64 / t_batch, 3),
+           "err_vs_fp64": float(f"{err:.3e}")}
+    for s in sol:
+        s.release()
+    del sol
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_c5(dev, count, rate):
+    """Serving: ``count`` requests of the seed-1 draw (as the batched
+    workload), Poisson arrivals at ``rate`` per second, 150 GB budget:
+    continuous lockstep batching and one stream per request; latency includes
+    each request's set-up (discretisation, operators, trace factorisation)."""
+    import torch
+    from pbte_gb300 import Solver
+    from pbte_gb300.config import batched_instances
+    from pbte_gb300.mixed import MixedOptions, run_mixed
+    from pbte_gb300.serve import Server
+
+    out = {"requests": count, "rate_per_s": rate, "draw": "config.batched_instances(seed=1)", "budget_gb": 150}
+    gaps = np.random.default_rng(1001).exponential(1.0 / rate, size=count)
+    for mode in ("lockstep", "streams"):
+        srv = Server(device=str(dev), hbm_budget=150e9, slots=8, mode=mode)
+        for c, gap in zip(batched_instances(1, count), gaps):
+            time.sleep(float(gap))
+            srv.submit(c)
+        srv.close()
+        st = srv.stats()
+        out[mode] = {k: (round(v, 3) if isinstance(v, float) else v) for k, v in st.items()}
+    # the same requests one after another in FP64, set-up included
+    t0 = time.perf_counter()
+    lat = []
+    for c in batched_instances(1, count):
+        t1 = time.perf_counter()
+        s = Solver(c, device=str(dev))
+        run_mixed(s, MixedOptions(inner_precision="fp64", inner_rtol=1e-12))
+        torch.cuda.synchronize(dev)
+        s.release()
+        lat.append(time.perf_counter() - t1)
+    span = time.perf_counter() - t0
+    out["serial_fp64"] = {"solves_per_s": round(count / span, 3), "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 1),
+                          "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 1),
+                          "form": "Krylov-accelerated GSIS with FP64 products, set-up included"}
+    torch.cuda.empty_cache()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -319,6 +419,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c3", action="store_true", help="skip the 131 072-triangle solve (~3 minutes)")
     ap.add_argument("--no-methods", action="store_true", help="skip the CIS/GMRES/GSIS method table")
+    ap.add_argument("--c4", type=int, default=16, help="instances of the batched workload (0: skip; 64: all)")
+    ap.add_argument("--c5", type=int, default=16, help="requests of the served workload (0: skip)")
+    ap.add_argument("--c5-rate", type=float, default=1.0, help="Poisson arrivals per second")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
 
@@ -515,11 +618,16 @@ def main():
 
     peak, kind = read_peaks()
     roof = sweep_roofline(solvers[1.0], peak, kind)
-    c3 = None
-    if rank == 0 and not args.no_c3:
+    c3 = c4 = c5 = None
+    if rank == 0:
         del solvers, fp64
         torch.cuda.empty_cache()
-        c3 = run_c3(dev, peak, kind)
+        if not args.no_c3:
+            c3 = run_c3(dev, peak, kind)
+        if args.c4:
+            c4 = run_c4(dev, args.c4)
+        if args.c5:
+            c5 = run_c5(dev, args.c5, args.c5_rate)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         from oracle import oracle as orc
@@ -547,7 +655,8 @@ def main():
                 "per_case": per_case, "c2_methods": methods, "batched": batched, "gsis": gsis,
                 "e2e": {"value": round(e2e, 4), "unit": "solves/s", "h2d_bytes_per_step": int(h2d / len(KN)),
                         "d2h_bytes_per_step": int(d2h / len(KN))},
-                "roofline": roof, "c3": c3, "cpu_baseline": cpu, "clocks": clocks,
+                "roofline": roof, "c3": c3, "batched_c4": c4, "serving_c5": c5, "cpu_baseline": cpu,
+                "clocks": clocks,
                 "gpu_launches": int(launches)}
         print(json.dumps(line), flush=True)
     if dist is not None:
