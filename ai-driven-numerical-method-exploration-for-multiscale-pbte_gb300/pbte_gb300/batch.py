@@ -394,3 +394,34 @@ def tune_batch_shape(solvers, shapes=((4, 64), (8, 64), (2, 128), (4, 128)), rep
     best = min(out, key=out.get)
     g, w = (int(v) for v in best.split("x"))
     return {"choice": (g, w), "ms": {k: round(v, 4) for k, v in out.items()}}
+
+
+def main(argv=None) -> int:
+    """``python -m pbte_gb300.batch --instances N [--seed S] [--runs R]``: the
+    first N instances of the batched workload's draw solved as one lockstep
+    batch (block shape autotuned); one JSON line with the shape timings and
+    the batch's wall clock per run."""
+    import argparse
+    import json
+
+    from .config import batched_instances
+
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--instances", type=int, default=16)
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--runs", type=int, default=2)
+    a = ap.parse_args(argv)
+    solvers = [Solver(c) for c in batched_instances(a.seed, a.instances)]
+    tune = tune_batch_shape(solvers)
+    batch = LockstepBatch(solvers, shape=tune["choice"])
+    walls = []
+    for _ in range(a.runs):
+        recs = batch.run()
+        walls.append(round(batch.wall_clock, 4))
+    print(json.dumps({"instances": a.instances, "seed": a.seed, "shape": list(tune["choice"]), "tune_ms": tune["ms"],
+                      "wall_s": walls, "converged": int(sum(r.converged for r in recs))}), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
