@@ -144,7 +144,11 @@ class ClockSampler:
 # DRAM bytes of one launch of the FP32 ring sweep (dram__bytes_read.sum +
 # dram__bytes_write.sum), by workload (n_tris, ndof, ndir), from the ncu
 # captures summarised under profiles/ (sweep_ring_fp32_*); None elsewhere
-SWEEP_TRAFFIC = {(8192, 6, 256): 7028480 + 1436672}
+SWEEP_TRAFFIC = {(8192, 6, 256): 7028480 + 1436672,
+                 (32768, 6, 512): 61752064 + 375911680,
+                 # the 131 072-triangle sweep, scaled from the 32 768-triangle capture
+                 # by the (velocity, element) pairs: its traffic is the distribution's writes
+                 (131072, 6, 512): 4 * (61752064 + 375911680)}
 
 
 def sweep_roofline(solver, peak, peak_kind, reps=20):
@@ -183,8 +187,10 @@ def sweep_roofline(solver, peak, peak_kind, reps=20):
             "kernel": f"sweep_ring_kernel<float, P{s.case.dg.deg}> (widest level {sch['ring_W']}, "
                       f"{sch['levels']} levels, {sch['unique_dirs']} blocks)",
             "kernel_ms": round(ms, 4), "algorithmic_bytes": int(algo), "peak_source": f"{peak_kind} hbm_gbs",
-            "traffic_source": ("ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same workload"
-                               if traffic is not None else "not captured for this workload")}
+            "traffic_source": ("not captured for this workload" if traffic is None else
+                               "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch at 32768 triangles, "
+                               "x4 (the pairs processed)" if nt == 131072 else
+                               "ncu dram__bytes_read.sum + dram__bytes_write.sum, one launch, same workload")}
 
 
 def cpu_solve(kn, nthreads):
