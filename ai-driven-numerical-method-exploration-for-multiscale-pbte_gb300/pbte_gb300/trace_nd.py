@@ -42,11 +42,13 @@ from . import _lib
 
 __all__ = ["NestedDissectionSolver", "dissect"]
 
-#: output rows of G or H per work item (one thread block of 8 warps): small
-#: enough that the few large fronts near the root still spread over many SMs
-#: (measured on GB300, solve at 8192 / 32768 triangles P2: 4 rows 0.64 /
-#: 2.16 ms, 8 rows 0.57 / 1.87, 16 rows 0.66 / 1.95, 32 rows 0.87 / 2.29)
-ROWS_PER_ITEM = 8
+#: threads per block of the solve kernels, and the work items aimed at per
+#: tree height (measured on GB300, solve at 8192 / 32768 triangles P2:
+#: 608 items 0.414 / 1.15 ms, 912 0.426 / 1.19, 1216 0.435 / 1.19)
+THREADS = 256
+SLOTS = 608
+#: column-group counts a height may use (a power of two, at most 64)
+GROUPS = (1, 2, 4, 8, 16, 32, 64)
 
 
 def _ranges(ptr: np.ndarray, rows: np.ndarray):
@@ -198,12 +200,28 @@ class NestedDissectionSolver:
             h_off += o * m
             d_off += m - o
             c_off += m + 1
+        # work items (node, first row, end row, column groups kc): a block
+        # of 256 threads holds 256 / kc rows, a thread per row and column
+        # group.  Per height the smallest kc of GROUPS that gives at least
+        # SLOTS items, so the few long-row fronts near the root split their
+        # columns over more SMs; a node's rows are cut into even runs.
+        rows = np.array([[mt[2], mt[1]] for mt in meta], dtype=np.int64)   # forward m, backward o
+        h_of = np.array([nd.height for nd in nodes])
+
+        def pieces(r, kc):
+            return -(-r // (THREADS // kc))
+
         fwd = [[] for _ in range(self.height)]
         bwd = [[] for _ in range(self.height)]
-        for i, nd in enumerate(nodes):
-            o, m = meta[i][1], meta[i][2]
-            fwd[nd.height] += [(i, r0, min(m, r0 + ROWS_PER_ITEM), 0) for r0 in range(0, m, ROWS_PER_ITEM)]
-            bwd[nd.height] += [(i, r0, min(o, r0 + ROWS_PER_ITEM), 0) for r0 in range(0, o, ROWS_PER_ITEM)]
+        for h in range(self.height):
+            at = np.flatnonzero(h_of == h)
+            for side, out in ((0, fwd), (1, bwd)):
+                r = rows[at, side]
+                kc = next((k for k in GROUPS if pieces(r, k).sum() >= SLOTS), GROUPS[-1])
+                for i, ri in zip(at, r):
+                    n = int(pieces(ri, kc))
+                    cut = np.linspace(0, ri, n + 1).round().astype(np.int64)
+                    out[h] += [(int(i), int(a), int(c), kc) for a, c in zip(cut[:-1], cut[1:]) if c > a]
         self.levels = []
         for h in range(self.height):
             fo = max((meta[it[0]][1] for it in fwd[h]), default=0)
@@ -336,14 +354,16 @@ class NestedDissectionSolver:
             i_off, o, m, g_off, h_off = (int(v) for v in meta[id(nd)][:5])
             mb = m - o
             if o:
-                G = torch.empty((m, o), **f64)
-                H = torch.empty((o, m), **f64)
-                G[:o] = Gtop[k, :o, :o]
-                G[o:] = Gbot[k, :mb, :o]
-                H[:, :o] = Uinv[k, :o, :o]
-                H[:, o:] = Hr[k, :o, :mb]
-                self.Gd[g_off:g_off + m * o].copy_(G.reshape(-1).to(dst))
-                self.Hd[h_off:h_off + o * m].copy_(H.reshape(-1).to(dst))
+                # stored column-major (G^T: o x m, H^T: m x o), one
+                # output row per thread in the solve kernels
+                Gt = torch.empty((o, m), **f64)
+                Ht = torch.empty((m, o), **f64)
+                Gt[:, :o] = Gtop[k, :o, :o].T
+                Gt[:, o:] = Gbot[k, :mb, :o].T
+                Ht[:o] = Uinv[k, :o, :o].T
+                Ht[o:] = Hr[k, :o, :mb].T
+                self.Gd[g_off:g_off + m * o].copy_(Gt.reshape(-1).to(dst))
+                self.Hd[h_off:h_off + o * m].copy_(Ht.reshape(-1).to(dst))
             if nd.parent is not None:
                 upd[id(nd)] = S[k, :mb, :mb]
 

@@ -489,13 +489,16 @@ int pbte_batched_inverse(const double *a, double *inv, int32_t n, int32_t m, int
  * One height of the forward / backward sweep of a nested-dissection
  * multifrontal solve of K x = b (factors made once on the host,
  * pbte_gb300/trace_nd.py).  items: [n_items][4] int32 (node, first row,
- * end row, 0); meta: [nodes][8] int64 (index offset, own count o, front size
- * m, G offset, H offset, delta offset, contribution-pointer offset, 0); idx:
- * the global unknowns of each front, own first; G: per node m x o,
- * H: o x m, row-major; cptr/csrc: per front position, the delta slots of
- * the children's updates to add.  max_own / max_front: the largest o / m of
- * the items (shared memory, at most 25 600 doubles).  done (optional device
- * flag): every block returns at once while *done != 0. */
+ * end row, column groups kc: a power of two up to 64; at most 256 / kc
+ * rows);
+ * meta: [nodes][8] int64 (index offset, own count o, front size m, G
+ * offset, H offset, delta offset, contribution-pointer offset, 0); idx: the
+ * global unknowns of each front, own first; G: per node m x o, H: o x m,
+ * both column-major; cptr/csrc: per front position, the delta slots of the
+ * children's updates to add.  max_own / max_front: the largest o of the
+ * forward items / m of the backward items (shared memory, at most 25 600
+ * doubles).  done (optional device flag):
+ * every block returns at once while *done != 0. */
 int pbte_nd_forward(const int32_t *items, int32_t n_items, const int64_t *meta, const int32_t *idx,
                     const int64_t *cptr, const int64_t *csrc, const double *G, const double *b, double *z,
                     double *delta, int32_t max_own, const int32_t *done, void *stream);

@@ -53,9 +53,10 @@ def emulate_solve(s: NestedDissectionSolver, rhs: np.ndarray) -> np.ndarray:
     for items, n_items, *_ in s.levels:
         for node, r0, r1, _ in items.numpy()[:n_items]:
             ioff, o, m, goff, _, doff, coff, _ = meta[node]
+            Gt = G[goff:goff + o * m].reshape(o, m)          # G stored column-major
             v = np.array([rhs[idx[ioff + p]] + upd(coff + p) for p in range(o)])
             for r in range(r0, r1):
-                acc = G[goff + r * o:goff + (r + 1) * o] @ v
+                acc = Gt[:, r] @ v
                 if r < o:
                     z[idx[ioff + r]] = acc
                 else:
@@ -63,9 +64,10 @@ def emulate_solve(s: NestedDissectionSolver, rhs: np.ndarray) -> np.ndarray:
     for *_, items, n_items, _ in reversed(s.levels):
         for node, r0, r1, _ in items.numpy()[:n_items]:
             ioff, o, m, _, hoff, _, _, _ = meta[node]
+            Ht = H[hoff:hoff + m * o].reshape(m, o)          # H stored column-major
             w = np.array([z[idx[ioff + p]] if p < o else x[idx[ioff + p]] for p in range(m)])
             for r in range(r0, r1):
-                x[idx[ioff + r]] = H[hoff + r * m:hoff + (r + 1) * m] @ w
+                x[idx[ioff + r]] = Ht[:, r] @ w
     return x
 
 
@@ -109,3 +111,40 @@ def test_dissection_separates_and_covers():
         if len(n.children) == 2:
             a, c = subtree(n.children[0]), subtree(n.children[1])
             assert A[a][:, c].nnz == 0
+
+
+@pytest.mark.parametrize("slots", [1216, 5])
+def test_work_items_cover_every_row_once_within_shared_bounds(monkeypatch, slots):
+    """Every forward row of every front (m rows of G) and every backward row
+    (o rows of H) is in exactly one item of its node's height; an item holds
+    at most 256 / kc rows (kc column groups of a 256-thread block, one kc per
+    height, a power of two up to 64); the shared sizes passed per height cover o (forward) and m
+    (backward).  Few resident blocks give whole 256-row runs at the
+    wide heights, many give split columns everywhere."""
+    import pbte_gb300.trace_nd as tnd
+    monkeypatch.setattr(tnd, "SLOTS", slots)
+    mesh = Discretisation.build(small_case(1, 4, 8, 1.0, 0.1, mesh="cavity:8")).mesh
+    K = trace_pattern_matrix(mesh, 6, seed=5, periodic=False)
+    xy = mesh.nodes[mesh.face_nodes].mean(axis=1)
+    s = NestedDissectionSolver(K, xy, 6, device="cpu", leaf=4, check_tol=None)
+    meta = s.meta.numpy()
+    seen_f = [np.zeros(mt[2], dtype=int) for mt in meta]
+    seen_b = [np.zeros(mt[1], dtype=int) for mt in meta]
+    groups = set()
+    for items_f, nf, fo, items_b, nb, bm in s.levels:
+        for items, n, side in ((items_f, nf, 0), (items_b, nb, 1)):
+            it = items.numpy()[:n]
+            assert len(set(it[:, 3])) == 1 and it[0, 3] in tnd.GROUPS
+            groups.add(int(it[0, 3]))
+            for node, r0, r1, kc in it:
+                assert 0 <= r0 < r1 <= meta[node][2 - side] and r1 - r0 <= tnd.THREADS // kc
+                if side == 0:
+                    assert meta[node][1] <= fo
+                    seen_f[node][r0:r1] += 1
+                else:
+                    assert meta[node][2] <= bm
+                    seen_b[node][r0:r1] += 1
+    assert all((c == 1).all() for c in seen_f) and all((c == 1).all() for c in seen_b)
+    assert (1 in groups) if slots == 5 else groups == {tnd.GROUPS[-1]}
+    rhs = np.random.default_rng(6).standard_normal(K.shape[0])
+    assert np.linalg.norm(K @ emulate_solve(s, rhs) - rhs) <= 1e-12 * np.linalg.norm(rhs)
