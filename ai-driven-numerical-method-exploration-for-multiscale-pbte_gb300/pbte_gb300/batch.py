@@ -258,7 +258,8 @@ class LockstepBatch:
         whether it has converged (or reached tmax); the others run one inner
         cycle in lockstep and update.  Returns the cases that finished in this
         step (with ``remove_finished`` they also leave the batch)."""
-        from .krylov import _solve_upper
+        from .krylov import _solve_upper, amplification
+        from .mixed import refined
 
         o = self.opts
         dev = self.device
@@ -268,23 +269,29 @@ class LockstepBatch:
                 s.reset()
                 k["op64"].sweeps = k["op32"].sweeps = 0
                 k.update(u=torch.zeros(k["op64"].n, dtype=torch.float64, device=dev), history=[], inner=0,
-                         done=False, converged=False, fresh=False, started=time.perf_counter())
+                         done=False, converged=False, fresh=False, started=time.perf_counter(),
+                         kappa=None, dnorm=None)
                 with self._lane(i):
                     k["fu"] = k["op64"].apply(k["u"])
         live = [(i, k) for i, k in enumerate(self.cases) if not k["done"]]
         for i, k in live:
             with self._lane(i):
+                dn = k["dnorm"] if k["dnorm"] is not None else torch.zeros((), dtype=torch.float64, device=dev)
                 k["nrm"] = torch.stack([torch.linalg.vector_norm(k["fu"] - k["u"]),
-                                        torch.linalg.vector_norm(k["fu"])])
+                                        torch.linalg.vector_norm(k["fu"]), dn])
         torch.cuda.synchronize(dev)
         finished = []
         if live:
             norms = torch.stack([k["nrm"] for _, k in live]).cpu().numpy()
-            for (_, k), (rn, fn) in zip(live, norms):
+            for (_, k), (rn, fn, dn) in zip(live, norms):
                 fn = float(fn) or 1.0
+                if k["dnorm"] is not None and k["rn"] > 0:
+                    # the last correction solved (I - T) d = r for the last defect
+                    amp = float(dn) / k["rn"]
+                    k["kappa"] = amp if k["kappa"] is None else max(k["kappa"], amp)
                 k["rn"] = float(rn)
                 k["history"].append(float(rn) / fn)
-                if rn <= o.refine_tol * fn:
+                if refined(float(rn), fn, k["kappa"], o):
                     k["done"] = k["converged"] = True
                 elif k["op64"].sweeps + k["inner"] >= k["s"].case.iteration.tmax:
                     k["done"] = True
@@ -319,8 +326,14 @@ class LockstepBatch:
             with self._lane(i):
                 if kk:
                     ar = k["ar"]
+                    amp = amplification(rmat)
+                    k["kappa"] = amp if k["kappa"] is None else max(k["kappa"], amp)
                     y = torch.from_numpy(_solve_upper(rmat, gam[:kk])).to(device=dev, dtype=ar.Q.dtype)
-                    k["u"] = k["u"] + (ar.Q[:kk].T @ y).to(torch.float64)
+                    d = (ar.Q[:kk].T @ y).to(torch.float64)
+                    k["dnorm"] = torch.linalg.vector_norm(d)
+                    k["u"] = k["u"] + d
+                else:
+                    k["dnorm"] = None
                 k["fu"] = k["op64"].apply(k["u"])
         return finished
 
@@ -336,7 +349,8 @@ class LockstepBatch:
                          time.perf_counter() - k["started"], "GSIS" if s.acc is not None else
                          ("KRYLOV" if s.case.scheme.method == "krylov" else "CIS"),
                          extra={"fp64_sweeps": s64, "fp32_sweeps": k["inner"], "inner_precision": "fp32",
-                                "outer_steps": len(h), "final_defect": h[-1], "batched": len(self.cases)})
+                                "outer_steps": len(h), "final_defect": h[-1], "kappa": k["kappa"],
+                                "batched": len(self.cases)})
 
     def run(self) -> list[RunRecord]:
         """Solve every case of the batch from zero; the records in the

@@ -506,8 +506,19 @@ class Extension:
         return self.reached >= 0 and self.count - self.reached > max(64, self.reached // 4)
 
 
+def amplification(R: np.ndarray) -> float:
+    """``1 / sigma_min`` of a cycle's ``R`` (the Givens-reduced Arnoldi
+    Hessenberg matrix, whose singular values are ``H_k``'s): the norm of
+    ``A^-1`` on the Krylov space the cycle explored, which holds the slow
+    modes GMRES had to resolve."""
+    if R.size == 0:
+        return 0.0
+    smin = float(np.linalg.svd(R, compute_uv=False)[-1])
+    return 1.0 / smin if smin > 0 else float("inf")
+
+
 def gmres(matvec, b: torch.Tensor, arnoldi: ArnoldiGraphs, x0=None, tol_abs: float = 0.0, maxiter=None,
-          rule: Extension | None = None, on_products=None):
+          rule: Extension | None = None, on_products=None, on_cycle=None):
     """Restarted GMRES for ``A x = b`` (``pybte/krylov.py:150-246``) with its
     restart cycles on the device (:meth:`ArnoldiGraphs.cycle`, basis of at
     most ``arnoldi.m_cap`` vectors).  The host forms each restart's residual
@@ -516,7 +527,8 @@ def gmres(matvec, b: torch.Tensor, arnoldi: ArnoldiGraphs, x0=None, tol_abs: flo
     ``Q_k y`` with ``R y = gam``.  ``rule``: the bounded extension, applied to
     the restart residuals here and to the cycle's columns on the device.
     ``on_products(residuals)``: the residual norms of the products just done,
-    in order (a restart's residual, then a cycle's columns).  Returns ``(x,
+    in order (a restart's residual, then a cycle's columns).
+    ``on_cycle(R)``: each cycle's k x k triangular factor.  Returns ``(x,
     converged, products)``."""
     ar = arnoldi
     x = torch.zeros_like(b) if x0 is None else x0.clone()
@@ -551,6 +563,8 @@ def gmres(matvec, b: torch.Tensor, arnoldi: ArnoldiGraphs, x0=None, tol_abs: flo
         if on_products is not None and k:
             on_products(list(hist))
         if k:
+            if on_cycle is not None:
+                on_cycle(rmat)
             y = torch.from_numpy(_solve_upper(rmat, gam[:k])).to(device=b.device, dtype=ar.Q.dtype)
             x += (ar.Q[:k].T @ y).to(x.dtype)
         if stop == 1:

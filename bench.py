@@ -287,7 +287,7 @@ def run_c3(dev, peak, kind):
 
     solve(MixedOptions())                                       # captures the product and cycle graphs
     tm, rm = solve(MixedOptions())
-    fp64_opts = MixedOptions(inner_precision="fp64", inner_rtol=1e-13, refine_tol=1e-13)
+    fp64_opts = MixedOptions(inner_precision="fp64", inner_rtol=1e-13, refine_tol=1e-13, error_tol=0.0)
     solve(fp64_opts)
     t64, r64 = solve(fp64_opts)
     c = s.case
@@ -301,15 +301,16 @@ def run_c3(dev, peak, kind):
     tp = time.perf_counter() - t
     c.iteration.tmax = keep
     out = {"workload": "square 256x256 grid (131072 tri), DG P2, 512 ordinates (8 polar x 64 azimuth), "
-                       "Kn_R=1e-3, Kn_N=1e-4, GSIS, tol 1e-9 (defect 1e-11)",
+                       "Kn_R=1e-3, Kn_N=1e-4, GSIS, mixed solve to an estimated error of 1e-9",
            "setup_s": round(setup, 1),
            "mixed": {"value": round(1.0 / tm, 4), "unit": "solves/s", "seconds": round(tm, 3),
                      "converged": bool(rm.converged), "outer_steps": rm.diagnostics["outer_steps"],
                      "fp32_sweeps": rm.diagnostics["fp32_sweeps"], "fp64_sweeps": rm.diagnostics["fp64_sweeps"],
-                     "final_defect": rm.diagnostics["final_defect"]},
+                     "final_defect": rm.diagnostics["final_defect"], "kappa": rm.diagnostics["kappa"]},
            "fp64": {"value": round(1.0 / t64, 4), "unit": "solves/s", "seconds": round(t64, 3),
                     "converged": bool(r64.converged), "fp64_sweeps": r64.diagnostics["fp64_sweeps"],
-                    "form": "the same Krylov-accelerated GSIS defect correction with FP64 products"},
+                    "form": "the same Krylov-accelerated GSIS defect correction with FP64 products, "
+                            "stopped at a defect of 1e-13 (the mixed solve stops on its error estimate 1e-9)"},
            "err_mixed_vs_fp64": float(f"{field_error(rm, r64):.3e}"),
            "speedup_mixed_over_fp64": round(t64 / tm, 3),
            "plain_fp64_gsis": {"ms_per_iteration": round(1e3 * tp / rp.iterations, 3), "iterations": int(rp.iterations),
@@ -359,7 +360,7 @@ def run_c4(dev, count):
         return time.perf_counter() - t, out
 
     t_serial, _ = serial(MixedOptions())
-    t64, r64 = serial(MixedOptions(inner_precision="fp64", inner_rtol=1e-13, refine_tol=1e-13))
+    t64, r64 = serial(MixedOptions(inner_precision="fp64", inner_rtol=1e-13, refine_tol=1e-13, error_tol=0.0))
     errs = [field_error(a, b) for a, b in zip(recs, r64)]
     err = max(errs)
     worst = int(np.argmax(errs))
@@ -369,7 +370,8 @@ def run_c4(dev, count):
                         "converged": int(sum(r.converged for r in recs))},
            "serial_mixed": {"value": round(count / t_serial, 4), "unit": "solves/s", "seconds": round(t_serial, 3)},
            "serial_fp64": {"value": round(count / t64, 4), "unit": "solves/s", "seconds": round(t64, 3),
-                           "form": "Krylov-accelerated GSIS defect correction with FP64 products"},
+                           "form": "Krylov-accelerated GSIS defect correction with FP64 products, stopped at a "
+                                   "defect of 1e-13 (the mixed solves stop on their error estimate 1e-9)"},
            "speedup_lockstep_over_fp64": round(t64 / t_batch, 3),
            "err_vs_fp64": float(f"{err:.3e}"),
            "worst": {"instance": worst, "converged": bool(recs[worst].converged),
