@@ -106,9 +106,14 @@ def ba_sol_blocks(disc, st, variant):
     std = (interior | ((~interior) & (code == BC_PERIODIC)))[:, :, None, None]
     wall_th = ((~interior) & (code == BC_THERMALISING))[:, :, None, None]
 
+    std_f = std.astype(float)
+    wall_f = wall_th.astype(float)
+
     def put(r, col, v, mask):
+        # the two masks are disjoint and every block starts at zero, so a
+        # masked add is the masked assignment
         sl = (slice(None), slice(None), slice(r * nf, (r + 1) * nf), slice(col * nd, (col + 1) * nd))
-        B[sl] = np.where(mask, v, B[sl])
+        B[sl] += v * (std_f if mask is std else wall_f)
     put(0, 0, 0.5 * bb2, std); put(0, 1, nx / 2.0 / st[0] * bb2, std); put(0, 2, ny / 2.0 / st[0] * bb2, std)
     put(1, 1, 0.5 * bb2, std); put(1, 3, -2.0 * nx / 3.0 / st[1] * bb2, std)
     put(1, 4, -ny / 2.0 / st[1] * bb2, std); put(1, 5, -ny / 2.0 / st[1] * bb2, std)

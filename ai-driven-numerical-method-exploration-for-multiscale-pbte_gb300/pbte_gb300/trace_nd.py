@@ -138,7 +138,7 @@ class NestedDissectionSolver:
         self.block = b
         Kb = sp.bsr_matrix(K, blocksize=(b, b))
         Kb.sort_indices()
-        KT = sp.bsr_matrix(K.T.tocsr(), blocksize=(b, b))
+        KT = Kb.transpose().tobsr(blocksize=(b, b))
         KT.sort_indices()
         rows = np.repeat(np.arange(n_faces), np.diff(Kb.indptr))
         A = sp.coo_matrix((np.ones(rows.size), (rows, Kb.indices)), shape=(n_faces, n_faces)).tocsr()
@@ -327,11 +327,11 @@ class NestedDissectionSolver:
             F.index_put_((T(kt_b), T(kt_r), T(kt_c)), kt_data[T(kt_e)], accumulate=True)
         if ch_b:
             F.index_put_((T(ch_b), T(ch_r), T(ch_c)), torch.cat(ch_v), accumulate=True)
-        eye_b = torch.eye(b, **f64)
-        for k, nd in enumerate(batch):
-            if nd.own.size < NO:
-                pad = torch.arange(nd.own.size, NO, device=dev)
-                F[k, pad, pad] = eye_b
+        # identity blocks on the padded own faces, all fronts at once
+        pad_k = np.concatenate([np.full(NO - nd.own.size, k) for k, nd in enumerate(batch)])
+        if pad_k.size:
+            pad_p = np.concatenate([np.arange(nd.own.size, NO) for nd in batch])
+            F[T([pad_k]), T([pad_p]), T([pad_p])] = torch.eye(b, **f64)
         Fm = F.permute(0, 1, 3, 2, 4).reshape(B, MF * b, MF * b)
         del F
         o_, m_ = NO * b, MF * b
@@ -342,7 +342,10 @@ class NestedDissectionSolver:
             eye = torch.eye(o_, **f64).expand(B, o_, o_)
             Linv = torch.linalg.solve_triangular(Lf, eye, upper=False, unitriangular=True)
             Uinv = torch.linalg.solve_triangular(Uf, eye, upper=True)
-            Gtop = Linv @ P.transpose(-1, -2)                # L11^-1 P^T
+            # L11^-1 P^T: P^T permutes the columns of L11^-1 (column j is
+            # column sigma(j), sigma(j) the column of row j's one in P)
+            sigma = P.argmax(dim=-1)
+            Gtop = torch.gather(Linv, 2, sigma[:, None, :].expand(B, o_, o_))
             U12 = Gtop @ F12
             L21 = F21 @ Uinv
             S = F22 - L21 @ U12
@@ -350,22 +353,54 @@ class NestedDissectionSolver:
             Hr = -(Uinv @ U12)
         else:
             S = F22.clone()
+        mt = np.array([meta[id(nd)][:5] for nd in batch], dtype=np.int64)
+        if o_:
+            # G^T (o x m) and H^T (m x o) of every front, column-major, out of
+            # the padded batch in one gather and one scatter each: front
+            # row r < o is padded row r, boundary row r >= o padded row
+            # o_ + r - o
+            Gfull = torch.cat([Gtop, Gbot], dim=1)                        # (B, m_, o_): G rows
+            Hfull = torch.cat([Uinv, Hr], dim=2)                          # (B, o_, m_): H rows
+            self._scatter_columns(Gfull, mt[:, 1], mt[:, 2], mt[:, 3], o_, True, self.Gd, dev)
+            self._scatter_columns(Hfull, mt[:, 1], mt[:, 2], mt[:, 4], o_, False, self.Hd, dev)
+            del Gfull, Hfull
         for k, nd in enumerate(batch):
-            i_off, o, m, g_off, h_off = (int(v) for v in meta[id(nd)][:5])
-            mb = m - o
-            if o:
-                # stored column-major (G^T: o x m, H^T: m x o), one
-                # output row per thread in the solve kernels
-                Gt = torch.empty((o, m), **f64)
-                Ht = torch.empty((m, o), **f64)
-                Gt[:, :o] = Gtop[k, :o, :o].T
-                Gt[:, o:] = Gbot[k, :mb, :o].T
-                Ht[:o] = Uinv[k, :o, :o].T
-                Ht[o:] = Hr[k, :o, :mb].T
-                self.Gd[g_off:g_off + m * o].copy_(Gt.reshape(-1).to(dst))
-                self.Hd[h_off:h_off + o * m].copy_(Ht.reshape(-1).to(dst))
             if nd.parent is not None:
+                mb = int(mt[k, 2] - mt[k, 1])
                 upd[id(nd)] = S[k, :mb, :mb]
+
+    @staticmethod
+    def _scatter_columns(full, o, m, off, o_, is_g, out, dev):
+        """Write each front's factor column-major into ``out``: G^T[c][r] =
+        G[r][c] at ``off + c * m + r`` (``is_g``; ``full`` (B, m_, o_)), or
+        H^T[r][c] = H[c][r] at ``off + r * o + c`` (``full`` (B, o_, m_))."""
+        size = o * m
+        keep = np.flatnonzero(size > 0)
+        if not keep.size:
+            return
+        starts = np.zeros(keep.size + 1, dtype=np.int64)
+        np.cumsum(size[keep], out=starts[1:])
+        total = int(starts[-1])
+        i64 = dict(dtype=torch.int64, device=dev)
+        t = torch.arange(total, **i64)
+        k = torch.searchsorted(torch.from_numpy(starts[1:]).to(dev), t, right=True)
+        l = t - torch.from_numpy(starts[:-1]).to(dev)[k]
+        ok = torch.from_numpy(o[keep]).to(dev)[k]
+        mk = torch.from_numpy(m[keep]).to(dev)[k]
+        kb = torch.from_numpy(keep).to(dev)[k]
+        dst = torch.from_numpy(off[keep]).to(dev)[k] + l
+        if is_g:
+            c, r = l // mk, l % mk
+        else:
+            r, c = l // ok, l % ok
+        rs = torch.where(r < ok, r, o_ + r - ok)          # the padded front row of front row r
+        B, d1, d2 = full.shape
+        if is_g:
+            src = (kb * d1 + rs) * d2 + c                  # full[kb, rs, c]
+        else:
+            src = (kb * d1 + c) * d2 + rs                  # full[kb, c, rs]
+        vals = full.reshape(-1)[src]
+        out[dst.to(out.device)] = vals.to(out.device)
 
     # -- solve -----------------------------------------------------------------
     def solve(self, b: torch.Tensor, out: torch.Tensor | None = None, stream=None, done=None) -> torch.Tensor:
