@@ -170,77 +170,99 @@ class NestedDissectionSolver:
     # -- device layout -------------------------------------------------------
     def _layout(self, nodes, b):
         dev = self.device
-        comp = np.arange(b)
         n_faces = self.n // b
-        loc = np.full(n_faces, -1, dtype=np.int64)
-        idx, meta, cptr, csrc = [], [], [], []
-        g_off = h_off = d_off = i_off = c_off = n_src = 0
-        delta_off = {}
-        for nd in nodes:
-            faces = np.concatenate([nd.own, nd.bnd])
-            o, m = nd.own.size * b, faces.size * b
-            loc[faces] = np.arange(faces.size)
-            # the children's boundary updates, by front position, children in order
-            tgt = [(loc[ch.bnd][:, None] * b + comp).ravel() for ch in nd.children]
-            src = [delta_off[id(ch)] + np.arange(ch.bnd.size * b) for ch in nd.children]
-            loc[faces] = -1
-            tgt = np.concatenate(tgt) if tgt else np.zeros(0, dtype=np.int64)
-            src = np.concatenate(src) if src else np.zeros(0, dtype=np.int64)
-            srt = np.argsort(tgt, kind="stable")
-            ptr = np.zeros(m + 1, dtype=np.int64)
-            np.cumsum(np.bincount(tgt, minlength=m), out=ptr[1:])
-            meta.append([i_off, o, m, g_off, h_off, d_off, c_off, 0])
-            delta_off[id(nd)] = d_off
-            idx.append((faces[:, None] * b + comp).ravel())
-            cptr.append(ptr + n_src)
-            csrc.append(src[srt])
-            n_src += src.size
-            i_off += m
-            g_off += m * o
-            h_off += o * m
-            d_off += m - o
-            c_off += m + 1
+        N = len(nodes)
+
+        def starts(v):                                   # exclusive prefix sums
+            out = np.zeros(v.size, dtype=np.int64)
+            np.cumsum(v[:-1], out=out[1:])
+            return out
+
+        own_n = np.array([nd.own.size for nd in nodes], dtype=np.int64)
+        fn = own_n + np.array([nd.bnd.size for nd in nodes], dtype=np.int64)   # faces per front
+        o, m = own_n * b, fn * b
+        i_off, g_off, d_off, c_off = starts(m), starts(m * o), starts(m - o), starts(m + 1)
+        faces = np.concatenate([f for nd in nodes for f in (nd.own, nd.bnd)]).astype(np.int64)
+        # the children's boundary updates: child boundary face -> its position
+        # in the parent's front (a sorted (node, face) key), by front position
+        # with the children in order
+        at = {id(nd): i for i, nd in enumerate(nodes)}
+        par = np.array([i for i, nd in enumerate(nodes) for _ in nd.children], dtype=np.int64)
+        kid = np.array([at[id(ch)] for nd in nodes for ch in nd.children], dtype=np.int64)
+        if kid.size:
+            kb = fn[kid] - own_n[kid]                    # boundary faces of each child
+            key = np.repeat(np.arange(N, dtype=np.int64), fn) * n_faces + faces
+            order = np.argsort(key, kind="stable")
+            q = np.repeat(par, kb) * n_faces + np.concatenate([nodes[k].bnd for k in kid]).astype(np.int64)
+            pos = order[np.searchsorted(key[order], q)] - np.repeat(starts(fn)[par], kb)
+            tgt = (pos[:, None] * b + np.arange(b)).ravel()
+            nb = kb * b
+            src = np.repeat(d_off[kid], nb) + (np.arange(nb.sum()) - np.repeat(starts(nb), nb))
+            gkey = np.repeat(i_off[par], nb) + tgt                 # position over all fronts
+            srt = np.argsort(gkey, kind="stable")
+            csrc = src[srt]
+            counts = np.bincount(gkey, minlength=int(m.sum()))
+        else:
+            csrc = np.zeros(0, dtype=np.int64)
+            counts = np.zeros(int(m.sum()), dtype=np.int64)
+        cum = np.zeros(counts.size + 1, dtype=np.int64)
+        np.cumsum(counts, out=cum[1:])
+        n_ptr = int((m + 1).sum())
+        cptr = cum[np.repeat(i_off, m + 1) + (np.arange(n_ptr) - np.repeat(c_off, m + 1))]
+        meta = np.stack([i_off, o, m, g_off, g_off, d_off, c_off, np.zeros(N, dtype=np.int64)], axis=1)
+        idx = (faces[:, None] * b + np.arange(b)).ravel()
+        g_total = int((m * o).sum())
+        d_total = int((m - o).sum())
         # work items (node, first row, end row, column groups kc): a block
         # of 256 threads holds 256 / kc rows, a thread per row and column
         # group.  Per height the smallest kc of GROUPS that gives at least
         # SLOTS items, so the few long-row fronts near the root split their
         # columns over more SMs; a node's rows are cut into even runs.
-        rows = np.array([[mt[2], mt[1]] for mt in meta], dtype=np.int64)   # forward m, backward o
+        rows = np.stack([m, o], axis=1)                                    # forward m, backward o
         h_of = np.array([nd.height for nd in nodes])
 
         def pieces(r, kc):
             return -(-r // (THREADS // kc))
 
-        fwd = [[] for _ in range(self.height)]
-        bwd = [[] for _ in range(self.height)]
-        for h in range(self.height):
-            at = np.flatnonzero(h_of == h)
-            for side, out in ((0, fwd), (1, bwd)):
-                r = rows[at, side]
-                kc = next((k for k in GROUPS if pieces(r, k).sum() >= SLOTS), GROUPS[-1])
-                for i, ri in zip(at, r):
-                    n = int(pieces(ri, kc))
-                    cut = np.linspace(0, ri, n + 1).round().astype(np.int64)
-                    out[h] += [(int(i), int(a), int(c), kc) for a, c in zip(cut[:-1], cut[1:]) if c > a]
+        def cuts(sel, r, kc):
+            # each node's rows cut into n even runs, at round(i * r / n) (the
+            # points of numpy's linspace(0, r, n + 1))
+            n = pieces(r, kc)
+            node = np.repeat(sel, n)
+            i = np.arange(n.sum()) - np.repeat(starts(n), n)
+            step = np.repeat(r / np.maximum(n, 1), n)
+            first = np.round(i * step).astype(np.int64)
+            last = np.where(i + 1 == np.repeat(n, n), np.repeat(r, n), np.round((i + 1) * step).astype(np.int64))
+            keep = last > first
+            items = np.stack([node, first, last, np.full(node.size, kc)], axis=1)[keep]
+            return items.astype(np.int32)
+
         self.levels = []
+        empty = torch.zeros((1, 4), dtype=torch.int32, device=dev)
         for h in range(self.height):
-            fo = max((meta[it[0]][1] for it in fwd[h]), default=0)
-            bm = max((meta[it[0]][2] for it in bwd[h]), default=0)
-            self.levels.append((torch.tensor(fwd[h] or [(0, 0, 0, 0)], dtype=torch.int32, device=dev), len(fwd[h]),
-                                int(fo), torch.tensor(bwd[h] or [(0, 0, 0, 0)], dtype=torch.int32, device=dev),
-                                len(bwd[h]), int(bm)))
+            sel = np.flatnonzero(h_of == h)
+            lv = []
+            for side, width in ((0, o), (1, m)):
+                r = rows[sel, side]
+                kc = next((k for k in GROUPS if pieces(r, k).sum() >= SLOTS), GROUPS[-1])
+                items = cuts(sel, r, kc)
+                # shared memory: the largest o (forward) / m (backward) of the items' nodes
+                big = int(width[np.unique(items[:, 0])].max()) if len(items) else 0
+                lv.append((torch.from_numpy(items).to(dev) if len(items) else empty, len(items), big))
+            (fi, nf_, fo), (bi, nb_, bm) = lv
+            self.levels.append((fi, nf_, fo, bi, nb_, bm))
         f64 = dict(dtype=torch.float64, device=dev)
-        self.meta_host = np.asarray(meta, dtype=np.int64)
+        self.meta_host = np.ascontiguousarray(meta, dtype=np.int64)
         self.meta = torch.from_numpy(self.meta_host).to(dev)
-        self.idx = torch.from_numpy(np.concatenate(idx).astype(np.int32)).to(dev)
-        self.cptr = torch.from_numpy(np.concatenate(cptr)).to(dev)
-        self.csrc = torch.from_numpy(np.concatenate(csrc + [np.zeros(1, np.int64)])).to(dev)
-        self.Gd = torch.empty(max(g_off, 1), **f64)
-        self.Hd = torch.empty(max(h_off, 1), **f64)
-        self.factor_entries = int(g_off + h_off)
-        self.max_front = int(max(mt[2] for mt in meta))
+        self.idx = torch.from_numpy(idx.astype(np.int32)).to(dev)
+        self.cptr = torch.from_numpy(cptr).to(dev)
+        self.csrc = torch.from_numpy(np.concatenate([csrc, np.zeros(1, np.int64)])).to(dev)
+        self.Gd = torch.empty(max(g_total, 1), **f64)
+        self.Hd = torch.empty(max(g_total, 1), **f64)
+        self.factor_entries = 2 * g_total
+        self.max_front = int(m.max())
         self.z = torch.zeros(self.n, **f64)
-        self.delta = torch.zeros(max(d_off, 1), **f64)
+        self.delta = torch.zeros(max(d_total, 1), **f64)
 
     # -- factorisation -----------------------------------------------------------
     #: fronts factorised together: at most this many, and padded to at most
