@@ -347,8 +347,13 @@ def main(argv=None) -> int:
     if a.serial_fp64:
         t0 = time.perf_counter()
         lat = []
-        for c in draw_cases(a.requests, a.seed, ints(a.grids), ints(a.degs), ints(a.ndirs), (lo, hi),
-                            precision="fp64"):
+        if a.batched_draw:
+            from .config import batched_instances
+            cases64 = batched_instances(a.seed, a.requests, precision="fp64")
+        else:
+            cases64 = draw_cases(a.requests, a.seed, ints(a.grids), ints(a.degs), ints(a.ndirs), (lo, hi),
+                                 precision="fp64")
+        for c in cases64:
             t1 = time.perf_counter()
             s = Solver(c)
             s.use_graphs = srv.use_graphs
