@@ -24,11 +24,15 @@ relaxation times, so it is factorised once, by nested dissection:
   ``G = [L11^-1 P ; -L21 L11^-1 P]`` maps the node's own right-hand side to
   its forward values and the update of its boundary, and
   ``H = [U11^-1, -U11^-1 U12]`` maps ``[forward values, x of the boundary]``
-  to the node's unknowns.
+  to the node's unknowns.  Both are stored column-major, so that the solve
+  kernels give each output row a thread and read the rows of a column
+  coalesced.
 
 The solve (``pbte_nd_forward`` / ``pbte_nd_backward``) walks the tree by
-height, one launch per height and direction; a node's right-hand side adds
-its children's updates in a fixed order, so the result is deterministic.
+height, one launch per height and direction, over work items of a front's
+rows and a count of column groups; a node's right-hand side adds its
+children's updates in a fixed order and the column groups' partial sums
+are added by a fixed tree, so the result is deterministic.
 At setup the device solve of a random right-hand side is checked against
 ``K`` (relative residual below ``check_tol``).
 """
